@@ -1,0 +1,374 @@
+#!/usr/bin/env python
+'''
+Benchmark of the block-sparse contraction path: the two-site DMRG effective-Hamiltonian matvec
+`einsum('EPaqj,JRSFb,AQsb->EPrf', head, tail, theta)` of a U(1) spin-1/2 Heisenberg chain at bond
+chi = 256 (17 Sz sectors q = -8..8 with multiplets ~ exp(-q^2/8) summing to 256, MPO bond w = 5,
+physical d = 2, theta in the Sz = 0 sector), inputs N(0, 1) float64 from a seed.
+
+A step is one matvec through the public API, with the operator (head, tail) prepared once as a
+Lanczos window uses it and a different resident vector every step.  L2 (129 MB) is flushed between
+timed steps by writing a 256 MB buffer, and each step is timed alone with CUDA events on the
+launching stream.  Prints ONE JSON line (rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P] [--impl reference]
+
+--impl reference times the reference's CPU path for the same workload on the host cores: the
+oracle port of tentorch's einsum (oracle/engine.py), a bounded sample of matvecs.  With N > 1 (one
+process per GPU under torchrun) every rank runs an independent replica; the path has no exchange
+between windows, so there is no collective on the data path.
+'''
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = 'DMRG s/sweep & matvecs/s (U(1) χ=256) vs plain FP64 on same GPU at ΔE≤1e-10'
+WORKLOAD = 'u1_heisenberg_twosite_matvec_chi256'
+CHI = 256
+SEED = 0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type = int, default = 1)
+    p.add_argument('--steps', type = int, default = 1000)
+    p.add_argument('--warmup', type = int, default = 10)
+    p.add_argument('--impl', default = 'gb300', choices = ['gb300', 'reference'])
+    p.add_argument('--precision', type = int, default = 0, help = '0: FP64 block products; k: bf16 slices')
+    p.add_argument('--chi', type = int, default = CHI)
+    p.add_argument('--cpu-sample', type = int, default = 20, help = 'matvecs in the CPU baseline sample')
+    return p.parse_args()
+
+
+def config(args, precision):
+    return {'workload': WORKLOAD, 'chi': args.chi, 'sectors': 17, 'mpo_bond': 5, 'physical': 2,
+            'equation': 'EPaqj,JRSFb,AQsb->EPrf', 'block_products': 'fp64' if precision == 0 else f'bf16x{precision} split',
+            'l2': 'flushed between timed steps (256 MB write)', 'inputs': f'N(0,1) float64, seed {SEED}',
+            'parallelism': f'replicas x{args.gpus}'}
+
+
+# ---------------------------------------------------------------------------------------------
+# the CPU baseline (oracle port of the reference's einsum)
+# ---------------------------------------------------------------------------------------------
+
+
+def cpu_matvecs(chi, count):
+    '''Time `count` matvecs of the oracle on the host after one untimed call that builds its
+    plans; returns (matvecs/s, seconds, count).'''
+    from oracle import engine as orc
+    head, tail, theta = orc.matvec_inputs(chi, seed = SEED)
+    orc.einsum(orc.MATVEC, head, tail, theta)
+    start = time.perf_counter()
+    for _ in range(count):
+        orc.einsum(orc.MATVEC, head, tail, theta)
+    elapsed = time.perf_counter() - start
+    return count / elapsed, elapsed, count
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    count = max(1, min(args.steps, args.cpu_sample))
+    value, elapsed, n = cpu_matvecs(args.chi, count)
+    cores = os.cpu_count()
+    line = {'metric': METRIC, 'value': value, 'unit': 'matvecs/s', 'n_gpus': args.gpus, 'steps': n,
+            'warmup': 1, 'ms_per_step': 1e3 * elapsed / n, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
+            'config': config(args, 0),
+            'cpu_baseline': {'value': value, 'unit': 'matvecs/s', 'cores': cores, 'kind': 'port',
+                             'sample': f'{n} matvecs of the oracle port of tentorch einsum (numpy; scatter '
+                                       f'single-threaded, block products on {cores} BLAS threads)'},
+            'e2e': {'value': value, 'unit': 'matvecs/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush = True)
+
+
+# ---------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------------------------
+
+
+class Clocks:
+    FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(index), f'--query-gpu={self.FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout = subprocess.PIPE, stderr = subprocess.DEVNULL, text = True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout = 10)
+        sm, sm_max, reasons = [], [], set()
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+        for row in out.strip().splitlines():
+            parts = [x.strip() for x in row.split(',')]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                sm_max.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower().startswith('active'):
+                    reasons.add(name)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': max(sm_max) if sm_max else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ---------------------------------------------------------------------------------------------
+# the GPU arm
+# ---------------------------------------------------------------------------------------------
+
+
+def fp64_peak_tflops(torch, device):
+    '''cuBLAS DGEMM 4096^3, best of 3: the FP64 roofline denominator (not in MEASURED_PEAKS.json).'''
+    a = torch.randn(4096, 4096, dtype = torch.float64, device = device)
+    b = torch.randn(4096, 4096, dtype = torch.float64, device = device)
+    torch.matmul(a, b)
+    torch.cuda.synchronize(device)
+    best = float('inf')
+    for _ in range(3):
+        s, e = torch.cuda.Event(enable_timing = True), torch.cuda.Event(enable_timing = True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def measured_peaks():
+    path = os.path.join(HERE, 'MEASURED_PEAKS.json')
+    if os.path.exists(path):
+        with open(path) as handle:
+            return json.load(handle), 'measured'
+    return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}, 'fallback'
+
+
+def ncu_traffic(kernel):
+    '''Per-launch DRAM bytes of a kernel from the committed ncu summary, or None.'''
+    path = os.path.join(HERE, 'profiles', 'traffic.json')
+    if not os.path.exists(path):
+        return None
+    with open(path) as handle:
+        return json.load(handle).get(kernel)
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import torch.distributed as dist
+
+    import tentorch_gb300 as tg
+    from oracle import engine as orc
+    from tentorch_gb300 import _lib
+
+    local = int(os.environ.get('LOCAL_RANK', 0))
+    torch.cuda.set_device(local)
+    device = torch.device('cuda', local)
+
+    def product(t):
+        legs = lambda ls: [tg.Leg(tg.u1, list(l.sectors), list(l.multiplicities)) for l in ls]
+        out = tg.Tensor(tg.u1, legs(t.codomain), legs(t.domain), t.qtotal, dtype = torch.float64, device = device)
+        for key, block in t.blocks.items():
+            out.block(*key).copy_(torch.from_numpy(block))
+        return out
+
+    head_o, tail_o, theta_o = orc.matvec_inputs(args.chi, seed = SEED + rank)
+    head, tail = product(head_o), product(tail_o)
+    gen = torch.Generator(device = device).manual_seed(SEED + 17 + rank)
+    vectors = []
+    for _ in range(4):
+        v = product(theta_o)
+        v.data.copy_(torch.randn(v.data.shape, dtype = torch.float64, device = device, generator = gen))
+        vectors.append(v)
+    plan = tg.linalg.plan_of(orc.MATVEC, head, tail, vectors[0])
+    flush = torch.empty(64 * 1024 * 1024, dtype = torch.float32, device = device)  # 256 MB > L2
+    stream = torch.cuda.current_stream(device)
+
+    def timed_loop(steps, precision, fn):
+        tg.set_precision(precision)
+        starts = [torch.cuda.Event(enable_timing = True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing = True) for _ in range(steps)]
+        for i in range(steps):
+            flush.zero_()
+            starts[i].record(stream)
+            fn(i)
+            ends[i].record(stream)
+        torch.cuda.synchronize(device)
+        return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+    def matvec(i):
+        return tg.einsum(orc.MATVEC, head, tail, vectors[i % 4])
+
+    # correctness of this very workload before timing it: FP64 against the oracle on rank 0's inputs
+    want = orc.einsum(orc.MATVEC, head_o, tail_o, theta_o)
+    with tg.precision(args.precision):
+        got = tg.einsum(orc.MATVEC, head, tail, product(theta_o))
+    scale = max(np.abs(b).max() for b in want.blocks.values())
+    parity = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.blocks.items()) / scale
+
+    for precision in sorted({0, args.precision}):
+        tg.set_precision(precision)
+        for i in range(args.warmup):
+            matvec(i)
+    torch.cuda.synchronize(device)
+
+    # --- the timed region ------------------------------------------------------------------
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(device)
+    clocks = Clocks(local)
+    wall0 = time.perf_counter()
+    times = timed_loop(args.steps, args.precision, matvec)
+    wall = time.perf_counter() - wall0
+    clock_record = clocks.stop()
+    torch.cuda.synchronize(device)
+    if world > 1:
+        dist.barrier()
+    total_ms = sum(times)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype = torch.float64, device = device)
+        dist.all_reduce(t, op = dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * args.steps / (total_ms / 1e3)
+
+    # plain FP64 on the same GPU, for the split-precision comparison
+    fp64_ms = ms_per_step
+    if args.precision != 0:
+        fp64_ms = sum(timed_loop(args.steps, 0, matvec)) / args.steps
+
+    # --- per-kernel durations inside the step (CUDA events on the launching stream) ----------
+    tg.set_precision(args.precision)
+    n_ops = plan.n_ops
+    op_ms = np.zeros(n_ops)
+    kinds = None
+    samples = min(args.steps, 200)
+    ws = torch.empty(max(plan.workspace, 1), dtype = torch.float64, device = device)
+    prepared = [tg.linalg._prepared_arena(plan, i, t, ws) for i, t in enumerate([head, tail, vectors[0]])]
+    for i in range(samples):
+        flush.zero_()
+        out = torch.empty(plan.out_space.size, dtype = torch.float64, device = device)
+        ms_arr, kind_arr = (_lib.ctypes.c_float * n_ops)(), (_lib.i32 * n_ops)()
+        _lib.check(_lib.lib.tt_plan_execute_timed(
+            plan.handle, 0, args.precision, _lib.pointers([head.data.data_ptr(), tail.data.data_ptr(), vectors[i % 4].data.data_ptr()]),
+            _lib.pointers([p.data_ptr() if p is not None else None for p in prepared]), out.data_ptr(), ws.data_ptr(),
+            stream.cuda_stream, n_ops, ms_arr, kind_arr))
+        op_ms += np.maximum(np.array(ms_arr[:n_ops]), 0.0)
+        kinds = list(kind_arr[:n_ops])
+    op_ms /= samples
+    names = {0: 'zero', 1: 'gather_kernel', 2: 'runs_kernel', 3: 'gemm_f64_kernel' if args.precision == 0 else 'gemm_split_kernel',
+             4: 'add_f64_kernel', 5: 'copy'}
+    by_kind = {}
+    launches_per_step = 0
+    for ms, k in zip(op_ms, kinds):
+        if ms <= 0:
+            continue
+        by_kind[names[k]] = by_kind.get(names[k], 0.0) + ms
+        if k in (1, 2, 3, 4):
+            launches_per_step += 1 if k != 3 or args.precision == 0 else 3
+    dominant = max(by_kind, key = by_kind.get)
+    gemm_ms = by_kind.get(names[3], 0.0)
+    peaks, peak_kind = measured_peaks()
+    if args.precision == 0:
+        peak = fp64_peak_tflops(torch, device)
+        achieved = plan.flops / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else 0.0
+        roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
+                    'traffic': ncu_traffic('gemm_f64_kernel'), 'kernel': 'gemm_f64_kernel',
+                    'peak_source': 'cuBLAS DGEMM 4096^3 best of 3 measured in this run (MEASURED_PEAKS.json has no FP64)',
+                    'algorithmic': f'{plan.flops:.4g} FLOP per launch (sum of 2mkn over the block pairs of both stages)',
+                    'kernel_ms': gemm_ms}
+    else:
+        slices = args.precision
+        bf16_flops = plan.flops * slices * (slices + 1) / 2
+        achieved = bf16_flops / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else 0.0
+        peak = peaks['bf16_tflops']
+        roofline = {'bound': 'tensor', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
+                    'traffic': ncu_traffic('gemm_split_kernel'), 'kernel': 'gemm_split_kernel',
+                    'peak_source': f'{peak_kind} bf16_tflops', 'kernel_ms': gemm_ms,
+                    'algorithmic': f'{bf16_flops:.4g} bf16 FLOP per step ({slices}({slices}+1)/2 slice products)'}
+    roofline['op_ms'] = {k: round(v, 6) for k, v in by_kind.items()}
+    roofline['dominant'] = dominant
+
+    # --- end to end through the public API with host buffers ---------------------------------
+    host_in = [torch.empty(v.data.shape, dtype = torch.float64, pin_memory = True) for v in vectors]
+    for h, v in zip(host_in, vectors):
+        h.copy_(v.data.cpu())
+    host_out = torch.empty(plan.out_space.size, dtype = torch.float64, pin_memory = True)
+    staging = product(theta_o)
+
+    def e2e_step(i):
+        staging.data.copy_(host_in[i % 4], non_blocking = True)
+        out = tg.einsum(orc.MATVEC, head, tail, staging)
+        host_out.copy_(out.data, non_blocking = True)
+
+    for i in range(3):
+        e2e_step(i)
+    e2e_times = timed_loop(args.steps, args.precision, e2e_step)
+    e2e_ms = sum(e2e_times) / args.steps
+    h2d = host_in[0].numel() * 8
+    d2h = host_out.numel() * 8
+
+    line = None
+    if rank == 0:
+        cpu_value, cpu_elapsed, cpu_n = cpu_matvecs(args.chi, args.cpu_sample)
+        line = {'metric': METRIC, 'value': value, 'unit': 'matvecs/s', 'n_gpus': world, 'steps': args.steps,
+                'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
+                'vs_baseline': None, 'dtype': 'f64' if args.precision == 0 else f'bf16x{args.precision}-split/f64',
+                'data': 'synthetic', 'config': config(args, args.precision),
+                'gflops': plan.flops / (ms_per_step / 1e3) / 1e9,
+                'fp64_matvecs_per_s': 1e3 / fp64_ms,
+                'wall_s_timed_region': wall,
+                'parity_vs_oracle': parity,
+                'roofline': roofline,
+                'cpu_baseline': {'value': cpu_value, 'unit': 'matvecs/s', 'cores': os.cpu_count(), 'kind': 'port',
+                                 'sample': f'{cpu_n} matvecs at chi={args.chi} of the oracle port of tentorch einsum '
+                                           f'(numpy; {cpu_elapsed:.1f} s)'},
+                'e2e': {'value': world * 1e3 / e2e_ms, 'unit': 'matvecs/s', 'h2d_bytes_per_step': h2d,
+                        'd2h_bytes_per_step': d2h,
+                        'path': 'pinned host theta -> H2D -> tentorch_gb300.einsum (C ABI) -> D2H of the image'},
+                'clocks': clock_record,
+                'gpu_launches': launches_per_step * args.steps}
+        print(json.dumps(line), flush = True)
+
+
+def main():
+    args = parse()
+    rank, world = int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1))
+    if world > 1:
+        import torch.distributed as dist
+        if args.impl == 'reference':
+            if rank != 0:
+                return
+        else:
+            dist.init_process_group('nccl' if args.impl == 'gb300' else 'gloo')
+    if args.impl == 'reference':
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

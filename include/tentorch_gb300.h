@@ -1,0 +1,144 @@
+/*
+ * tentorch_gb300: the C ABI of the GB300 block-sparse contraction engine.
+ *
+ * A drop-in for the block-sparse contraction path of Jumqyc/TenTorch (`tensors.einsum` /
+ * `contract` / `Tensor.place`).  The reference binds that path to Python with pybind11
+ * (tentorch/_ext/bindings.cpp:250-361); this library exposes the same operations as plain C entry
+ * points over integer handles and raw device pointers, so any host language binds it through its
+ * FFI (the Python package `tentorch_gb300` binds it with ctypes).
+ *
+ * Model.  A category, a leg and a space (the shape of a tensor: category, codomain legs, domain
+ * legs, total charge) are interned and named by int32 handles.  A tensor is a space plus one arena
+ * of device memory holding every block, row major, at the offsets `tt_space_blocks` reports.  A
+ * plan (a place, a contraction or an einsum) is compiled once per combination of spaces and cached;
+ * executing it reads the operand arenas and writes the output arena on a CUDA stream, using a
+ * caller-provided workspace.  The library never allocates arena memory.
+ *
+ * Conventions.  Sectors are passed as one int64 label (every category here has rank 1).  dtype 0 is
+ * float64, 1 is complex128.  Every function returns a status: 0 on success, else one of TT_E*; the
+ * message of the last failure on the calling thread is `tt_last_error()`.  Nothing throws across
+ * the ABI.  Host-side functions (everything but tt_plan_execute / tt_plan_prepare / tt_dots) need no
+ * GPU.
+ */
+#ifndef TENTORCH_GB300_H
+#define TENTORCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TT_OK 0
+#define TT_EINVAL 1 /* malformed request: the reference raises ValueError (std::invalid_argument) */
+#define TT_ERANGE 2 /* lookup outside a tensor: IndexError (std::out_of_range) */
+#define TT_ELOGIC 3 /* broken invariant: RuntimeError (std::logic_error / TORCH_CHECK) */
+#define TT_ECUDA 4  /* a CUDA call failed: RuntimeError */
+
+#define TT_DTYPE_FLOAT64 0
+#define TT_DTYPE_COMPLEX128 1
+
+typedef struct tt_plan tt_plan;
+
+/* The message of the last failure on this thread. */
+const char *tt_last_error(void);
+/* The ABI version (monotone). */
+int32_t tt_version(void);
+
+/* ---- categories (tentorch/symmetry/cat/cat.h:190-429) ------------------------------------ */
+
+/* kind: 0 no symmetry, 1 U(1), 2 SU(2), 3 Fibonacci, 4 Z_N (param = N), 5 fermion parity.
+ * Replaces the module singletons of tentorch/_ext/bindings.cpp:464-470. */
+int32_t tt_category(int32_t kind, int64_t param, int32_t *out);
+/* Fusion outcomes of a x b in the category's order (FusionCategory::outcomes, cat.h:231).
+ * Writes up to `cap` (sector, multiplicity) pairs, *n the total. */
+int32_t tt_outcomes(int32_t cat, int64_t a, int64_t b, int32_t cap, int64_t *sectors, int32_t *mult, int32_t *n);
+int32_t tt_dual(int32_t cat, int64_t a, int64_t *out);
+int32_t tt_q_dim(int32_t cat, int64_t a, double *out);
+/* F^d_{abc} (cat.h:282) / R_{bc} (cat.h:300) as row-major complex (re, im interleaved). */
+int32_t tt_F_symbol(int32_t cat, int64_t a, int64_t b, int64_t c, int64_t d, int32_t cap, double *values,
+                    int32_t *rows, int32_t *cols);
+int32_t tt_R_symbol(int32_t cat, int64_t b, int64_t c, int32_t cap, double *values, int32_t *rows, int32_t *cols);
+
+/* ---- legs and trees (tentorch/symmetry/tree/tree.h:33-199) ---------------------------------- */
+
+/* Intern a leg (Leg::Leg, tree.cpp:90-140): blocks sorted by sector, distinct, positive. */
+int32_t tt_leg(int32_t cat, int32_t n, const int64_t *sectors, const int64_t *mult, int32_t *out);
+/* The blocks of a leg, sorted. */
+int32_t tt_leg_blocks(int32_t leg, int32_t cap, int64_t *sectors, int64_t *mult, int32_t *n);
+/* reachable_charges (tree.cpp:375-398). */
+int32_t tt_reachable_charges(int32_t cat, int32_t nlegs, const int32_t *legs, int32_t cap, int64_t *out, int32_t *n);
+/* fusion_trees (tree.cpp:400-471) flattened: per tree `nlegs` sectors, max(nlegs-2,0) inner
+ * sectors, max(nlegs-1,0) copies, then the coupled sector; `stride` the int64 count per tree. */
+int32_t tt_fusion_trees(int32_t cat, int32_t nlegs, const int32_t *legs, int64_t coupled, int64_t cap, int64_t *out,
+                        int64_t *n_trees, int32_t *stride);
+
+/* ---- spaces (tentorch/tensors/tensor.h:43-216, layout.h:64-127) --------------------------- */
+
+/* Intern the shape of a tensor; its blocks follow block_keys (layout.cpp:34-47) in key order. */
+int32_t tt_space(int32_t cat, int32_t ncod, const int32_t *cod, int32_t ndom, const int32_t *dom, int64_t qtotal,
+                 int32_t *out);
+/* Number of blocks and arena elements (block starts are 16-byte aligned, padding stays zero). */
+int32_t tt_space_size(int32_t space, int64_t *nblocks, int64_t *elements);
+/* Per block: (codomain root, domain root, copy) and (rows, cols, offset). */
+int32_t tt_space_blocks(int32_t space, int64_t cap, int64_t *keys, int64_t *shapes);
+/* The legs and charge of a space. */
+int32_t tt_space_legs(int32_t space, int32_t cap, int32_t *legs, int32_t *ncod, int32_t *ndom, int64_t *qtotal);
+
+/* ---- plans -------------------------------------------------------------------------------- */
+
+/* Tensor::place(above, below) (tensors/place.cpp:183-247). */
+int32_t tt_plan_place(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
+                      tt_plan **out);
+/* contract(left, right, left_legs, right_legs[, charge]) (linalg/graded/contract.cpp:117-175). */
+int32_t tt_plan_contract(int32_t left, int32_t right, int32_t n, const int32_t *left_legs, const int32_t *right_legs,
+                         int32_t has_charge, int64_t charge, tt_plan **out);
+/* einsum(spec, *operands, outcharge=) (linalg/graded/einsum.cpp:444-605, bindings.cpp:347-361). */
+int32_t tt_plan_einsum(const char *spec, int32_t n, const int32_t *spaces, int32_t has_charge, int64_t charge,
+                       tt_plan **out);
+/* The output space, workspace elements, GEMM flops, recoupled elements and op count of a plan. */
+int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace, double *gemm_flops,
+                     int64_t *moved_elements, int32_t *n_ops);
+/* Elements of operand `i`'s prepared arena, 0 when the operand needs no preparation. */
+int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements);
+/* Execute on `stream` (a cudaStream_t, 0 for the legacy stream).  precision 0: FP64 block
+ * products; k >= 1: split products on the tensor cores with k bf16 slices per operand.
+ * `prepared` (may be NULL, or hold NULLs) gives operands' prepared arenas from tt_plan_prepare. */
+int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                        const void *const *prepared, void *output, void *workspace, void *stream);
+/* The same, synchronously, recording a CUDA event pair around every operation on `stream`: per op
+ * its device milliseconds (-1 when it did not run) and its kind (0 zero, 1 gather, 2 runs, 3 gemm,
+ * 4 add, 5 copy).  For measurement; the caller's stream is synchronised before it returns. */
+int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                              const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
+                              float *op_ms, int32_t *op_kind);
+/* Run operand `operand`'s preparation only, writing its prepared arena. */
+int32_t tt_plan_prepare(const tt_plan *plan, int32_t dtype, int32_t operand, const void *input, void *prepared,
+                        void *workspace, void *stream);
+
+/* ---- per-step plans, for checking against the reference (tensors/regroup.h:22-96) --------- */
+
+/* The shifts of one step on one block of `space`: kind 0 exchange at `arm`, 1 bend down, 2 bend
+ * up.  Per piece 8 doubles: first, last, from_step, to_step, run, re, im and the shift number;
+ * per shift 9 int64 in `shifts`: from key (3), to key (3), rows, cols, piece count. */
+int32_t tt_step_plan(int32_t space, int32_t kind, int32_t arm, int64_t key_cod, int64_t key_dom, int32_t key_copy,
+                     int64_t cap_shifts, int64_t *shifts, int64_t cap_pieces, double *pieces, int64_t *n_shifts,
+                     int64_t *n_pieces);
+/* The chain of steps of a place: per step (kind, arm, space after). */
+int32_t tt_chain(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
+                 int32_t cap, int32_t *steps, int32_t *n);
+
+/* ---- Krylov arithmetic on arenas ----------------------------------------------------------- */
+
+/* out[2j], out[2j+1] = <a_j, b> (conjugating a_j) for j < count, on `stream`, with no host
+ * synchronisation; `as` is a device array of `count` arena pointers, n the arena elements,
+ * `scratch` 2*120*count doubles of device memory. */
+int32_t tt_dots(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *scratch,
+                double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -796,7 +796,7 @@ def plan_of(cat, codomain, domain, key, qtotal, step):
 def _piece_arrays(pieces):
     '''The runs of a shift expanded to flat index arrays, so a plan applies in one numpy pass.'''
     if not pieces:
-        return np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0, complex)
+        return np.zeros(0, np.int64), np.zeros(0, np.int64), np.zeros(0, complex), True
     arr = np.array([(p[0], p[1], p[2], p[3], p[4]) for p in pieces], np.int64)
     runs = arr[:, 4]
     rep = np.repeat(np.arange(len(pieces)), runs)
@@ -805,18 +805,22 @@ def _piece_arrays(pieces):
     src = arr[rep, 0] + step * arr[rep, 2]
     dst = arr[rep, 1] + step * arr[rep, 3]
     coef = np.array([p[5] for p in pieces], complex)[rep]
-    return src, dst, coef
+    unique = np.unique(dst).size == dst.size
+    return src, dst, coef, unique
 
 
 def _apply(arrays, source, target):
     '''tentorch/tensors/cache.cpp:66-92: to[last + i*ts] += c * from[first + i*fs]; a float64
     block takes the real part of the coefficient (tentorch/tensors/cache.cpp:84-92).'''
-    src, dst, coef = arrays
+    src, dst, coef, unique = arrays
     if src.size == 0:
         return
     flat = target.reshape(-1)
     c = coef if np.iscomplexobj(target) else coef.real
-    np.add.at(flat, dst, c * source.reshape(-1)[src])
+    if unique:
+        flat[dst] += c * source.reshape(-1)[src]
+    else:
+        np.add.at(flat, dst, c * source.reshape(-1)[src])
 
 
 def carried(tensor, steps):

@@ -1,0 +1,526 @@
+// The C ABI (include/tentorch_gb300.h): integer handles over the interned categories, legs and
+// spaces, cached plans, and status codes instead of exceptions.
+#include "../../include/tentorch_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "engine.h"
+#include "executor.h"
+#include "program.h"
+
+struct tt_plan
+{
+  std::shared_ptr<ttg::Program> program;
+  std::unique_ptr<ttg::DeviceTables> tables;
+};
+
+namespace
+{
+  thread_local std::string last_error;
+  std::recursive_mutex registry_mutex;  // categories, legs, spaces, plan caches
+
+  int32_t fail(int32_t code, const std::string &message)
+  {
+    last_error = message;
+    return code;
+  }
+
+  template <typename F>
+  int32_t guarded(F &&body)
+  {
+    try
+    {
+      std::lock_guard<std::recursive_mutex> lock(registry_mutex);
+      body();
+      return TT_OK;
+    }
+    catch (const ttg::OutOfRange &e)
+    {
+      return fail(TT_ERANGE, e.what());
+    }
+    catch (const ttg::InvalidArgument &e)
+    {
+      return fail(TT_EINVAL, e.what());
+    }
+    catch (const std::invalid_argument &e)
+    {
+      return fail(TT_EINVAL, e.what());
+    }
+    catch (const std::out_of_range &e)
+    {
+      return fail(TT_ERANGE, e.what());
+    }
+    catch (const std::exception &e)
+    {
+      return fail(TT_ELOGIC, e.what());
+    }
+  }
+
+  std::vector<const ttg::Category *> &categories()
+  {
+    static std::vector<const ttg::Category *> held;
+    return held;
+  }
+
+  const ttg::Category *cat_of(int32_t id)
+  {
+    auto &held = categories();
+    if (id < 0 || static_cast<size_t>(id) >= held.size()) throw ttg::InvalidArgument("no category " + std::to_string(id));
+    return held[static_cast<size_t>(id)];
+  }
+
+  ttg::Sector S(int64_t v) { return ttg::Sector{v}; }
+
+  void write_matrix(const ttg::Matrix &m, int32_t cap, double *values, int32_t *rows, int32_t *cols)
+  {
+    *rows = m.rows;
+    *cols = m.cols;
+    const int32_t n = std::min<int32_t>(cap, m.rows * m.cols);
+    for (int32_t i = 0; i < n; ++i)
+    {
+      values[2 * i] = m.v[static_cast<size_t>(i)].real();
+      values[2 * i + 1] = m.v[static_cast<size_t>(i)].imag();
+    }
+  }
+
+  std::vector<ttg::Leg> legs_of(int32_t n, const int32_t *ids)
+  {
+    std::vector<ttg::Leg> out;
+    for (int32_t i = 0; i < n; ++i) out.push_back(ttg::leg_by_id(ids[i]));
+    return out;
+  }
+
+  tt_plan *keep(std::map<std::string, std::unique_ptr<tt_plan>> &cache, const std::string &name,
+                const std::function<std::shared_ptr<ttg::Program>()> &build)
+  {
+    auto found = cache.find(name);
+    if (found != cache.end()) return found->second.get();
+    auto plan = std::make_unique<tt_plan>();
+    plan->program = build();
+    plan->tables = std::make_unique<ttg::DeviceTables>();
+    return cache.emplace(name, std::move(plan)).first->second.get();
+  }
+
+  std::map<std::string, std::unique_ptr<tt_plan>> &plan_cache()
+  {
+    static std::map<std::string, std::unique_ptr<tt_plan>> cache;
+    return cache;
+  }
+
+  std::string ints(const int32_t *v, int32_t n)
+  {
+    std::string out;
+    for (int32_t i = 0; i < n; ++i) out += std::to_string(v[i]) + ",";
+    return out;
+  }
+} // namespace
+
+extern "C"
+{
+  const char *tt_last_error(void) { return last_error.c_str(); }
+
+  int32_t tt_version(void) { return 1; }
+
+  int32_t tt_category(int32_t kind, int64_t param, int32_t *out)
+  {
+    return guarded([&] {
+      if (kind < 0 || kind > 5) throw ttg::InvalidArgument("unknown category kind " + std::to_string(kind));
+      const ttg::Category *c = ttg::category(static_cast<ttg::CategoryKind>(kind), param);
+      auto &held = categories();
+      for (size_t i = 0; i < held.size(); ++i)
+        if (held[i] == c)
+        {
+          *out = static_cast<int32_t>(i);
+          return;
+        }
+      held.push_back(c);
+      *out = static_cast<int32_t>(held.size() - 1);
+    });
+  }
+
+  int32_t tt_outcomes(int32_t cat, int64_t a, int64_t b, int32_t cap, int64_t *sectors, int32_t *mult, int32_t *n)
+  {
+    return guarded([&] {
+      const auto &o = cat_of(cat)->outcomes(S(a), S(b));
+      *n = static_cast<int32_t>(o.size());
+      for (int32_t i = 0; i < std::min<int32_t>(cap, *n); ++i)
+      {
+        sectors[i] = o[static_cast<size_t>(i)].sector[0];
+        mult[i] = o[static_cast<size_t>(i)].multiplicity;
+      }
+    });
+  }
+
+  int32_t tt_dual(int32_t cat, int64_t a, int64_t *out)
+  {
+    return guarded([&] { *out = cat_of(cat)->dual(S(a))[0]; });
+  }
+
+  int32_t tt_q_dim(int32_t cat, int64_t a, double *out)
+  {
+    return guarded([&] { *out = cat_of(cat)->q_dim(S(a)); });
+  }
+
+  int32_t tt_F_symbol(int32_t cat, int64_t a, int64_t b, int64_t c, int64_t d, int32_t cap, double *values,
+                      int32_t *rows, int32_t *cols)
+  {
+    return guarded([&] { write_matrix(cat_of(cat)->F(S(a), S(b), S(c), S(d)), cap, values, rows, cols); });
+  }
+
+  int32_t tt_R_symbol(int32_t cat, int64_t b, int64_t c, int32_t cap, double *values, int32_t *rows, int32_t *cols)
+  {
+    return guarded([&] { write_matrix(cat_of(cat)->R(S(b), S(c)), cap, values, rows, cols); });
+  }
+
+  int32_t tt_leg(int32_t cat, int32_t n, const int64_t *sectors, const int64_t *mult, int32_t *out)
+  {
+    return guarded([&] {
+      std::vector<ttg::Sector> s;
+      std::vector<int64_t> m;
+      for (int32_t i = 0; i < n; ++i)
+      {
+        s.push_back(S(sectors[i]));
+        m.push_back(mult[i]);
+      }
+      *out = ttg::make_leg(cat_of(cat), std::move(s), std::move(m))->id;
+    });
+  }
+
+  int32_t tt_leg_blocks(int32_t leg, int32_t cap, int64_t *sectors, int64_t *mult, int32_t *n)
+  {
+    return guarded([&] {
+      ttg::Leg l = ttg::leg_by_id(leg);
+      *n = static_cast<int32_t>(l->sectors.size());
+      for (int32_t i = 0; i < std::min<int32_t>(cap, *n); ++i)
+      {
+        sectors[i] = l->sectors[static_cast<size_t>(i)][0];
+        mult[i] = l->mult[static_cast<size_t>(i)];
+      }
+    });
+  }
+
+  int32_t tt_reachable_charges(int32_t cat, int32_t nlegs, const int32_t *legs, int32_t cap, int64_t *out, int32_t *n)
+  {
+    return guarded([&] {
+      const auto charges = ttg::reachable_charges(*cat_of(cat), legs_of(nlegs, legs));
+      *n = static_cast<int32_t>(charges.size());
+      for (int32_t i = 0; i < std::min<int32_t>(cap, *n); ++i) out[i] = charges[static_cast<size_t>(i)][0];
+    });
+  }
+
+  int32_t tt_fusion_trees(int32_t cat, int32_t nlegs, const int32_t *legs, int64_t coupled, int64_t cap, int64_t *out,
+                          int64_t *n_trees, int32_t *stride)
+  {
+    return guarded([&] {
+      const auto trees = ttg::fusion_trees(*cat_of(cat), legs_of(nlegs, legs), S(coupled));
+      const int32_t per = nlegs + std::max(nlegs - 2, 0) + std::max(nlegs - 1, 0) + 1;
+      *stride = per;
+      *n_trees = static_cast<int64_t>(trees.size());
+      int64_t at = 0;
+      for (const ttg::Tree &t : trees)
+      {
+        if (at + per > cap) break;
+        for (const auto &s : t.sectors) out[at++] = s[0];
+        for (const auto &s : t.inner) out[at++] = s[0];
+        for (int32_t c : t.copies) out[at++] = c;
+        out[at++] = t.coupled[0];
+      }
+    });
+  }
+
+  int32_t tt_space(int32_t cat, int32_t ncod, const int32_t *cod, int32_t ndom, const int32_t *dom, int64_t qtotal,
+                   int32_t *out)
+  {
+    return guarded([&] { *out = ttg::make_space(cat_of(cat), legs_of(ncod, cod), legs_of(ndom, dom), S(qtotal))->id; });
+  }
+
+  int32_t tt_space_size(int32_t space, int64_t *nblocks, int64_t *elements)
+  {
+    return guarded([&] {
+      ttg::Space s = ttg::space_by_id(space);
+      *nblocks = static_cast<int64_t>(s->blocks.size());
+      *elements = s->size;
+    });
+  }
+
+  int32_t tt_space_blocks(int32_t space, int64_t cap, int64_t *keys, int64_t *shapes)
+  {
+    return guarded([&] {
+      ttg::Space s = ttg::space_by_id(space);
+      for (int64_t i = 0; i < std::min<int64_t>(cap, static_cast<int64_t>(s->blocks.size())); ++i)
+      {
+        const ttg::Block &b = s->blocks[static_cast<size_t>(i)];
+        keys[3 * i] = b.key.codomain[0];
+        keys[3 * i + 1] = b.key.domain[0];
+        keys[3 * i + 2] = b.key.copy;
+        shapes[3 * i] = b.rows;
+        shapes[3 * i + 1] = b.cols;
+        shapes[3 * i + 2] = b.offset;
+      }
+    });
+  }
+
+  int32_t tt_space_legs(int32_t space, int32_t cap, int32_t *legs, int32_t *ncod, int32_t *ndom, int64_t *qtotal)
+  {
+    return guarded([&] {
+      ttg::Space s = ttg::space_by_id(space);
+      *ncod = static_cast<int32_t>(s->codomain.size());
+      *ndom = static_cast<int32_t>(s->domain.size());
+      *qtotal = s->qtotal[0];
+      int32_t at = 0;
+      for (ttg::Leg l : s->legs())
+        if (at < cap) legs[at++] = l->id;
+    });
+  }
+
+  int32_t tt_plan_place(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
+                        tt_plan **out)
+  {
+    return guarded([&] {
+      const std::string name = "place|" + std::to_string(space) + "|" + ints(above, nabove) + "|" + ints(below, nbelow);
+      *out = keep(plan_cache(), name, [&] {
+        return ttg::compile_place(ttg::space_by_id(space), std::vector<int32_t>(above, above + nabove),
+                                  std::vector<int32_t>(below, below + nbelow));
+      });
+    });
+  }
+
+  int32_t tt_plan_contract(int32_t left, int32_t right, int32_t n, const int32_t *left_legs, const int32_t *right_legs,
+                           int32_t has_charge, int64_t charge, tt_plan **out)
+  {
+    return guarded([&] {
+      const std::string name = "contract|" + std::to_string(left) + "|" + std::to_string(right) + "|" +
+                               ints(left_legs, n) + "|" + ints(right_legs, n) + "|" + std::to_string(has_charge) + "|" +
+                               std::to_string(charge);
+      *out = keep(plan_cache(), name, [&] {
+        return ttg::compile_contract(ttg::space_by_id(left), ttg::space_by_id(right),
+                                     std::vector<int32_t>(left_legs, left_legs + n),
+                                     std::vector<int32_t>(right_legs, right_legs + n), has_charge != 0, S(charge));
+      });
+    });
+  }
+
+  int32_t tt_plan_einsum(const char *spec, int32_t n, const int32_t *spaces, int32_t has_charge, int64_t charge,
+                         tt_plan **out)
+  {
+    return guarded([&] {
+      const std::string name = std::string("einsum|") + spec + "|" + ints(spaces, n) + "|" + std::to_string(has_charge) +
+                               "|" + std::to_string(charge);
+      *out = keep(plan_cache(), name, [&] {
+        std::vector<ttg::Space> ops;
+        for (int32_t i = 0; i < n; ++i) ops.push_back(ttg::space_by_id(spaces[i]));
+        return ttg::compile_einsum(spec, ops, has_charge != 0, S(charge));
+      });
+    });
+  }
+
+  int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace, double *gemm_flops,
+                       int64_t *moved_elements, int32_t *n_ops)
+  {
+    return guarded([&] {
+      if (!plan) throw ttg::InvalidArgument("no plan");
+      const ttg::Program &p = *plan->program;
+      *out_space = p.output_space->id;
+      *workspace = p.workspace;
+      *gemm_flops = p.gemm_flops;
+      *moved_elements = p.moved_elements;
+      *n_ops = static_cast<int32_t>(p.ops.size());
+    });
+  }
+
+  int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements)
+  {
+    return guarded([&] {
+      const ttg::Program &p = *plan->program;
+      if (operand < 0 || operand >= p.n_inputs) throw ttg::InvalidArgument("no operand " + std::to_string(operand));
+      const int32_t b = p.prepared[static_cast<size_t>(operand)];
+      *elements = b < 0 ? 0 : p.buffers[static_cast<size_t>(b)].size;
+    });
+  }
+
+  int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                          const void *const *prepared, void *output, void *workspace, void *stream)
+  {
+    if (!plan) return fail(TT_EINVAL, "no plan");
+    if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128) return fail(TT_EINVAL, "unknown dtype");
+    if (precision < 0 || precision > 8) return fail(TT_EINVAL, "precision is 0 (FP64) or 1..8 slices");
+    if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
+      return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
+    ttg::ExecArgs args;
+    args.complex = dtype == TT_DTYPE_COMPLEX128;
+    args.precision = precision;
+    args.inputs = inputs;
+    args.prepared = prepared;
+    args.output = output;
+    args.workspace = workspace;
+    args.stream = static_cast<cudaStream_t>(stream);
+    if (plan->program->complex_coefficients && !args.complex)
+    {
+      // a float64 tensor keeps the real part of a complex coefficient, as the reference does
+      // (tentorch/tensors/cache.cpp:84-92); nothing to do here, the kernel reads .re only
+    }
+    const cudaError_t e = ttg::execute(*plan->program, *plan->tables, args);
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+
+  int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                                const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
+                                float *op_ms, int32_t *op_kind)
+  {
+    if (!plan) return fail(TT_EINVAL, "no plan");
+    if (precision < 0 || precision > 8) return fail(TT_EINVAL, "precision is 0 (FP64) or 1..8 slices");
+    if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
+      return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
+    const ttg::Program &p = *plan->program;
+    const size_t n = p.ops.size();
+    std::vector<cudaEvent_t> events(2 * n, nullptr);
+    cudaError_t e = cudaSuccess;
+    for (size_t i = 0; i < events.size() && e == cudaSuccess; ++i) e = cudaEventCreate(&events[i]);
+    if (e == cudaSuccess)
+    {
+      ttg::ExecArgs args;
+      args.complex = dtype == TT_DTYPE_COMPLEX128;
+      args.precision = precision;
+      args.inputs = inputs;
+      args.prepared = prepared;
+      args.output = output;
+      args.workspace = workspace;
+      args.stream = static_cast<cudaStream_t>(stream);
+      args.events = events.data();
+      e = ttg::execute(p, *plan->tables, args);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(args.stream);
+      for (size_t i = 0; i < n && e == cudaSuccess; ++i)
+      {
+        float ms = -1.0f;
+        // an op that did not run left its events unrecorded: cudaEventElapsedTime reports that
+        if (cudaEventQuery(events[2 * i]) == cudaSuccess && cudaEventElapsedTime(&ms, events[2 * i], events[2 * i + 1]) != cudaSuccess)
+          ms = -1.0f;
+        cudaGetLastError();
+        if (static_cast<int32_t>(i) < cap)
+        {
+          op_ms[i] = ms;
+          op_kind[i] = static_cast<int32_t>(p.ops[i].kind);
+        }
+      }
+    }
+    for (cudaEvent_t ev : events)
+      if (ev) cudaEventDestroy(ev);
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+
+  int32_t tt_plan_prepare(const tt_plan *plan, int32_t dtype, int32_t operand, const void *input, void *prepared,
+                          void *workspace, void *stream)
+  {
+    if (!plan) return fail(TT_EINVAL, "no plan");
+    const ttg::Program &p = *plan->program;
+    if (operand < 0 || operand >= p.n_inputs || p.prepared[static_cast<size_t>(operand)] < 0)
+      return fail(TT_EINVAL, "operand " + std::to_string(operand) + " has no preparation");
+    std::vector<const void *> inputs(static_cast<size_t>(p.n_inputs), nullptr);
+    inputs[static_cast<size_t>(operand)] = input;
+    ttg::ExecArgs args;
+    args.complex = dtype == TT_DTYPE_COMPLEX128;
+    args.inputs = inputs.data();
+    args.workspace = workspace;
+    args.stream = static_cast<cudaStream_t>(stream);
+    args.only_phase = operand;
+    args.prepared_out = prepared;
+    const cudaError_t e = ttg::execute(p, *plan->tables, args);
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+
+  int32_t tt_step_plan(int32_t space, int32_t kind, int32_t arm, int64_t key_cod, int64_t key_dom, int32_t key_copy,
+                       int64_t cap_shifts, int64_t *shifts, int64_t cap_pieces, double *pieces, int64_t *n_shifts,
+                       int64_t *n_pieces)
+  {
+    return guarded([&] {
+      ttg::Space s = ttg::space_by_id(space);
+      if (kind < 0 || kind > 2) throw ttg::InvalidArgument("a step is 0 (exchange), 1 (bend down) or 2 (bend up)");
+      std::vector<ttg::Leg> cod = s->codomain, dom = s->domain;
+      if (kind == 0)
+      {
+        if (arm < 0 || arm + 1 >= static_cast<int32_t>(cod.size())) throw ttg::InvalidArgument("no such exchange");
+        std::swap(cod[static_cast<size_t>(arm)], cod[static_cast<size_t>(arm + 1)]);
+      }
+      else if (kind == 1)
+      {
+        if (cod.empty()) throw ttg::InvalidArgument("no codomain leg to bend");
+        dom.push_back(cod.back());
+        cod.pop_back();
+      }
+      else
+      {
+        if (dom.empty()) throw ttg::InvalidArgument("no domain leg to bend");
+        cod.push_back(dom.back());
+        dom.pop_back();
+      }
+      ttg::Step step{kind, kind == 0 ? arm : 0, s, ttg::make_space(s->cat, cod, dom, s->qtotal)};
+      const auto &plan = ttg::step_plan(step, ttg::BlockKey{S(key_cod), S(key_dom), key_copy});
+      *n_shifts = static_cast<int64_t>(plan.size());
+      int64_t np = 0;
+      for (size_t i = 0; i < plan.size(); ++i)
+      {
+        const ttg::Shift &sh = plan[i];
+        if (static_cast<int64_t>(i) < cap_shifts)
+        {
+          int64_t *o = shifts + 9 * i;
+          o[0] = sh.from.codomain[0], o[1] = sh.from.domain[0], o[2] = sh.from.copy;
+          o[3] = sh.to.codomain[0], o[4] = sh.to.domain[0], o[5] = sh.to.copy;
+          o[6] = sh.rows, o[7] = sh.cols, o[8] = static_cast<int64_t>(sh.pieces.size());
+        }
+        for (const ttg::Piece &pc : sh.pieces)
+        {
+          if (np < cap_pieces)
+          {
+            double *o = pieces + 8 * np;
+            o[0] = static_cast<double>(pc.first), o[1] = static_cast<double>(pc.last);
+            o[2] = static_cast<double>(pc.from_step), o[3] = static_cast<double>(pc.to_step);
+            o[4] = static_cast<double>(pc.run), o[5] = pc.coefficient.real(), o[6] = pc.coefficient.imag();
+            o[7] = static_cast<double>(i);
+          }
+          ++np;
+        }
+      }
+      *n_pieces = np;
+    });
+  }
+
+  int32_t tt_chain(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
+                   int32_t cap, int32_t *steps, int32_t *n)
+  {
+    return guarded([&] {
+      const auto ch = ttg::chain(ttg::space_by_id(space), std::vector<int32_t>(above, above + nabove),
+                                 std::vector<int32_t>(below, below + nbelow));
+      *n = static_cast<int32_t>(ch.size());
+      for (int32_t i = 0; i < std::min<int32_t>(cap, *n); ++i)
+      {
+        steps[3 * i] = ch[static_cast<size_t>(i)].kind;
+        steps[3 * i + 1] = ch[static_cast<size_t>(i)].arm;
+        steps[3 * i + 2] = ch[static_cast<size_t>(i)].after->id;
+      }
+    });
+  }
+
+  int32_t tt_dots(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *scratch,
+                  double *out, void *stream)
+  {
+    if (count <= 0) return TT_OK;
+    const bool complex = dtype == TT_DTYPE_COMPLEX128;
+    const cudaError_t e = ttg::arena_dots(reinterpret_cast<const double *const *>(as), count,
+                                          static_cast<const double *>(b), n * (complex ? 2 : 1), complex, scratch, out,
+                                          static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+}

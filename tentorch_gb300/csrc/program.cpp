@@ -1,0 +1,826 @@
+// The plan compiler: place / contract / einsum -> device program (see program.h).
+#include "program.h"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <map>
+#include <numeric>
+#include <optional>
+#include <unordered_map>
+
+namespace ttg
+{
+  namespace
+  {
+    // A value the program computes: an arena of `space`, read from `buffer` through an optional
+    // pending gather (a composed chain of permutations not yet written out).
+    struct Value
+    {
+      int32_t buffer = -1;
+      Space space = nullptr;
+      std::shared_ptr<std::vector<int32_t>> pending;
+      int32_t phase = -1;  // operand whose prepare phase computes it, -1 for the core
+    };
+
+    class Builder
+    {
+    public:
+      explicit Builder(Program &p) : p_(p) {}
+
+      Value input(int32_t index, Space space)
+      {
+        Buffer b{BufferKind::input, index, 0, space->size};
+        p_.buffers.push_back(b);
+        return Value{static_cast<int32_t>(p_.buffers.size() - 1), space, nullptr, index};
+      }
+
+      int32_t output_buffer(Space space)
+      {
+        p_.buffers.push_back(Buffer{BufferKind::output, 0, 0, space->size});
+        return static_cast<int32_t>(p_.buffers.size() - 1);
+      }
+
+      int32_t temp(Space space)
+      {
+        p_.buffers.push_back(Buffer{BufferKind::temp, -1, p_.workspace, space->size});
+        p_.workspace += (space->size + 31) / 32 * 32;  // keep every temporary 256-byte aligned
+        return static_cast<int32_t>(p_.buffers.size() - 1);
+      }
+
+      // Write a value out into a buffer of its own (or `into` when given).
+      Value materialize(const Value &v, int32_t into = -1)
+      {
+        if (!v.pending)
+        {
+          if (into < 0 || into == v.buffer) return v;
+          emit(Op{OpKind::copy, v.buffer, -1, into, 0, 0, v.space->size, v.phase});
+          return Value{into, v.space, nullptr, v.phase};
+        }
+        const std::vector<int32_t> &index = *v.pending;
+        const Buffer &base = p_.buffers[static_cast<size_t>(v.buffer)];
+        bool identity = into < 0 && base.size == static_cast<int64_t>(index.size());
+        for (size_t i = 0; identity && i < index.size(); ++i) identity = index[i] == static_cast<int32_t>(i);
+        if (identity) return Value{v.buffer, v.space, nullptr, v.phase};
+        const int32_t dst = into >= 0 ? into : temp(v.space);
+        Op op{OpKind::gather, v.buffer, -1, dst, static_cast<int64_t>(p_.gather_index.size()),
+              static_cast<int64_t>(index.size()), static_cast<int64_t>(index.size()), v.phase};
+        p_.gather_index.insert(p_.gather_index.end(), index.begin(), index.end());
+        p_.moved_elements += static_cast<int64_t>(index.size());
+        emit(op);
+        return Value{dst, v.space, nullptr, v.phase};
+      }
+
+      // tentorch/tensors/place.cpp:199-247, compiled: the chain of steps becomes one composed
+      // gather for categories whose symbols are all 1, and one RUNS pass per step otherwise.
+      Value place(const Value &v, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
+      {
+        const std::vector<Step> steps = chain(v.space, above, below);
+        if (steps.empty()) return v;
+        const Category &cat = *v.space->cat;
+        if (cat.trivial_symbols())
+        {
+          std::shared_ptr<std::vector<int32_t>> current = v.pending;
+          for (const Step &step : steps)
+          {
+            std::vector<int32_t> back = permutation_of(step);
+            if (current)
+              for (int32_t &b : back) b = b >= 0 ? (*current)[static_cast<size_t>(b)] : -1;
+            current = std::make_shared<std::vector<int32_t>>(std::move(back));
+          }
+          return Value{v.buffer, steps.back().after, current, v.phase};
+        }
+        Value at = materialize(v);
+        for (const Step &step : steps)
+        {
+          const int32_t dst = temp(step.after);
+          emit(Op{OpKind::zero, -1, -1, dst, 0, 0, step.after->size, v.phase});
+          append_runs(step, at.buffer, dst, v.phase);
+          at = Value{dst, step.after, nullptr, v.phase};
+        }
+        return at;
+      }
+
+      // tentorch/linalg/graded/contract.cpp:134-164 on operands already aligned: every output
+      // block is the sum over the middle roots of the block products, one grouped GEMM.
+      Value contract_aligned(const Value &a_in, const Value &b_in, const Sector &charge)
+      {
+        const Value a = materialize(a_in), b = materialize(b_in);
+        const Category &cat = *a.space->cat;
+        Space out = make_space(a.space->cat, a.space->codomain, b.space->domain, charge);
+        for (const Block &blk : a.space->blocks) require_single_closing(cat, blk.key.codomain, blk.key.domain, a.space->qtotal, "the roots", "a contraction");
+        for (const Block &blk : b.space->blocks) require_single_closing(cat, blk.key.codomain, blk.key.domain, b.space->qtotal, "the roots", "a contraction");
+        for (const Block &blk : out->blocks) require_single_closing(cat, blk.key.codomain, blk.key.domain, charge, "the roots", "a contraction");
+        const int32_t phase = a.phase == b.phase ? a.phase : -1;
+        const int32_t dst = temp(out);
+        // pairs per output block, in the order the reference sums them (A blocks in key order, B
+        // blocks of the matching codomain root in key order)
+        std::vector<std::vector<GemmPair>> pairs(out->blocks.size());
+        std::map<Sector, std::vector<const Block *>> rows;
+        for (const Block &blk : b.space->blocks) rows[blk.key.codomain].push_back(&blk);
+        for (const Block &left : a.space->blocks)
+        {
+          const auto found = rows.find(left.key.domain);
+          if (found == rows.end()) continue;
+          for (const Block *right : found->second)
+          {
+            if (cat.n_symbol(left.key.codomain, cat.dual(right->key.domain), charge) == 0) continue;
+            if (left.cols != right->rows)
+              throw LogicError("the two blocks over the roots " + left.key.domain.str() + " do not line up: " +
+                               std::to_string(left.cols) + " against " + std::to_string(right->rows));
+            const int32_t at = out->find(BlockKey{left.key.codomain, right->key.domain, 0});
+            if (at < 0) throw LogicError("a block product lands outside the output");
+            pairs[static_cast<size_t>(at)].push_back(GemmPair{left.offset, right->offset, static_cast<int32_t>(left.cols), 0});
+            p_.gemm_flops += 2.0 * static_cast<double>(left.rows) * static_cast<double>(left.cols) *
+                             static_cast<double>(right->cols);
+          }
+        }
+        Op op{OpKind::gemm, a.buffer, b.buffer, dst, static_cast<int64_t>(p_.gemm_blocks.size()), 0, out->size, phase};
+        for (size_t i = 0; i < out->blocks.size(); ++i)
+        {
+          const Block &c = out->blocks[i];
+          p_.gemm_blocks.push_back(GemmBlock{c.offset, static_cast<int32_t>(c.rows), static_cast<int32_t>(c.cols),
+                                             static_cast<int32_t>(p_.gemm_pairs.size()),
+                                             static_cast<int32_t>(pairs[i].size())});
+          p_.gemm_pairs.insert(p_.gemm_pairs.end(), pairs[i].begin(), pairs[i].end());
+        }
+        op.count = static_cast<int64_t>(out->blocks.size());
+        emit(op);
+        return Value{dst, out, nullptr, phase};
+      }
+
+      // tentorch/linalg/graded/einsum.cpp:95-159: the trace of the last codomain leg against the
+      // last domain leg, one result per charge the kept roots close to (in sector order).
+      std::vector<Value> partial_trace(const Value &v_in)
+      {
+        const Value v = materialize(v_in);
+        Space s = v.space;
+        const Category &cat = *s->cat;
+        const std::vector<Leg> out_cod(s->codomain.begin(), s->codomain.end() - 1);
+        const std::vector<Leg> out_dom(s->domain.begin(), s->domain.end() - 1);
+        struct Contribution
+        {
+          int64_t src, dst;
+          int64_t inside_rows, inside_cols, copies, src_stride, dst_stride;
+        };
+        std::map<Sector, std::vector<Contribution>> by_charge;
+        for (const Block &blk : s->blocks)
+        {
+          require_single_closing(cat, blk.key.codomain, blk.key.domain, s->qtotal, "the roots", "a trace");
+          const Layout &rows = layout_of(cat, s->codomain, blk.key.codomain);
+          const Layout &cols = layout_of(cat, s->domain, blk.key.domain);
+          for (size_t ri = 0; ri < rows.trees.size(); ++ri)
+          {
+            const Tree &above_tree = rows.trees[ri];
+            const int64_t row_span = rows.offsets[ri + 1] - rows.offsets[ri];
+            const Tree kept_above = trimmed(cat, above_tree);
+            for (size_t ci = 0; ci < cols.trees.size(); ++ci)
+            {
+              const Tree &under_tree = cols.trees[ci];
+              if (!(above_tree.sectors.back() == under_tree.sectors.back())) continue;
+              const Tree kept_under = trimmed(cat, under_tree);
+              const Layout &out_rows = layout_of(cat, out_cod, kept_above.coupled);
+              const Layout &out_cols = layout_of(cat, out_dom, kept_under.coupled);
+              const int32_t new_row = out_rows.find(kept_above), new_col = out_cols.find(kept_under);
+              if (new_row < 0 || new_col < 0) throw LogicError("a kept tree of a trace is not in the layout it was trimmed from");
+              const int64_t inside_rows = out_rows.offsets[static_cast<size_t>(new_row) + 1] - out_rows.offsets[static_cast<size_t>(new_row)];
+              const int64_t inside_cols = out_cols.offsets[static_cast<size_t>(new_col) + 1] - out_cols.offsets[static_cast<size_t>(new_col)];
+              const int64_t copies = row_span / inside_rows;
+              for (const Outcome &closing : cat.outcomes(kept_above.coupled, cat.dual(kept_under.coupled)))
+              {
+                require_single_closing(cat, kept_above.coupled, kept_under.coupled, closing.sector, "the kept roots", "a trace");
+                Space out = make_space(s->cat, out_cod, out_dom, closing.sector);
+                const int32_t at = out->find(BlockKey{kept_above.coupled, kept_under.coupled, 0});
+                if (at < 0) throw LogicError("a trace lands outside its output");
+                const Block &ob = out->blocks[static_cast<size_t>(at)];
+                by_charge[closing.sector].push_back(Contribution{
+                  blk.offset + rows.offsets[ri] * blk.cols + cols.offsets[ci],
+                  ob.offset + out_rows.offsets[static_cast<size_t>(new_row)] * ob.cols + out_cols.offsets[static_cast<size_t>(new_col)],
+                  inside_rows, inside_cols, copies, blk.cols, ob.cols});
+              }
+            }
+          }
+        }
+        std::vector<Value> out;
+        for (const auto &[charge, contributions] : by_charge)
+        {
+          Space space = make_space(s->cat, out_cod, out_dom, charge);
+          const int32_t dst = temp(space);
+          emit(Op{OpKind::zero, -1, -1, dst, 0, 0, space->size, v.phase});
+          // element (i, j) of the kept block gathers sum_c src[(i*copies + c) * stride + j*copies + c]
+          std::map<int64_t, std::vector<Term>> groups;
+          for (const Contribution &c : contributions)
+            for (int64_t i = 0; i < c.inside_rows; ++i)
+              for (int64_t j = 0; j < c.inside_cols; ++j)
+              {
+                std::vector<Term> &terms = groups[c.dst + i * c.dst_stride + j];
+                for (int64_t k = 0; k < c.copies; ++k)
+                  terms.push_back(Term{c.src + (i * c.copies + k) * c.src_stride + j * c.copies + k, 0, 1.0, 0.0});
+              }
+          Op op{OpKind::runs, v.buffer, -1, dst, static_cast<int64_t>(p_.chunks.size()), 0, space->size, v.phase};
+          for (const auto &[dst_at, terms] : groups)
+          {
+            p_.chunks.push_back(Chunk{dst_at, 1, 0, static_cast<int32_t>(p_.terms.size()), static_cast<int32_t>(terms.size())});
+            p_.terms.insert(p_.terms.end(), terms.begin(), terms.end());
+          }
+          op.count = static_cast<int64_t>(p_.chunks.size()) - op.begin;
+          emit(op);
+          out.push_back(Value{dst, space, nullptr, v.phase});
+        }
+        return out;
+      }
+
+      void add_into(const Value &v, int32_t dst)
+      {
+        const Value m = materialize(v);
+        emit(Op{OpKind::add, m.buffer, -1, dst, 0, 0, m.space->size, -1});
+      }
+
+      static void require_single_closing(const Category &cat, const Sector &above, const Sector &below,
+                                         const Sector &charge, const std::string &subject, const std::string &what)
+      {
+        if (cat.n_symbol(above, cat.dual(below), charge) > 1)
+          throw InvalidArgument(subject + " " + above.str() + " and " + below.str() + " close to " + charge.str() +
+                                " in more than one way, which " + what + " does not recouple yet");
+      }
+
+      Program &p_;
+
+    private:
+      void emit(const Op &op) { p_.ops.push_back(op); }
+
+      // The gather index of one step whose coefficients are all 1: after[i] = before[index[i]].
+      std::vector<int32_t> permutation_of(const Step &step)
+      {
+        Space before = step.before, after = step.after;
+        if (after->size > std::numeric_limits<int32_t>::max() || before->size > std::numeric_limits<int32_t>::max())
+          throw InvalidArgument("an arena of more than 2^31 entries");
+        std::vector<int32_t> back(static_cast<size_t>(after->size), -1);
+        for (const Block &blk : before->blocks)
+          for (const Shift &shift : step_plan(step, blk.key))
+          {
+            const int32_t t = after->find(shift.to);
+            if (t < 0) throw LogicError("a move lands outside the tensor it builds");
+            const int64_t ot = after->blocks[static_cast<size_t>(t)].offset;
+            for (const Piece &piece : shift.pieces)
+            {
+              if (piece.coefficient != cplx(1.0, 0.0)) throw LogicError("a permutation step with a coefficient");
+              for (int64_t i = 0; i < piece.run; ++i)
+              {
+                int32_t &slot = back[static_cast<size_t>(ot + piece.last + i * piece.to_step)];
+                if (slot >= 0) throw LogicError("a permutation step writes one entry twice");
+                slot = static_cast<int32_t>(blk.offset + piece.first + i * piece.from_step);
+              }
+            }
+          }
+        return back;
+      }
+
+      // One step with coefficients: the pieces of every block grouped by destination run.
+      void append_runs(const Step &step, int32_t src, int32_t dst, int32_t phase)
+      {
+        Space before = step.before, after = step.after;
+        struct RunKey
+        {
+          int64_t dst, step, len;
+          bool operator<(const RunKey &o) const { return std::tie(dst, step, len) < std::tie(o.dst, o.step, o.len); }
+        };
+        std::map<RunKey, std::vector<Term>> groups;
+        for (const Block &blk : before->blocks)
+          for (const Shift &shift : step_plan(step, blk.key))
+          {
+            const int32_t t = after->find(shift.to);
+            if (t < 0) throw LogicError("a move lands outside the tensor it builds");
+            const int64_t ot = after->blocks[static_cast<size_t>(t)].offset;
+            for (const Piece &piece : shift.pieces)
+              groups[RunKey{ot + piece.last, piece.to_step, piece.run}].push_back(
+                Term{blk.offset + piece.first, piece.from_step, piece.coefficient.real(), piece.coefficient.imag()});
+          }
+        // destination runs must not overlap; when they do the step is laid out entry by entry
+        std::vector<uint8_t> seen(static_cast<size_t>(after->size), 0);
+        bool overlap = false;
+        for (const auto &[k, terms] : groups)
+          for (int64_t i = 0; i < k.len && !overlap; ++i)
+          {
+            uint8_t &mark = seen[static_cast<size_t>(k.dst + i * k.step)];
+            overlap = mark != 0;
+            mark = 1;
+          }
+        if (overlap)
+        {
+          std::map<RunKey, std::vector<Term>> single;
+          for (const auto &[k, terms] : groups)
+            for (int64_t i = 0; i < k.len; ++i)
+            {
+              std::vector<Term> &into = single[RunKey{k.dst + i * k.step, 0, 1}];
+              for (const Term &t : terms) into.push_back(Term{t.src + i * t.src_step, 0, t.re, t.im});
+            }
+          groups = std::move(single);
+        }
+        Op op{OpKind::runs, src, -1, dst, static_cast<int64_t>(p_.chunks.size()), 0, after->size, phase};
+        for (const auto &[k, terms] : groups)
+          for (int64_t c0 = 0; c0 < k.len; c0 += kChunk)
+          {
+            p_.chunks.push_back(Chunk{k.dst + c0 * k.step, static_cast<int32_t>(std::min<int64_t>(kChunk, k.len - c0)),
+                                      static_cast<int32_t>(k.step), static_cast<int32_t>(p_.terms.size()),
+                                      static_cast<int32_t>(terms.size())});
+            for (const Term &t : terms)
+            {
+              p_.terms.push_back(Term{t.src + c0 * t.src_step, t.src_step, t.re, t.im});
+              if (t.im != 0.0) p_.complex_coefficients = true;
+            }
+            p_.moved_elements += std::min<int64_t>(kChunk, k.len - c0);
+          }
+        op.count = static_cast<int64_t>(p_.chunks.size()) - op.begin;
+        emit(op);
+      }
+    };
+
+    std::vector<int32_t> without(int32_t total, const std::vector<int32_t> &taken)
+    {
+      std::vector<bool> named(static_cast<size_t>(total), false);
+      for (int32_t leg : taken) named[static_cast<size_t>(leg)] = true;
+      std::vector<int32_t> out;
+      for (int32_t leg = 0; leg < total; ++leg)
+        if (!named[static_cast<size_t>(leg)]) out.push_back(leg);
+      return out;
+    }
+
+    void check_side(Space s, const std::vector<int32_t> &legs, const char *side)
+    {
+      std::vector<bool> named(static_cast<size_t>(s->nlegs()), false);
+      for (int32_t leg : legs)
+      {
+        if (leg < 0 || leg >= s->nlegs())
+          throw InvalidArgument("the leg " + std::to_string(leg) + " of the " + side + " tensor is out of range of its " +
+                                std::to_string(s->nlegs()) + " legs");
+        if (named[static_cast<size_t>(leg)])
+          throw InvalidArgument("the leg " + std::to_string(leg) + " of the " + side + " tensor is summed twice");
+        named[static_cast<size_t>(leg)] = true;
+      }
+    }
+
+    // tentorch/linalg/graded/contract.cpp:47-77 (the scalar type is checked by the caller)
+    void check_pairs(Space left, Space right, const std::vector<int32_t> &left_legs, const std::vector<int32_t> &right_legs)
+    {
+      if (left->cat != right->cat) throw InvalidArgument("a contraction needs both tensors over one category");
+      if (left_legs.size() != right_legs.size())
+        throw InvalidArgument("the two legs of a contraction must be given in pairs, got " + std::to_string(left_legs.size()) +
+                              " and " + std::to_string(right_legs.size()));
+      check_side(left, left_legs, "first");
+      check_side(right, right_legs, "second");
+      const std::vector<Leg> la = left->legs(), ra = right->legs();
+      for (size_t at = 0; at < left_legs.size(); ++at)
+      {
+        Leg one = la[static_cast<size_t>(left_legs[at])], other = ra[static_cast<size_t>(right_legs[at])];
+        if (one != other)
+          throw InvalidArgument("the pair at position " + std::to_string(at) + " joins the leg " + std::to_string(left_legs[at]) +
+                                " of the first tensor, over " + render(one->sectors) + ", to the leg " +
+                                std::to_string(right_legs[at]) + " of the second, over " + render(other->sectors) +
+                                ", and the two do not name one space");
+      }
+    }
+
+    void finish(Program &p, Builder &b, const std::vector<Value> &results)
+    {
+      if (results.empty()) throw LogicError("a program without a result");
+      p.output_space = results.front().space;
+      const int32_t out = b.output_buffer(p.output_space);
+      // a result computed by the core (or a prepared value) writes straight into the output
+      Value first = results.front();
+      if (first.pending)
+        b.materialize(first, out);
+      else if (p.buffers[static_cast<size_t>(first.buffer)].kind == BufferKind::temp && first.phase < 0 &&
+               !p.ops.empty() && p.ops.back().dst == first.buffer)
+        p.ops.back().dst = out, p.buffers[static_cast<size_t>(first.buffer)].size = 0;
+      else
+        b.materialize(first, out);
+      for (size_t i = 1; i < results.size(); ++i) b.add_into(results[i], out);
+      // an operand's prepared value is the last buffer its phase writes that the core reads
+      p.prepared.assign(static_cast<size_t>(p.n_inputs), -1);
+      for (const Op &op : p.ops)
+        if (op.phase < 0)
+          for (int32_t src : {op.src, op.src2})
+            if (src >= 0)
+            {
+              const Buffer &buf = p.buffers[static_cast<size_t>(src)];
+              if (buf.kind == BufferKind::temp)
+                for (const Op &producer : p.ops)
+                  if (producer.dst == src && producer.phase >= 0)
+                  {
+                    // more than one prepared buffer per operand: leave the operand unprepared
+                    int32_t &slot = p.prepared[static_cast<size_t>(producer.phase)];
+                    slot = (slot == -1 || slot == src) ? src : -2;
+                  }
+            }
+      for (int32_t i = 0; i < p.n_inputs; ++i)
+        if (p.prepared[static_cast<size_t>(i)] >= 0)
+          p.buffers[static_cast<size_t>(p.prepared[static_cast<size_t>(i)])].prepared_of = i;
+        else
+          p.prepared[static_cast<size_t>(i)] = -1;
+      // ops of an unprepared operand's phase run as core ops
+      for (Op &op : p.ops)
+        if (op.phase >= 0 && p.prepared[static_cast<size_t>(op.phase)] < 0) op.phase = -1;
+    }
+
+    // --------------------------------------------------------------------------------------
+    // einsum helpers (tentorch/linalg/graded/einsum.cpp:27-301)
+    // --------------------------------------------------------------------------------------
+
+    struct SideSpec
+    {
+      std::vector<char> labels;
+      std::vector<bool> above;
+    };
+
+    SideSpec side_of(const std::string &text)
+    {
+      SideSpec out;
+      for (const char letter : text)
+      {
+        if (letter == ' ') continue;
+        out.labels.push_back(static_cast<char>(std::tolower(static_cast<unsigned char>(letter))));
+        out.above.push_back(letter >= 'A' && letter <= 'Z');
+      }
+      return out;
+    }
+
+    bool holds(const std::vector<char> &labels, char label)
+    {
+      return std::find(labels.begin(), labels.end(), label) != labels.end();
+    }
+
+    int32_t position_of(const std::vector<char> &labels, char label)
+    {
+      const auto it = std::find(labels.begin(), labels.end(), label);
+      if (it == labels.end()) throw LogicError(std::string("the label '") + label + "' left the equation");
+      return static_cast<int32_t>(it - labels.begin());
+    }
+
+    std::vector<char> union_of(const std::vector<char> &a, const std::vector<char> &b)
+    {
+      std::vector<char> out = a;
+      for (char l : b)
+        if (!holds(out, l)) out.push_back(l);
+      return out;
+    }
+
+    std::vector<char> shared_of(const std::vector<char> &a, const std::vector<char> &b)
+    {
+      std::vector<char> out;
+      for (char l : a)
+        if (holds(b, l)) out.push_back(l);
+      return out;
+    }
+
+    std::vector<char> product_labels(const std::vector<char> &a, const std::vector<char> &b)
+    {
+      const std::vector<char> shared = shared_of(a, b);
+      std::vector<char> out;
+      for (char l : union_of(a, b))
+        if (!holds(shared, l)) out.push_back(l);
+      return out;
+    }
+
+    double leg_size(const Category &cat, Leg leg)
+    {
+      double out = 0;
+      for (size_t i = 0; i < leg->sectors.size(); ++i) out += static_cast<double>(leg->mult[i]) * cat.q_dim(leg->sectors[i]);
+      return out;
+    }
+
+    double tensor_size(const std::vector<char> &labels, const std::map<char, double> &dims)
+    {
+      double out = 1;
+      for (char l : labels) out *= dims.at(l);
+      return out;
+    }
+
+    // tentorch/linalg/graded/einsum.cpp:216-301
+    std::vector<int32_t> fold_order(const std::vector<std::vector<char>> &inputs, const std::map<char, double> &dims)
+    {
+      const int32_t count = static_cast<int32_t>(inputs.size());
+      std::vector<int32_t> order;
+      if (count <= 12)
+      {
+        const int64_t masks = int64_t(1) << (count - 1);
+        std::vector<std::vector<char>> labels(static_cast<size_t>(masks), inputs.front());
+        for (int64_t mask = 1; mask < masks; ++mask)
+        {
+          const int bit = __builtin_ctzll(static_cast<unsigned long long>(mask));
+          labels[static_cast<size_t>(mask)] = union_of(labels[static_cast<size_t>(mask ^ (int64_t(1) << bit))], inputs[static_cast<size_t>(bit + 1)]);
+        }
+        for (int pass = 0; pass < 2; ++pass)
+        {
+          std::vector<double> cost(static_cast<size_t>(masks), std::numeric_limits<double>::infinity());
+          std::vector<int64_t> summed(static_cast<size_t>(masks), 0), last(static_cast<size_t>(masks), 0);
+          cost[0] = 0;
+          for (int64_t mask = 1; mask < masks; ++mask)
+            for (int64_t bit = 0; bit < count - 1; ++bit)
+              if (mask & (int64_t(1) << bit))
+              {
+                const int64_t prev = mask ^ (int64_t(1) << bit);
+                const std::vector<char> shared = shared_of(labels[static_cast<size_t>(prev)], inputs[static_cast<size_t>(bit + 1)]);
+                if (pass == 0 && shared.empty()) continue;
+                const double candidate = cost[static_cast<size_t>(prev)] + tensor_size(labels[static_cast<size_t>(mask)], dims);
+                const size_t m = static_cast<size_t>(mask);
+                const bool better = candidate < cost[m] ||
+                                    (candidate == cost[m] && static_cast<int64_t>(shared.size()) > summed[m]) ||
+                                    (candidate == cost[m] && static_cast<int64_t>(shared.size()) == summed[m] && bit > last[m]);
+                if (better)
+                {
+                  cost[m] = candidate;
+                  summed[m] = static_cast<int64_t>(shared.size());
+                  last[m] = bit;
+                }
+              }
+          if (cost[static_cast<size_t>(masks - 1)] == std::numeric_limits<double>::infinity()) continue;
+          for (int64_t mask = masks - 1; mask; mask ^= int64_t(1) << last[static_cast<size_t>(mask)])
+            order.push_back(static_cast<int32_t>(last[static_cast<size_t>(mask)] + 1));
+          order.push_back(0);
+          std::reverse(order.begin(), order.end());
+          return order;
+        }
+      }
+      std::vector<bool> taken(inputs.size(), false);
+      std::vector<char> live = inputs.front();
+      order.push_back(0);
+      taken[0] = true;
+      for (int32_t step = 1; step < count; ++step)
+      {
+        int32_t best = -1;
+        double best_size = 0;
+        bool found = false;
+        for (int pass = 0; pass < 2 && !found; ++pass)
+          for (int32_t at = 0; at < count; ++at)
+          {
+            if (taken[static_cast<size_t>(at)]) continue;
+            if (shared_of(live, inputs[static_cast<size_t>(at)]).empty() != (pass == 1)) continue;
+            const double size = tensor_size(union_of(live, inputs[static_cast<size_t>(at)]), dims);
+            if (!found || size < best_size)
+            {
+              found = true;
+              best = at;
+              best_size = size;
+            }
+          }
+        order.push_back(best);
+        taken[static_cast<size_t>(best)] = true;
+        live = union_of(live, inputs[static_cast<size_t>(best)]);
+      }
+      return order;
+    }
+
+    constexpr int64_t kMaxCharges = 4096;
+  } // namespace
+
+  std::shared_ptr<Program> compile_place(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
+  {
+    auto p = std::make_shared<Program>();
+    p->n_inputs = 1;
+    p->input_spaces = {space};
+    Builder b(*p);
+    Value v = b.input(0, space);
+    v.phase = -1;
+    finish(*p, b, {b.place(v, above, below)});
+    return p;
+  }
+
+  std::shared_ptr<Program> compile_contract(Space left, Space right, const std::vector<int32_t> &left_legs,
+                                            const std::vector<int32_t> &right_legs, bool has_charge, const Sector &charge_in)
+  {
+    const Category &cat = *left->cat;
+    Sector charge = charge_in;
+    if (!has_charge)
+    {
+      if (!(right->qtotal == cat.trivial()))
+        throw InvalidArgument("the second tensor of a contraction must carry the trivial charge");
+      charge = left->qtotal;
+    }
+    check_pairs(left, right, left_legs, right_legs);
+    if (cat.n_symbol(left->qtotal, right->qtotal, charge) == 0)
+      throw InvalidArgument("the charge " + charge.str() + " is not an outcome of " + left->qtotal.str() + " and " +
+                            right->qtotal.str());
+    Builder::require_single_closing(cat, left->qtotal, right->qtotal, charge, "the charges", "a contraction");
+    auto p = std::make_shared<Program>();
+    p->n_inputs = 2;
+    p->input_spaces = {left, right};
+    Builder b(*p);
+    const Value l = b.input(0, left), r = b.input(1, right);
+    const Value above = b.place(l, without(left->nlegs(), left_legs), left_legs);
+    const Value under = b.place(r, right_legs, without(right->nlegs(), right_legs));
+    finish(*p, b, {b.contract_aligned(above, under, charge)});
+    return p;
+  }
+
+  std::shared_ptr<Program> compile_einsum(const std::string &spec, const std::vector<Space> &operands, bool has_charge,
+                                          const Sector &charge_in)
+  {
+    if (operands.empty()) throw InvalidArgument("an einsum needs at least one operand");
+    const size_t at_arrow = spec.find("->");
+    if (at_arrow == std::string::npos) throw InvalidArgument("the equation '" + spec + "' does not say what it leaves");
+    std::vector<SideSpec> groups;
+    const std::string left = spec.substr(0, at_arrow);
+    size_t start = 0;
+    while (true)
+    {
+      const size_t comma = left.find(',', start);
+      groups.push_back(side_of(left.substr(start, comma == std::string::npos ? std::string::npos : comma - start)));
+      if (comma == std::string::npos) break;
+      start = comma + 1;
+    }
+    const SideSpec output = side_of(spec.substr(at_arrow + 2));
+    if (groups.size() != operands.size())
+      throw InvalidArgument("the equation '" + spec + "' names " + std::to_string(groups.size()) + " operands but got " +
+                            std::to_string(operands.size()));
+    const Category &cat = *operands.front()->cat;
+    const Sector charge = has_charge ? charge_in : cat.trivial();
+    for (size_t at = 0; at < operands.size(); ++at)
+    {
+      if (operands[at]->cat != &cat) throw InvalidArgument("an einsum needs every operand over one category");
+      if (groups[at].labels.size() != static_cast<size_t>(operands[at]->nlegs()))
+        throw InvalidArgument("the group " + std::to_string(at) + " of '" + spec + "' names " +
+                              std::to_string(groups[at].labels.size()) + " legs but the tensor has " +
+                              std::to_string(operands[at]->nlegs()));
+    }
+    std::vector<char> seen;
+    for (const SideSpec &g : groups)
+      for (char label : g.labels)
+      {
+        if (std::count(seen.begin(), seen.end(), label) >= 2)
+          throw InvalidArgument(std::string("the label '") + label + "' of '" + spec + "' names more than two legs");
+        seen.push_back(label);
+      }
+    for (char label : seen)
+    {
+      const auto count = std::count(seen.begin(), seen.end(), label);
+      if (count == 1 && !holds(output.labels, label))
+        throw InvalidArgument(std::string("the label '") + label + "' of '" + spec +
+                              "' names one leg but is not kept in the output, which would leave it open");
+      if (count == 2 && holds(output.labels, label))
+        throw InvalidArgument(std::string("the label '") + label + "' of '" + spec + "' is summed over and still kept");
+    }
+    for (char label : output.labels)
+      if (std::count(seen.begin(), seen.end(), label) != 1)
+        throw InvalidArgument(std::string("the output label '") + label + "' of '" + spec + "' does not name a leg of the operands");
+    std::vector<char> summed;
+    for (char label : seen)
+      if (std::count(seen.begin(), seen.end(), label) == 2 && !holds(summed, label)) summed.push_back(label);
+
+    auto p = std::make_shared<Program>();
+    p->n_inputs = static_cast<int32_t>(operands.size());
+    p->input_spaces = operands;
+    Builder b(*p);
+    // laid_out (einsum.cpp:65-81)
+    std::vector<std::vector<Value>> prepared;
+    std::vector<std::vector<char>> labels_of;
+    for (size_t at = 0; at < operands.size(); ++at)
+    {
+      Space s = operands[at];
+      const int32_t codomain = static_cast<int32_t>(s->codomain.size());
+      std::vector<int32_t> above, below;
+      for (int32_t leg = 0; leg < s->nlegs(); ++leg)
+      {
+        const bool stays = holds(summed, groups[at].labels[static_cast<size_t>(leg)]) ? leg < codomain
+                                                                                       : static_cast<bool>(groups[at].above[static_cast<size_t>(leg)]);
+        (stays ? above : below).push_back(leg);
+      }
+      std::vector<char> labels;
+      for (int32_t leg : above) labels.push_back(groups[at].labels[static_cast<size_t>(leg)]);
+      for (int32_t leg : below) labels.push_back(groups[at].labels[static_cast<size_t>(leg)]);
+      std::vector<Value> alternatives{b.place(b.input(static_cast<int32_t>(at), s), above, below)};
+      // self contractions (einsum.cpp:386-439)
+      while (true)
+      {
+        int32_t first = -1, second = -1;
+        for (size_t one = 0; one < labels.size() && first < 0; ++one)
+          for (size_t other = one + 1; other < labels.size(); ++other)
+            if (labels[one] == labels[other])
+            {
+              first = static_cast<int32_t>(one);
+              second = static_cast<int32_t>(other);
+              break;
+            }
+        if (first < 0) break;
+        Space front = alternatives.front().space;
+        const int32_t codomain_now = static_cast<int32_t>(front->codomain.size());
+        const std::vector<Leg> legs = front->legs();
+        if (legs[static_cast<size_t>(first)] != legs[static_cast<size_t>(second)])
+          throw InvalidArgument(std::string("the label '") + labels[static_cast<size_t>(first)] + "' of '" + spec +
+                                "' names two different spaces in the operand " + std::to_string(at) +
+                                ", and a trace sums a space with itself");
+        const int32_t above_leg = first < codomain_now ? first : second;
+        const int32_t below_leg = first < codomain_now ? second : first;
+        std::vector<int32_t> above2, below2;
+        for (int32_t leg = 0; leg < front->nlegs(); ++leg)
+          if (leg != above_leg && leg != below_leg) (leg < codomain_now ? above2 : below2).push_back(leg);
+        above2.push_back(above_leg);
+        below2.push_back(below_leg);
+        std::vector<Value> traced;
+        for (const Value &alt : alternatives)
+          for (const Value &t : b.partial_trace(b.place(alt, above2, below2))) traced.push_back(t);
+        alternatives = std::move(traced);
+        labels.erase(labels.begin() + second);
+        labels.erase(labels.begin() + first);
+      }
+      prepared.push_back(std::move(alternatives));
+      labels_of.push_back(std::move(labels));
+    }
+    // the output legs must close to the charge (einsum.cpp:525-544)
+    std::vector<Leg> above_legs, below_legs;
+    for (size_t one = 0; one < output.labels.size(); ++one)
+      for (size_t at = 0; at < labels_of.size(); ++at)
+        if (holds(labels_of[at], output.labels[one]))
+        {
+          if (prepared[at].empty()) break;
+          const Leg leg = prepared[at].front().space->legs()[static_cast<size_t>(position_of(labels_of[at], output.labels[one]))];
+          (output.above[one] ? above_legs : below_legs).push_back(leg);
+          break;
+        }
+    bool closes = output.labels.empty();
+    for (const Sector &a : reachable_charges(cat, above_legs))
+      for (const Sector &c : reachable_charges(cat, below_legs))
+        if (cat.n_symbol(a, cat.dual(c), charge) > 0) closes = true;
+    if (!closes) throw InvalidArgument("the output legs of '" + spec + "' cannot close to " + charge.str());
+    size_t combinations = 1;
+    for (const std::vector<Value> &alts : prepared)
+    {
+      if (alts.empty()) throw InvalidArgument("the traces of '" + spec + "' leave nothing to sum");
+      if (static_cast<int64_t>(alts.size()) > kMaxCharges / static_cast<int64_t>(combinations))
+        throw InvalidArgument("the traces of '" + spec + "' leave more than " + std::to_string(kMaxCharges) +
+                              " combinations of charges, which is more than this sums");
+      combinations *= alts.size();
+    }
+    std::map<char, double> dims;
+    for (size_t at = 0; at < labels_of.size(); ++at)
+    {
+      const std::vector<Leg> legs = prepared[at].front().space->legs();
+      for (size_t leg = 0; leg < labels_of[at].size(); ++leg) dims[labels_of[at][leg]] = leg_size(cat, legs[leg]);
+    }
+    const std::vector<int32_t> order = fold_order(labels_of, dims);
+
+    std::vector<Value> results;
+    std::vector<size_t> choice(prepared.size(), 0);
+    while (true)
+    {
+      // contract_path (einsum.cpp:351-376)
+      std::vector<char> labels = labels_of.front();
+      std::vector<Value> states{prepared[0][choice[0]]};
+      for (size_t step = 1; step < order.size(); ++step)
+      {
+        const int32_t at = order[step];
+        const Value right = prepared[static_cast<size_t>(at)][choice[static_cast<size_t>(at)]];
+        const std::vector<char> &right_labels = labels_of[static_cast<size_t>(at)];
+        // combine (einsum.cpp:306-345)
+        const std::vector<char> shared = shared_of(labels, right_labels);
+        std::vector<int32_t> left_legs, right_legs;
+        for (char l : shared)
+        {
+          left_legs.push_back(position_of(labels, l));
+          right_legs.push_back(position_of(right_labels, l));
+        }
+        std::vector<Value> folded;
+        for (const Value &lv : states)
+        {
+          check_pairs(lv.space, right.space, left_legs, right_legs);
+          const Value above = b.place(lv, without(lv.space->nlegs(), left_legs), left_legs);
+          const Value under = b.place(right, right_legs, without(right.space->nlegs(), right_legs));
+          std::vector<Sector> closings;
+          for (const Outcome &o : cat.outcomes(lv.space->qtotal, right.space->qtotal))
+            if (std::find(closings.begin(), closings.end(), o.sector) == closings.end()) closings.push_back(o.sector);
+          for (const Sector &closed : closings)
+          {
+            Builder::require_single_closing(cat, lv.space->qtotal, right.space->qtotal, closed, "the charges", "a contraction");
+            folded.push_back(b.contract_aligned(above, under, closed));
+          }
+        }
+        if (static_cast<int64_t>(folded.size()) > kMaxCharges)
+          throw InvalidArgument("the products of the equation leave more than " + std::to_string(kMaxCharges) +
+                                " charges to sum, which is more than this takes");
+        labels = product_labels(labels, right_labels);
+        states = std::move(folded);
+      }
+      std::vector<int32_t> above, below;
+      for (size_t at = 0; at < output.labels.size(); ++at)
+        (output.above[at] ? above : below).push_back(position_of(labels, output.labels[at]));
+      for (const Value &state : states)
+      {
+        if (!(state.space->qtotal == charge)) continue;
+        const Value placed = b.place(state, above, below);
+        if (placed.space->blocks.empty()) continue;
+        results.push_back(placed);
+      }
+      size_t digit = 0;
+      while (digit < choice.size() && ++choice[digit] == prepared[digit].size())
+      {
+        choice[digit] = 0;
+        ++digit;
+      }
+      if (digit == choice.size()) break;
+    }
+    if (results.empty()) throw InvalidArgument("no way for the charges of '" + spec + "' to fuse to " + charge.str());
+    finish(*p, b, results);
+    return p;
+  }
+
+} // namespace ttg

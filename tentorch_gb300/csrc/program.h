@@ -1,0 +1,128 @@
+// The plan compiler: a place, a contraction or a whole einsum compiled once per shape into a
+// device program, a short list of operations over arenas with their descriptor tables.
+//
+//   GATHER   dst[i] = src[index[i]] (index -1 writes 0): a composed chain of leg moves whose every
+//            coefficient is 1 (abelian groups), one pass however many steps the chain has.
+//   RUNS     dst[d + t*ds] (+)= sum_k c_k src[s_k + t*ss_k] over chunks of runs: one leg-move step
+//            (or a trace) with F/R coefficients, grouped by destination so the pass is atomic free.
+//   GEMM     C_blk = sum_pairs A_blk(m x k) B_blk(k x n) over all output blocks of a contraction in
+//            one grouped launch (every output block written, zero when it has no pair).
+//   ADD      dst += src over a whole arena (the sum over charge alternatives of an einsum).
+//   COPY     dst = src.
+//   ZERO     dst = 0.
+//
+// Buffers are the operands, the output, and temporaries placed in one caller-provided workspace.
+// Operations that depend on one operand alone form that operand's "prepare" phase; a caller can
+// run it once and pass the prepared arena on later calls (the loop-invariant head and tail of a
+// Lanczos matvec).
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+namespace ttg
+{
+  enum class OpKind : int32_t
+  {
+    zero = 0,
+    gather = 1,
+    runs = 2,
+    gemm = 3,
+    add = 4,
+    copy = 5,
+  };
+
+  struct Op
+  {
+    OpKind kind;
+    int32_t src = -1, src2 = -1, dst = -1;
+    int64_t begin = 0, count = 0;  // range in the op's descriptor table
+    int64_t elements = 0;          // destination elements (zero/add/copy/gather)
+    int32_t phase = -1;            // operand whose prepare phase this belongs to, -1 for the core
+  };
+
+  // One destination run of a RUNS pass, already cut to at most kChunk elements.
+  struct Chunk
+  {
+    int64_t dst;
+    int32_t len;
+    int32_t dst_step;
+    int32_t term_begin;
+    int32_t term_count;
+  };
+  struct Term
+  {
+    int64_t src;
+    int64_t src_step;
+    double re, im;
+  };
+  constexpr int32_t kChunk = 128;
+
+  // One output block of a grouped GEMM and the block pairs summed into it.
+  struct GemmBlock
+  {
+    int64_t c;
+    int32_t m, n;
+    int32_t pair_begin, pair_count;
+  };
+  struct GemmPair
+  {
+    int64_t a, b;
+    int32_t k, pad;
+  };
+
+  enum class BufferKind : int32_t
+  {
+    input = 0,
+    output = 1,
+    temp = 2,
+  };
+
+  struct Buffer
+  {
+    BufferKind kind;
+    int32_t index;   // operand number for inputs
+    int64_t offset;  // elements into the workspace for temporaries
+    int64_t size;    // elements
+    int32_t prepared_of = -1;  // the operand whose prepared value this temporary holds
+  };
+
+  struct Program
+  {
+    int32_t n_inputs = 0;
+    std::vector<Space> input_spaces;
+    Space output_space = nullptr;
+    std::vector<Buffer> buffers;
+    std::vector<Op> ops;
+    int64_t workspace = 0;  // elements
+    // per operand: the buffer holding its prepared value (the input itself when no op prepares it)
+    std::vector<int32_t> prepared;
+    // descriptor tables
+    std::vector<int32_t> gather_index;
+    std::vector<Chunk> chunks;
+    std::vector<Term> terms;
+    std::vector<GemmBlock> gemm_blocks;
+    std::vector<GemmPair> gemm_pairs;
+    // bookkeeping for the roofline: useful flops of the GEMMs, elements moved by recouplings
+    double gemm_flops = 0;
+    int64_t moved_elements = 0;
+    bool complex_coefficients = false;  // some RUNS term has an imaginary part
+  };
+
+  // Compile one leg move of an arena of `space` into `above` / `below`.
+  std::shared_ptr<Program> compile_place(Space space, const std::vector<int32_t> &above,
+                                         const std::vector<int32_t> &below);
+  // Compile a contraction (tentorch/linalg/graded/contract.cpp:117-175).  `has_charge` false takes
+  // the charge of `left` and requires a neutral `right`.
+  std::shared_ptr<Program> compile_contract(Space left, Space right, const std::vector<int32_t> &left_legs,
+                                            const std::vector<int32_t> &right_legs, bool has_charge,
+                                            const Sector &charge);
+  // Compile an einsum (tentorch/linalg/graded/einsum.cpp:444-605).
+  std::shared_ptr<Program> compile_einsum(const std::string &spec, const std::vector<Space> &operands,
+                                          bool has_charge, const Sector &charge);
+
+} // namespace ttg

@@ -1,0 +1,401 @@
+'''
+The contraction path and the linear algebra over block-sparse tensors, with the Python surface of
+the reference: `einsum(spec, *tensors, outcharge=None)`, `contract(left, right, left_legs,
+right_legs, charge=None)`, `Tensor.place`, `inner`, `norm`, `is_close`, `svd`, `svdvals`, `qr`,
+`rq` (tentorch/_ext/bindings.cpp:330-431).
+
+`einsum`, `contract` and `place` compile a plan once per combination of operand spaces (the
+engine caches it) and run it on the tensors' CUDA device, on the current torch stream, with no
+host synchronisation.  An operand's "prepare" work (the leg moves that depend on it alone) is
+cached against the operand's arena and its version counter, so a loop that applies the same
+operator to changing vectors (the Lanczos matvec) recouples the operator once.
+
+Block products run in FP64 by default; `precision(k)` switches them to split products on the
+tensor cores with k bf16 slices per operand (see gemm_split.cu).
+'''
+from __future__ import annotations
+
+import contextlib
+import ctypes
+import math
+import weakref
+from typing import Optional
+
+import torch
+
+from tentorch_gb300._lib import check, f64, i32, i64, ints32, lib, pointers, vp
+from tentorch_gb300.symmetry import Leg, _label
+from tentorch_gb300.tensor import BlockKey, Space, Tensor
+
+_DTYPE = {torch.float64: 0, torch.complex128: 1}
+_precision = 0
+
+
+def set_precision(slices: int) -> None:
+    '''0: FP64 block products; k in 1..8: split products with k bf16 slices per operand.'''
+    global _precision
+    if not 0 <= int(slices) <= 8:
+        raise ValueError(f'precision is 0 (FP64) or 1..8 slices, not {slices}')
+    _precision = int(slices)
+
+
+def get_precision() -> int:
+    return _precision
+
+
+@contextlib.contextmanager
+def precision(slices: int):
+    '''Run the block products inside the block with `slices` bf16 slices (0: FP64).'''
+    old = _precision
+    set_precision(slices)
+    try:
+        yield
+    finally:
+        set_precision(old)
+
+
+class Plan:
+    '''A compiled program: its output space, workspace and the size of each operand's prepared
+    arena.'''
+    __slots__ = ('handle', 'cat', 'out_space', 'workspace', 'flops', 'moved', 'n_ops', 'prepared', '__weakref__')
+
+    def __init__(self, handle, cat):
+        self.handle, self.cat = handle, cat
+        space, ws, flops, moved, ops = i32(), i64(), f64(), i64(), i32()
+        check(lib.tt_plan_info(handle, ctypes.byref(space), ctypes.byref(ws), ctypes.byref(flops), ctypes.byref(moved),
+                               ctypes.byref(ops)))
+        self.out_space = Space._load(cat, space.value)
+        self.workspace, self.flops, self.moved, self.n_ops = ws.value, flops.value, moved.value, ops.value
+        self.prepared = []
+
+    def prepared_size(self, operand: int) -> int:
+        n = i64()
+        check(lib.tt_plan_prepared_size(self.handle, operand, ctypes.byref(n)))
+        return n.value
+
+
+_plans = {}
+# (plan handle, operand) -> (weakref to the operand arena, its version, the prepared arena)
+_prepared = {}
+
+
+def _plan(key, build, cat) -> Plan:
+    plan = _plans.get(key)
+    if plan is None:
+        handle = vp()
+        check(build(ctypes.byref(handle)))
+        plan = Plan(handle, cat)
+        _plans[key] = plan
+    return plan
+
+
+def _check_device(tensors) -> None:
+    dtype, device = tensors[0].dtype, tensors[0].device
+    for t in tensors:
+        if t.dtype != dtype:
+            raise ValueError('a contraction needs both tensors of one scalar type')
+        if t.device != device:
+            raise ValueError('a contraction needs every tensor on one device')
+    if device.type != 'cuda':
+        raise RuntimeError('tentorch_gb300 computes on a CUDA device; these tensors live on the host '
+                           '(move them with .to("cuda"))')
+
+
+def _workspace(plan: Plan, tensors) -> Optional[torch.Tensor]:
+    if plan.workspace <= 0:
+        return None
+    return torch.empty(plan.workspace, dtype = tensors[0].dtype, device = tensors[0].device)
+
+
+def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws) -> Optional[torch.Tensor]:
+    size = plan.prepared_size(operand)
+    if size <= 0:
+        return None
+    key = (plan.handle.value, operand)
+    held = _prepared.get(key)
+    data = tensor._data
+    if held is not None and held[0]() is data and held[1] == data._version:
+        return held[2]
+    arena = torch.empty(size, dtype = data.dtype, device = data.device)
+    stream = torch.cuda.current_stream(data.device).cuda_stream
+    check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
+                              ws.data_ptr() if ws is not None else None, stream))
+    _prepared[key] = (weakref.ref(data), data._version, arena)
+    return arena
+
+
+def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool = True) -> Tensor:
+    '''Execute a plan on the operands' device and return the output tensor.'''
+    _check_device(tensors)
+    data0 = tensors[0]._data
+    if out is None:
+        out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = data0.dtype, device = data0.device))
+    ws = _workspace(plan, tensors)
+    prepared = [(_prepared_arena(plan, i, t, ws) if reuse_prepared else None) for i, t in enumerate(tensors)]
+    inputs = pointers(t._data.data_ptr() for t in tensors)
+    prep = pointers((p.data_ptr() if p is not None else None) for p in prepared)
+    stream = torch.cuda.current_stream(data0.device).cuda_stream
+    check(lib.tt_plan_execute(plan.handle, _DTYPE[data0.dtype], _precision, inputs, prep, out._data.data_ptr(),
+                              ws.data_ptr() if ws is not None else None, stream))
+    return out
+
+
+def place(tensor: Tensor, above, below = None) -> Tensor:
+    '''tentorch/tensors/place.cpp:183-247'''
+    total = tensor.nlegs()
+    above = [int(a) for a in above]
+    if below is None:
+        named = set(a for a in above if 0 <= a < total)
+        below = [leg for leg in range(total) if leg not in named]
+    below = [int(b) for b in below]
+    a, na = ints32(above)
+    b, nb = ints32(below)
+    plan = _plan(('place', tensor._space.id, tuple(above), tuple(below)),
+                 lambda out: lib.tt_plan_place(tensor._space.id, na, a, nb, b, out), tensor.cat)
+    if plan.n_ops == 0:
+        return tensor
+    return run(plan, [tensor], reuse_prepared = False)
+
+
+def contract(left: Tensor, right: Tensor, left_legs, right_legs, charge = None) -> Tensor:
+    '''tentorch/linalg/graded/contract.cpp:117-175'''
+    if left.cat is not right.cat:
+        raise ValueError('a contraction needs both tensors over one category')
+    if left.dtype != right.dtype:
+        raise ValueError('a contraction needs both tensors of one scalar type')
+    left_legs, right_legs = [int(x) for x in left_legs], [int(x) for x in right_legs]
+    has = charge is not None
+    q = _label(charge) if has else 0
+    la, n = ints32(left_legs)
+    ra, m = ints32(right_legs)
+    if n != m:
+        raise ValueError(f'the two legs of a contraction must be given in pairs, got {n} and {m}')
+    plan = _plan(('contract', left._space.id, right._space.id, tuple(left_legs), tuple(right_legs), has, q),
+                 lambda out: lib.tt_plan_contract(left._space.id, right._space.id, n, la, ra, int(has), q, out),
+                 left.cat)
+    return run(plan, [left, right])
+
+
+def einsum(spec: str, *tensors: Tensor, **options) -> Tensor:
+    '''tentorch/linalg/graded/einsum.cpp:444-605 with the binding's keyword handling
+    (tentorch/_ext/bindings.cpp:347-361): only `outcharge` is accepted.'''
+    for name in options:
+        if name != 'outcharge':
+            raise ValueError(f"einsum does not take the keyword '{name}'")
+    outcharge = options.get('outcharge')
+    if not tensors:
+        raise ValueError('an einsum needs at least one operand')
+    cat = tensors[0].cat
+    for t in tensors:
+        if t.cat is not cat:
+            raise ValueError('an einsum needs every operand over one category')
+    has = outcharge is not None
+    q = _label(outcharge) if has else 0
+    ids, n = ints32(t._space.id for t in tensors)
+    plan = _plan(('einsum', spec, tuple(t._space.id for t in tensors), has, q),
+                 lambda out: lib.tt_plan_einsum(spec.encode(), n, ids, int(has), q, out), cat)
+    return run(plan, list(tensors))
+
+
+def plan_of(spec: str, *tensors: Tensor, outcharge = None) -> Plan:
+    '''The compiled plan an einsum of these operands runs (for timing and the roofline).'''
+    has = outcharge is not None
+    q = _label(outcharge) if has else 0
+    ids, n = ints32(t._space.id for t in tensors)
+    return _plan(('einsum', spec, tuple(t._space.id for t in tensors), has, q),
+                 lambda out: lib.tt_plan_einsum(spec.encode(), n, ids, int(has), q, out), tensors[0].cat)
+
+
+# ---------------------------------------------------------------------------------------------
+# scalar products (tentorch/linalg/graded/compare.cpp)
+# ---------------------------------------------------------------------------------------------
+
+
+def _same_legs(a: Tensor, b: Tensor) -> None:
+    if a.cat is not b.cat:
+        raise ValueError('a scalar product needs both tensors over one category')
+    if a._space.codomain != b._space.codomain or a._space.domain != b._space.domain:
+        raise ValueError('a scalar product needs both tensors with the same legs')
+
+
+def inner_device(a: Tensor, b: Tensor) -> torch.Tensor:
+    '''<a, b> as a 0-d device tensor, with no host synchronisation (the arena padding is zero).'''
+    _same_legs(a, b)
+    if a.qtotal != b.qtotal:
+        return torch.zeros((), dtype = a.dtype, device = a.device)
+    return torch.vdot(a._data, b._data)
+
+
+def inner(a: Tensor, b: Tensor) -> complex:
+    '''tentorch/linalg/graded/compare.cpp:31-43'''
+    return complex(inner_device(a, b).item())
+
+
+def norm(t: Tensor) -> float:
+    '''tentorch/linalg/graded/compare.cpp:45'''
+    return math.sqrt(abs(inner(t, t)))
+
+
+def is_close(first: Tensor, second: Tensor, rtol: float = 1e-10, atol: float = 1e-12) -> bool:
+    '''tentorch/linalg/graded/compare.cpp:12-29'''
+    if first.cat is not second.cat or first.qtotal != second.qtotal:
+        return False
+    if first._space is not second._space:
+        return False
+    return bool(torch.allclose(first._data, second._data.to(first.device), rtol = rtol, atol = atol))
+
+
+# ---------------------------------------------------------------------------------------------
+# splittings (tentorch/linalg/graded/svd.cpp)
+# ---------------------------------------------------------------------------------------------
+
+
+def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
+    '''tentorch/linalg/graded/svd.cpp:41-177: per-block SVD on the device, one host read of all the
+    singular values, a global ranking, truncation, and the +-q pairing of the bond.'''
+    if absorb not in (0, 1, 2, 3):
+        raise ValueError(f'absorb has to be 0, 1, 2 or 3, got {absorb}')
+    if max_bond is not None and max_bond < 1:
+        raise ValueError(f'a bond needs at least one multiplet, got {max_bond}')
+    arranged = tensor.place(left) if left is not None else tensor
+    cat = arranged.cat
+    factors = []
+    for i, key in enumerate(arranged.keys()):
+        matrix = arranged._view(i)
+        if matrix.numel() == 0:
+            continue
+        u, s, vh = torch.linalg.svd(matrix, full_matrices = False)
+        factors.append([key, u, s, vh, 0, 0])
+    host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
+    candidates, at = [], 0
+    for fi, f in enumerate(factors):
+        for index in range(f[2].numel()):
+            candidates.append((host[at], fi, index))
+            at += 1
+    candidates.sort(key = lambda c: -c[0])
+    cut = next((i for i, c in enumerate(candidates) if c[0] <= tol), len(candidates))
+    candidates = candidates[:cut]
+    if max_bond is not None and len(candidates) > max_bond:
+        candidates = candidates[:max_bond]
+    for _, fi, index in candidates:
+        factors[fi][4] = max(factors[fi][4], index + 1)
+    multiplicities = {}
+    for f in factors:
+        if f[4]:
+            multiplicities[f[0].domain] = multiplicities.get(f[0].domain, 0) + f[4]
+    paired = {}
+    for sector, count in multiplicities.items():
+        other = multiplicities.get(cat.dual(sector))
+        if other is not None:
+            paired[sector] = min(count, other)
+    if paired and paired != multiplicities:
+        for f in factors:
+            f[4] = 0
+        used = {}
+        for _, fi, index in candidates:
+            f = factors[fi]
+            room = paired.get(f[0].domain)
+            if room is None or used.get(f[0].domain, 0) >= room:
+                continue
+            used[f[0].domain] = used.get(f[0].domain, 0) + 1
+            f[4] = max(f[4], index + 1)
+        multiplicities = paired
+    nxt = {}
+    for f in factors:
+        f[5] = nxt.get(f[0].domain, 0)
+        nxt[f[0].domain] = f[5] + f[4]
+    placed, run_at = {}, 0
+    for sector in sorted(multiplicities):
+        placed[sector] = run_at
+        run_at += multiplicities[sector]
+    if not multiplicities:
+        multiplicities = {cat.trivial(): 1}
+    bond = Leg.from_blocks(cat, sorted(multiplicities.items()))[0]
+    first = Tensor(cat, arranged.codomain, [bond], arranged.qtotal, arranged.dtype, arranged.device)
+    values = torch.zeros(bond.multiplets(), dtype = arranged.dtype, device = arranged.device)
+    second = Tensor(cat, [bond], arranged.domain, cat.trivial(), arranged.dtype, arranged.device)
+    for key, u, s, vh, kept, offset in factors:
+        if kept == 0:
+            continue
+        u, vh, s = u[:, :kept], vh[:kept], s[:kept]
+        if absorb == 3:
+            u = u * s.sqrt()
+            vh = s.sqrt().unsqueeze(1) * vh
+        elif absorb == 1:
+            u = u * s
+        elif absorb == 2:
+            vh = s.unsqueeze(1) * vh
+        first.block(key.codomain, key.domain, key.copy)[:, offset:offset + kept].copy_(u)
+        second.block(key.domain, key.domain)[offset:offset + kept, :].copy_(vh)
+        values[placed[key.domain] + offset:placed[key.domain] + offset + kept].copy_(s.to(arranged.dtype))
+    return first, values, second
+
+
+def svd(tensor: Tensor, *args, **kwargs):
+    '''svd(tensor, max_bond=None, tol=0.0, absorb=0) or svd(tensor, left, max_bond=None, tol=0.0,
+    absorb=0) -> (first, values, second): the two overloads of tentorch/_ext/bindings.cpp:365-382.'''
+    left = None
+    if args and isinstance(args[0], (list, tuple)):
+        left, args = list(args[0]), args[1:]
+    elif 'left' in kwargs:
+        left = kwargs.pop('left')
+    params = {'max_bond': None, 'tol': 0.0, 'absorb': 0}
+    for name, value in zip(('max_bond', 'tol', 'absorb'), args):
+        params[name] = value
+    for name, value in kwargs.items():
+        if name not in params:
+            raise TypeError(f'svd() got an unexpected keyword argument {name!r}')
+        params[name] = value
+    return _split_over(tensor, left, params['max_bond'], params['tol'], params['absorb'])
+
+
+def svdvals(tensor: Tensor, left = None) -> torch.Tensor:
+    return _split_over(tensor, left, None, 0.0, 0)[1]
+
+
+def _split_blocks(tensor: Tensor, pieces):
+    '''tentorch/linalg/graded/svd.cpp:203-229'''
+    cat = tensor.cat
+    multiplicities, nxt, placed = {}, {}, []
+    for key, left, right, kept in pieces:
+        if kept == 0:
+            continue
+        offset = nxt.get(key.domain, 0)
+        nxt[key.domain] = offset + kept
+        multiplicities[key.domain] = multiplicities.get(key.domain, 0) + kept
+        placed.append((key, left, right, kept, offset))
+    if not multiplicities:
+        multiplicities = {cat.trivial(): 1}
+    bond = Leg.from_blocks(cat, sorted(multiplicities.items()))[0]
+    first = Tensor(cat, tensor.codomain, [bond], tensor.qtotal, tensor.dtype, tensor.device)
+    second = Tensor(cat, [bond], tensor.domain, cat.trivial(), tensor.dtype, tensor.device)
+    for key, left, right, kept, offset in placed:
+        first.block(key.codomain, key.domain, key.copy)[:, offset:offset + kept].copy_(left)
+        second.block(key.domain, key.domain)[offset:offset + kept, :].copy_(right)
+    return first, second
+
+
+def qr(tensor: Tensor, left = None):
+    '''tentorch/linalg/graded/svd.cpp:233-244'''
+    arranged = tensor.place(left) if left is not None else tensor
+    pieces = []
+    for i, key in enumerate(arranged.keys()):
+        matrix = arranged._view(i)
+        if matrix.numel() == 0:
+            continue
+        q, r = torch.linalg.qr(matrix, mode = 'reduced')
+        pieces.append((key, q, r, q.shape[1]))
+    return _split_blocks(arranged, pieces)
+
+
+def rq(tensor: Tensor, left = None):
+    '''tentorch/linalg/graded/svd.cpp:246-257'''
+    arranged = tensor.place(left) if left is not None else tensor
+    pieces = []
+    for i, key in enumerate(arranged.keys()):
+        matrix = arranged._view(i)
+        if matrix.numel() == 0:
+            continue
+        q, r = torch.linalg.qr(matrix.transpose(0, 1), mode = 'reduced')
+        pieces.append((key, r.transpose(0, 1), q.transpose(0, 1), q.shape[1]))
+    return _split_blocks(arranged, pieces)

@@ -1,0 +1,171 @@
+'''The product's host engine (no GPU needed): the C ABI loads and exports what include/ declares,
+and the categories, trees, layouts, block keys and per-step regrouping plans match the reference's
+own outputs (tests/golden/, produced from the reference) — the plans bit for bit.'''
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from golden_io import load_json
+
+import tentorch_gb300 as tg
+from tentorch_gb300 import _lib
+from tentorch_gb300.tensor import Space
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CATS = {'u1': tg.u1, 'su2': tg.su2, 'fibonacci': tg.fibonacci, 'no_symmetry': tg.no_symmetry}
+
+
+def declared():
+    text = open(os.path.join(ROOT, 'include', 'tentorch_gb300.h')).read()
+    return sorted(set(re.findall(r'\b(tt_[a-z_A-Z0-9]+)\s*\(', text)))
+
+
+def test_library_exports_every_declared_symbol():
+    names = declared()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(_lib.lib, name), name
+    assert _lib.lib.tt_version() >= 1
+    assert set(names) == set(_lib.EXPORTED)
+
+
+def legs(cat, specs):
+    return [tg.Leg(cat, [tuple(s) for s, _ in spec], [m for _, m in spec]) for spec in specs]
+
+
+@pytest.mark.parametrize('name', ['su2', 'fibonacci'])
+def test_symbols_match_the_reference(name):
+    cat = CATS[name]
+    table = load_json('symbols.json')[name]
+    for a, b, c, d, re_, im_ in table['F']:
+        got = cat.F_symbol(tuple(a), tuple(b), tuple(c), tuple(d)).numpy()
+        want = np.array(re_) + 1j * np.array(im_)
+        assert got.shape == want.shape
+        assert np.abs(got - want).max(initial = 0) < 1e-13, (a, b, c, d)
+    for b, c, re_, im_ in table['R']:
+        got = cat.R_symbol(tuple(b), tuple(c)).numpy()
+        want = np.array(re_) + 1j * np.array(im_)
+        assert got.shape == want.shape and np.abs(got - want).max(initial = 0) < 1e-13
+
+
+def test_trees_layouts_and_keys_match_the_reference():
+    data = load_json('structure.json')
+    for case in data['layouts']:
+        cat = CATS[case['cat']]
+        ls = legs(cat, case['legs'])
+        trees = tg.fusion_trees(cat, ls, tuple(case['root']))
+        want = [(tuple(map(tuple, t[0])), tuple(map(tuple, t[1])), tuple(t[2]), tuple(t[3])) for t in case['trees']]
+        assert [tuple(t) for t in trees] == want
+        offsets = [0]
+        for t in trees:
+            rows = 1
+            for leg, s in zip(ls, t.sectors):
+                rows *= leg.multiplicities[leg.sectors.index(s)]
+            offsets.append(offsets[-1] + rows)
+        assert offsets == case['offsets']
+    for case in data['keys']:
+        cat = CATS[case['cat']]
+        space = Space.of(cat, legs(cat, case['codomain']), legs(cat, case['domain']), tuple(case['qtotal']))
+        want = sorted((tuple(k[0]), tuple(k[1]), k[2]) for k in case['keys'])
+        assert [tuple(k) for k in space.keys] == want
+
+
+def step_plan(space_id, kind, arm, key):
+    ns, npc = ctypes.c_int64(), ctypes.c_int64()
+    args = (space_id, kind, arm, key[0][0], key[1][0], key[2])
+    _lib.check(_lib.lib.tt_step_plan(*args, 0, (ctypes.c_int64 * 1)(), 0, (ctypes.c_double * 1)(),
+                                     ctypes.byref(ns), ctypes.byref(npc)))
+    shifts = (ctypes.c_int64 * max(9 * ns.value, 1))()
+    pieces = (ctypes.c_double * max(8 * npc.value, 1))()
+    _lib.check(_lib.lib.tt_step_plan(*args, ns.value, shifts, npc.value, pieces, ctypes.byref(ns), ctypes.byref(npc)))
+    out, at = [], 0
+    for i in range(ns.value):
+        s = shifts[9 * i:9 * i + 9]
+        count = s[8]
+        ps = [pieces[8 * j:8 * j + 7] for j in range(at, at + count)]
+        at += count
+        out.append(((s[0], s[1], s[2]), (s[3], s[4], s[5]), s[6], s[7], ps))
+    return out
+
+
+def test_step_plans_match_the_reference_bit_for_bit():
+    '''Every piece of every shift of every block of every step: first, last, steps and run exactly,
+    the coefficient to 1e-12.'''
+    kinds = {'x': 0, 'down': 1, 'up': 2}
+    checked = 0
+    for record in load_json('plans.json'):
+        cat = CATS[record['cat']]
+        for step in record['steps']:
+            space = Space.of(cat, legs(cat, step['codomain']), legs(cat, step['domain']), tuple(record['qtotal']))
+            for block in step['blocks']:
+                key = (tuple(block['key'][0]), tuple(block['key'][1]), block['key'][2])
+                got = step_plan(space.id, kinds[step['kind']], step['arm'], key)
+                want = block['shifts']
+                assert len(got) == len(want)
+                for mine, theirs in zip(got, want):
+                    assert list(mine[0]) == theirs[0][0] + theirs[0][1] + [theirs[0][2]]
+                    assert list(mine[1]) == theirs[1][0] + theirs[1][1] + [theirs[1][2]]
+                    assert (mine[2], mine[3]) == (theirs[2], theirs[3])
+                    assert [tuple(int(x) for x in p[:5]) for p in mine[4]] == [tuple(p[:5]) for p in theirs[4]]
+                    coef = np.array([p[5] + 1j * p[6] for p in mine[4]])
+                    ref = np.array([p[5] + 1j * p[6] for p in theirs[4]])
+                    assert np.abs(coef - ref).max(initial = 0) < 1e-12
+                    checked += len(mine[4])
+    assert checked > 1000
+
+
+def test_chain_matches_the_oracle_step_sequence():
+    from oracle import engine as orc
+    for record in load_json('plans.json'):
+        cat = CATS[record['cat']]
+        space = Space.of(cat, legs(cat, record['codomain']), legs(cat, record['domain']), tuple(record['qtotal']))
+        above, n_above = _lib.ints32(record['above'])
+        below, n_below = _lib.ints32(record['below'])
+        steps, n = (ctypes.c_int32 * 192)(), ctypes.c_int32()
+        _lib.check(_lib.lib.tt_chain(space.id, n_above, above, n_below, below, 64, steps, ctypes.byref(n)))
+        kinds = {0: 'x', 1: 'down', 2: 'up'}
+        got = [(kinds[steps[3 * i]], steps[3 * i + 1]) for i in range(n.value)]
+        assert got == [(s['kind'], s['arm']) for s in record['steps']]
+
+
+def test_errors_map_to_the_reference_exceptions():
+    leg = tg.Leg(tg.u1, [(1,), (-1,)], [1, 1])
+    with pytest.raises(ValueError, match = 'twice'):
+        tg.Leg(tg.u1, [(1,), (1,)], [1, 1])
+    with pytest.raises(ValueError, match = 'positive'):
+        tg.Leg(tg.u1, [(1,)], [0])
+    with pytest.raises(ValueError, match = 'no components'):
+        tg.Leg(tg.su2, [(-1,)], [1])
+    t = tg.Tensor(tg.u1, [leg, leg], [leg], (1,), device = 'cpu')
+    with pytest.raises(ValueError, match = 'named twice'):
+        _lib.check(_lib.lib.tt_plan_place(t._space.id, 2, _lib.ints32([0, 0])[0], 1, _lib.ints32([2])[0],
+                                          ctypes.byref(ctypes.c_void_p())))
+    with pytest.raises(IndexError):
+        t.block((5,), (5,))
+    with pytest.raises(ValueError, match = 'does not say what it leaves'):
+        tg.linalg.plan_of('ab', t)
+    with pytest.raises(ValueError, match = 'names more than two legs'):
+        tg.linalg.plan_of('abc,aab->c', t, t)
+    with pytest.raises(ValueError, match = "does not take the keyword 'charge'"):
+        tg.einsum('ABc->ABc', t, charge = (1,))
+    with pytest.raises(RuntimeError, match = 'CUDA device'):
+        tg.einsum('ABc->ABc', t, outcharge = (1,))
+
+
+def test_einsum_plan_compiles_on_the_host():
+    '''The matvec plan compiles without a GPU and reports its work.'''
+    from oracle import engine as orc
+    qs, deg = orc.degeneracies(64)
+    bond = tg.Leg(tg.u1, [(2 * q,) for q in qs], deg)
+    phys = tg.Leg(tg.u1, [(1,), (-1,)], [1, 1])
+    w = tg.Leg(tg.u1, [(0,), (2,), (-2,)], [3, 1, 1])
+    head = tg.Tensor(tg.u1, [bond, phys], [bond, phys, w], (0,), device = 'cpu')
+    tail = tg.Tensor(tg.u1, [w, phys, phys, bond], [bond], (0,), device = 'cpu')
+    theta = tg.Tensor(tg.u1, [bond, phys], [phys, bond], (0,), device = 'cpu')
+    plan = tg.linalg.plan_of('EPaqj,JRSFb,AQsb->EPrf', head, tail, theta)
+    assert plan.flops > 0 and plan.n_ops >= 3
+    assert plan.prepared_size(0) > 0 and plan.prepared_size(1) > 0 and plan.prepared_size(2) == 0
+    assert plan.out_space.codomain == [bond, phys] and plan.out_space.domain == [phys, bond]
