@@ -381,6 +381,62 @@ namespace ttg
       }
     }
 
+    // Every descriptor stays inside the buffers its op reads and writes: checked once on the host
+    // when the program is compiled, so no launch can be handed an offset outside an arena.
+    void validate(const Program &p)
+    {
+      const auto size_of = [&](int32_t buffer) { return p.buffers[static_cast<size_t>(buffer)].size; };
+      const auto require = [](bool ok, const char *what) {
+        if (!ok) throw LogicError(std::string("a compiled program reaches outside its buffers: ") + what);
+      };
+      for (const Op &op : p.ops)
+      {
+        const int64_t dst = op.dst >= 0 ? size_of(op.dst) : 0;
+        switch (op.kind)
+        {
+        case OpKind::zero:
+        case OpKind::copy:
+        case OpKind::add:
+          require(op.elements <= dst && (op.src < 0 || op.elements <= size_of(op.src)), "arena op");
+          break;
+        case OpKind::gather:
+          require(op.elements <= dst, "gather destination");
+          for (int64_t i = op.begin; i < op.begin + op.count; ++i)
+            require(p.gather_index[static_cast<size_t>(i)] < size_of(op.src), "gather source");
+          break;
+        case OpKind::runs:
+          for (int64_t c = op.begin; c < op.begin + op.count; ++c)
+          {
+            const Chunk &ch = p.chunks[static_cast<size_t>(c)];
+            require(ch.len >= 1 && ch.len <= kChunk && ch.dst >= 0 && ch.dst_step >= 0, "runs chunk");
+            require(ch.dst + static_cast<int64_t>(ch.len - 1) * ch.dst_step < dst, "runs destination");
+            for (int32_t t = 0; t < ch.term_count; ++t)
+            {
+              const Term &term = p.terms[static_cast<size_t>(ch.term_begin + t)];
+              require(term.src >= 0 && term.src_step >= 0 &&
+                        term.src + static_cast<int64_t>(ch.len - 1) * term.src_step < size_of(op.src),
+                      "runs source");
+            }
+          }
+          break;
+        case OpKind::gemm:
+          for (int64_t bi = op.begin; bi < op.begin + op.count; ++bi)
+          {
+            const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(bi)];
+            const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
+            require(blk.c >= 0 && blk.c + entries + (entries & 1) <= dst, "gemm output block");
+            for (int32_t k = 0; k < blk.pair_count; ++k)
+            {
+              const GemmPair &pr = p.gemm_pairs[static_cast<size_t>(blk.pair_begin + k)];
+              require(pr.a >= 0 && pr.a + static_cast<int64_t>(blk.m) * pr.k <= size_of(op.src), "gemm left block");
+              require(pr.b >= 0 && pr.b + static_cast<int64_t>(pr.k) * blk.n <= size_of(op.src2), "gemm right block");
+            }
+          }
+          break;
+        }
+      }
+    }
+
     void finish(Program &p, Builder &b, const std::vector<Value> &results)
     {
       if (results.empty()) throw LogicError("a program without a result");
@@ -421,6 +477,7 @@ namespace ttg
       // ops of an unprepared operand's phase run as core ops
       for (Op &op : p.ops)
         if (op.phase >= 0 && p.prepared[static_cast<size_t>(op.phase)] < 0) op.phase = -1;
+      validate(p);
     }
 
     // --------------------------------------------------------------------------------------
