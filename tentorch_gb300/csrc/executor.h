@@ -7,6 +7,7 @@
 #include <mutex>
 #include <vector>
 
+#include "gemm.h"
 #include "program.h"
 
 namespace ttg
@@ -22,11 +23,16 @@ namespace ttg
     Term *terms = nullptr;
     GemmBlock *blocks = nullptr;
     GemmPair *pairs = nullptr;
-    int32_t *tiles = nullptr;  // (block, m0, n0, 0) per 32x32 output tile
-    std::vector<int64_t> tile_begin, tile_count;
-    // split-precision scratch layout (see gemm_split.cu), per GEMM op
-    std::vector<int64_t> split_tile_begin, split_tile_count;
-    int32_t *split_tiles = nullptr;
+    // per op: the balanced work items of a GEMM (FP64 tiles and split-precision tiles) and, for
+    // the split path, the rows and columns to slice
+    struct GemmTables
+    {
+      GemmItem *items = nullptr;
+      GemmReduce *reduces = nullptr;
+      void *lines = nullptr;
+      int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0;
+    };
+    std::vector<GemmTables> gemm, split;
 
     cudaError_t ensure(const Program &p);
     ~DeviceTables();
@@ -48,9 +54,12 @@ namespace ttg
 
   cudaError_t execute(const Program &p, DeviceTables &t, const ExecArgs &args);
 
-  // The split-precision grouped GEMM of one op (gemm_split.cu).
+  // The grouped GEMM of one op (gemm.cu): FP64 / complex128, or split precision with `slices`.
+  cudaError_t launch_gemm_f64(const Program &p, DeviceTables &t, size_t op_index, const void *A, const void *B, void *C,
+                              bool complex, void *scratch, cudaStream_t stream);
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
-                                const double *B, double *C, int32_t slices, cudaStream_t stream);
+                                const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream);
+  cudaError_t upload_gemm(const Program &p, DeviceTables &t);
 
   constexpr int kDotParts = 120;
   // out[2j], out[2j+1] = re, im of <a_j, b> for j < count; partial holds 2*kDotParts*count doubles.

@@ -1,0 +1,61 @@
+// Grouped block-pair GEMM schedules and launchers.
+//
+// A GEMM op of a program computes every output block C_b = sum over its pairs A_p B_p.  Its output
+// tiles are cut into work items of roughly equal multiply-add count, each covering a contiguous
+// range of the tile's K (concatenated over the tile's pairs), so one long block product is spread
+// over many SMs.  An item that covers its whole tile writes C; otherwise it writes a partial tile
+// to scratch and a reduction sums the partials of the tile in a fixed order (deterministic, no
+// atomics).
+//
+// Split precision (gemm.cu): every row of A and column of B is scaled by a power of two so that
+// its entries lie in [-1, 1], then cut into `s` slices of 7 bits held exactly as bf16 integers
+// (|q_1| <= 128, |q_t| <= 64).  The products of slices are sums of integers that fp32 accumulates
+// exactly over a K-chunk of up to 256, so the only rounding is the final FP64 combination and the
+// truncation after s slices (about 2^-7s of the row and column maxima): Ozaki's error-free
+// splitting (K. Ozaki, T. Ogita, S. Oishi, S. M. Rump, Numer. Algorithms 59 (2012)) on bf16
+// tensor cores with fp32 accumulation.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "program.h"
+
+namespace ttg
+{
+  struct GemmItem
+  {
+    int32_t block, m0, n0, k0, k1, slot;  // slot -1: the item covers its tile and writes C
+  };
+  struct GemmReduce
+  {
+    int32_t block, m0, n0, slot0, nslots, pad;
+  };
+  struct GemmSchedule
+  {
+    std::vector<GemmItem> items;
+    std::vector<GemmReduce> reduces;
+    int64_t slots = 0;  // partial tiles of bm x bn doubles
+  };
+
+  // Tile sizes of the two kernels.
+  constexpr int kF64TileM = 32, kF64TileN = 32;
+  constexpr int kSplitTileM = 64, kSplitTileN = 32;
+  constexpr int kMaxSlices = 8;
+  constexpr int kExactChunk = 256;  // K over which fp32 sums of slice products stay exact
+
+  GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn);
+
+  // Scratch doubles a program's GEMM ops need at most (FP64 partials, or slices + exponents +
+  // partials for split precision), laid out per op from offset 0.
+  int64_t gemm_scratch(const Program &p);
+
+  // The distinct left blocks (offset, rows, cols) and right blocks of one GEMM op.
+  struct OperandBlock
+  {
+    int64_t offset;
+    int32_t rows, cols;
+  };
+  void gemm_operands(const Program &p, const Op &op, std::vector<OperandBlock> &left, std::vector<OperandBlock> &right);
+
+} // namespace ttg

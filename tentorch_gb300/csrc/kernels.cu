@@ -5,12 +5,9 @@
 //                      and one gathered read per entry (HBM/L2 bound; index 4 B per entry)
 //   runs_kernel        a leg-move step with F/R coefficients: one destination run per warp slice,
 //                      sum over the run's terms in registers, no atomics
-//   gemm_f64_kernel    grouped block-pair products in FP64 (one CTA per 32x32 output tile, all
-//                      tiles of all output blocks of a contraction in one launch)
-//   gemm_c128_kernel   the same for complex128
 //   add_kernel         dst += src over an arena
 //
-// The split-precision GEMM lives in gemm_split.cu.
+// The grouped GEMMs live in gemm.cu.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -106,175 +103,6 @@ namespace ttg
       }
     }
 
-    // ------------------------------------------------------------------------------------------
-    // grouped GEMM, FP64 / complex128
-    // ------------------------------------------------------------------------------------------
-
-    struct DevBlock
-    {
-      int64_t c;
-      int32_t m, n, pair_begin, pair_count;
-    };
-    struct DevPair
-    {
-      int64_t a, b;
-      int32_t k, pad;
-    };
-    static_assert(sizeof(DevBlock) == sizeof(GemmBlock), "block layout");
-    static_assert(sizeof(DevPair) == sizeof(GemmPair), "pair layout");
-
-    // 32x32 output tile per CTA, 64 threads, 4x4 per thread, K staged 16 at a time through shared
-    // memory.  FP64 on this part issues about two DFMA per SM clock, so the tile is small to spread
-    // the uneven blocks of a contraction over all SMs.
-    constexpr int BM = 32, BN = 32, BK = 16, TM = 4, TN = 4;
-    constexpr int GEMM_THREADS = (BM / TM) * (BN / TN);
-
-    __global__ void __launch_bounds__(GEMM_THREADS) gemm_f64_kernel(const double *__restrict__ A,
-                                                                    const double *__restrict__ B, double *__restrict__ C,
-                                                                    const DevBlock *__restrict__ blocks,
-                                                                    const DevPair *__restrict__ pairs,
-                                                                    const int4 *__restrict__ tiles)
-    {
-      __shared__ double as[BK][BM];
-      __shared__ double bs[BK][BN + 1];
-      const int4 tile = tiles[blockIdx.x];  // (block, m0, n0, 0)
-      const DevBlock blk = blocks[tile.x];
-      const int m0 = tile.y, n0 = tile.z;
-      const int tx = threadIdx.x % (BN / TN), ty = threadIdx.x / (BN / TN);
-      double acc[TM][TN] = {};
-      for (int32_t pi = 0; pi < blk.pair_count; ++pi)
-      {
-        const DevPair pr = pairs[blk.pair_begin + pi];
-        const double *a = A + pr.a;
-        const double *b = B + pr.b;
-        const int K = pr.k;
-        for (int k0 = 0; k0 < K; k0 += BK)
-        {
-          for (int i = threadIdx.x; i < BM * BK; i += GEMM_THREADS)
-          {
-            const int r = i / BK, kk = i % BK;
-            const int gm = m0 + r, gk = k0 + kk;
-            as[kk][r] = (gm < blk.m && gk < K) ? a[static_cast<int64_t>(gm) * K + gk] : 0.0;
-          }
-          for (int i = threadIdx.x; i < BK * BN; i += GEMM_THREADS)
-          {
-            const int kk = i / BN, cc = i % BN;
-            const int gk = k0 + kk, gn = n0 + cc;
-            bs[kk][cc] = (gk < K && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : 0.0;
-          }
-          __syncthreads();
-#pragma unroll
-          for (int kk = 0; kk < BK; ++kk)
-          {
-            double av[TM], bv[TN];
-#pragma unroll
-            for (int i = 0; i < TM; ++i) av[i] = as[kk][ty * TM + i];
-#pragma unroll
-            for (int j = 0; j < TN; ++j) bv[j] = bs[kk][tx * TN + j];
-#pragma unroll
-            for (int i = 0; i < TM; ++i)
-#pragma unroll
-              for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
-          }
-          __syncthreads();
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < TM; ++i)
-      {
-        const int gm = m0 + ty * TM + i;
-        if (gm >= blk.m) continue;
-#pragma unroll
-        for (int j = 0; j < TN; ++j)
-        {
-          const int gn = n0 + tx * TN + j;
-          if (gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[i][j];
-        }
-      }
-      // the block's alignment pad (one entry after an odd-sized block) reads as zero in arena sums
-      const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (threadIdx.x == 0 && m0 + BM >= blk.m && n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = 0.0;
-    }
-
-    constexpr int CBM = 32, CBN = 32, CBK = 8, CTM = 4, CTN = 4;
-    constexpr int CGEMM_THREADS = (CBM / CTM) * (CBN / CTN);
-
-    __global__ void __launch_bounds__(CGEMM_THREADS) gemm_c128_kernel(const double2 *__restrict__ A,
-                                                                      const double2 *__restrict__ B,
-                                                                      double2 *__restrict__ C,
-                                                                      const DevBlock *__restrict__ blocks,
-                                                                      const DevPair *__restrict__ pairs,
-                                                                      const int4 *__restrict__ tiles)
-    {
-      __shared__ double2 as[CBK][CBM];
-      __shared__ double2 bs[CBK][CBN + 1];
-      const int4 tile = tiles[blockIdx.x];
-      const DevBlock blk = blocks[tile.x];
-      const int m0 = tile.y, n0 = tile.z;
-      const int tx = threadIdx.x % (CBN / CTN), ty = threadIdx.x / (CBN / CTN);
-      double2 acc[CTM][CTN];
-#pragma unroll
-      for (int i = 0; i < CTM; ++i)
-#pragma unroll
-        for (int j = 0; j < CTN; ++j) acc[i][j] = make_double2(0.0, 0.0);
-      for (int32_t pi = 0; pi < blk.pair_count; ++pi)
-      {
-        const DevPair pr = pairs[blk.pair_begin + pi];
-        const double2 *a = A + pr.a;
-        const double2 *b = B + pr.b;
-        const int K = pr.k;
-        for (int k0 = 0; k0 < K; k0 += CBK)
-        {
-          for (int i = threadIdx.x; i < CBM * CBK; i += CGEMM_THREADS)
-          {
-            const int r = i / CBK, kk = i % CBK;
-            const int gm = m0 + r, gk = k0 + kk;
-            as[kk][r] = (gm < blk.m && gk < K) ? a[static_cast<int64_t>(gm) * K + gk] : make_double2(0.0, 0.0);
-          }
-          for (int i = threadIdx.x; i < CBK * CBN; i += CGEMM_THREADS)
-          {
-            const int kk = i / CBN, cc = i % CBN;
-            const int gk = k0 + kk, gn = n0 + cc;
-            bs[kk][cc] = (gk < K && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : make_double2(0.0, 0.0);
-          }
-          __syncthreads();
-#pragma unroll
-          for (int kk = 0; kk < CBK; ++kk)
-          {
-            double2 av[CTM], bv[CTN];
-#pragma unroll
-            for (int i = 0; i < CTM; ++i) av[i] = as[kk][ty * CTM + i];
-#pragma unroll
-            for (int j = 0; j < CTN; ++j) bv[j] = bs[kk][tx * CTN + j];
-#pragma unroll
-            for (int i = 0; i < CTM; ++i)
-#pragma unroll
-              for (int j = 0; j < CTN; ++j)
-              {
-                acc[i][j].x = fma(av[i].x, bv[j].x, fma(-av[i].y, bv[j].y, acc[i][j].x));
-                acc[i][j].y = fma(av[i].x, bv[j].y, fma(av[i].y, bv[j].x, acc[i][j].y));
-              }
-          }
-          __syncthreads();
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < CTM; ++i)
-      {
-        const int gm = m0 + ty * CTM + i;
-        if (gm >= blk.m) continue;
-#pragma unroll
-        for (int j = 0; j < CTN; ++j)
-        {
-          const int gn = n0 + tx * CTN + j;
-          if (gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[i][j];
-        }
-      }
-      const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (threadIdx.x == 0 && m0 + CBM >= blk.m && n0 + CBN >= blk.n && (entries & 1))
-        C[blk.c + entries] = make_double2(0.0, 0.0);
-    }
-
     int grid_for(int64_t n, int threads)
     {
       // enough CTAs to cover the arena, capped at 8 waves of the 152 SMs
@@ -292,8 +120,12 @@ namespace ttg
   DeviceTables::~DeviceTables()
   {
     for (void *p : {static_cast<void *>(gather), static_cast<void *>(chunks), static_cast<void *>(terms),
-                    static_cast<void *>(blocks), static_cast<void *>(pairs), static_cast<void *>(tiles)})
+                    static_cast<void *>(blocks), static_cast<void *>(pairs)})
       if (p) cudaFree(p);
+    for (auto *tables : {&gemm, &split})
+      for (GemmTables &g : *tables)
+        for (void *p : {static_cast<void *>(g.items), static_cast<void *>(g.reduces), g.lines})
+          if (p) cudaFree(p);
   }
 
   namespace
@@ -309,34 +141,6 @@ namespace ttg
     }
   } // namespace
 
-  // The output tiles of every GEMM op, in op order; tile_begin of op i is recorded per op.
-  void build_tiles(const Program &p, std::vector<int32_t> &host_tiles, std::vector<int64_t> &tile_begin,
-                   std::vector<int64_t> &tile_count)
-  {
-    host_tiles.clear();
-    tile_begin.assign(p.ops.size(), 0);
-    tile_count.assign(p.ops.size(), 0);
-    for (size_t i = 0; i < p.ops.size(); ++i)
-    {
-      const Op &op = p.ops[i];
-      if (op.kind != OpKind::gemm) continue;
-      tile_begin[i] = static_cast<int64_t>(host_tiles.size() / 4);
-      for (int64_t b = op.begin; b < op.begin + op.count; ++b)
-      {
-        const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(b)];
-        for (int32_t m0 = 0; m0 < blk.m; m0 += BM)
-          for (int32_t n0 = 0; n0 < blk.n; n0 += BN)
-          {
-            host_tiles.push_back(static_cast<int32_t>(b));
-            host_tiles.push_back(m0);
-            host_tiles.push_back(n0);
-            host_tiles.push_back(0);
-          }
-      }
-      tile_count[i] = static_cast<int64_t>(host_tiles.size() / 4) - tile_begin[i];
-    }
-  }
-
   cudaError_t DeviceTables::ensure(const Program &p)
   {
     std::lock_guard<std::mutex> lock(mutex);
@@ -347,9 +151,7 @@ namespace ttg
     if ((e = upload(p.terms, &terms)) != cudaSuccess) return e;
     if ((e = upload(p.gemm_blocks, &blocks)) != cudaSuccess) return e;
     if ((e = upload(p.gemm_pairs, &pairs)) != cudaSuccess) return e;
-    std::vector<int32_t> host_tiles;
-    build_tiles(p, host_tiles, tile_begin, tile_count);
-    if ((e = upload(host_tiles, &tiles)) != cudaSuccess) return e;
+    if ((e = upload_gemm(p, *this)) != cudaSuccess) return e;
     ready = true;
     return cudaSuccess;
   }
@@ -437,23 +239,12 @@ namespace ttg
         break;
       case OpKind::gemm:
       {
-        const int64_t ntiles = t.tile_count[i];
-        if (ntiles == 0) break;
-        const auto *blk = reinterpret_cast<const DevBlock *>(t.blocks);
-        const auto *prs = reinterpret_cast<const DevPair *>(t.pairs);
-        const int4 *tl = reinterpret_cast<const int4 *>(t.tiles) + t.tile_begin[i];
-        if (args.complex)
-          gemm_c128_kernel<<<static_cast<unsigned>(ntiles), CGEMM_THREADS, 0, args.stream>>>(
-            reinterpret_cast<const double2 *>(src), reinterpret_cast<const double2 *>(src2),
-            reinterpret_cast<double2 *>(dst), blk, prs, tl);
-        else if (args.precision > 0)
+        void *scratch = static_cast<char *>(args.workspace) + p.scratch_offset * esize;
+        if (args.precision > 0 && !args.complex)
           e = launch_gemm_split(p, op, t, i, reinterpret_cast<const double *>(src), reinterpret_cast<const double *>(src2),
-                                reinterpret_cast<double *>(dst), args.precision, args.stream);
+                                reinterpret_cast<double *>(dst), args.precision, scratch, args.stream);
         else
-          gemm_f64_kernel<<<static_cast<unsigned>(ntiles), GEMM_THREADS, 0, args.stream>>>(
-            reinterpret_cast<const double *>(src), reinterpret_cast<const double *>(src2), reinterpret_cast<double *>(dst),
-            blk, prs, tl);
-        if (e == cudaSuccess) e = check_launch();
+          e = launch_gemm_f64(p, t, i, src, src2, dst, args.complex, scratch, args.stream);
         break;
       }
       }

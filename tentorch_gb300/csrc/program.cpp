@@ -1,6 +1,8 @@
 // The plan compiler: place / contract / einsum -> device program (see program.h).
 #include "program.h"
 
+#include "gemm.h"
+
 #include <algorithm>
 #include <cmath>
 #include <limits>
@@ -437,6 +439,13 @@ namespace ttg
       }
     }
 
+    bool read_by_any(const Program &p, int32_t buffer)
+    {
+      for (const Op &op : p.ops)
+        if (op.src == buffer || op.src2 == buffer) return true;
+      return false;
+    }
+
     void finish(Program &p, Builder &b, const std::vector<Value> &results)
     {
       if (results.empty()) throw LogicError("a program without a result");
@@ -447,8 +456,13 @@ namespace ttg
       if (first.pending)
         b.materialize(first, out);
       else if (p.buffers[static_cast<size_t>(first.buffer)].kind == BufferKind::temp && first.phase < 0 &&
-               !p.ops.empty() && p.ops.back().dst == first.buffer)
-        p.ops.back().dst = out, p.buffers[static_cast<size_t>(first.buffer)].size = 0;
+               !p.ops.empty() && p.ops.back().dst == first.buffer && !read_by_any(p, first.buffer))
+      {
+        // every op that writes the final temporary (a zero and its runs pass, or one gather or
+        // GEMM) writes the output instead
+        for (Op &op : p.ops)
+          if (op.dst == first.buffer) op.dst = out;
+      }
       else
         b.materialize(first, out);
       for (size_t i = 1; i < results.size(); ++i) b.add_into(results[i], out);
@@ -477,6 +491,8 @@ namespace ttg
       // ops of an unprepared operand's phase run as core ops
       for (Op &op : p.ops)
         if (op.phase >= 0 && p.prepared[static_cast<size_t>(op.phase)] < 0) op.phase = -1;
+      p.scratch_offset = p.workspace;
+      p.workspace += gemm_scratch(p);
       validate(p);
     }
 

@@ -99,6 +99,7 @@ namespace ttg
     std::vector<Buffer> buffers;
     std::vector<Op> ops;
     int64_t workspace = 0;  // elements
+    int64_t scratch_offset = 0;  // elements: GEMM scratch (partial tiles, slices) at the end of the workspace
     // per operand: the buffer holding its prepared value (the input itself when no op prepares it)
     std::vector<int32_t> prepared;
     // descriptor tables

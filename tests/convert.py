@@ -17,8 +17,7 @@ def product_leg(cat, leg):
 
 def to_product(t, cat, device = 'cuda'):
     '''An oracle tensor as a product tensor on `device`.'''
-    dtype = torch.complex128 if np.iscomplexobj(next(iter(t.blocks.values()), np.zeros(0))) or \
-        t.dtype == np.complex128 else torch.float64
+    dtype = torch.complex128 if t.dtype == np.complex128 else torch.float64
     out = tg.Tensor(cat, [product_leg(cat, l) for l in t.codomain], [product_leg(cat, l) for l in t.domain],
                     t.qtotal, dtype = dtype, device = device)
     for key, block in t.blocks.items():

@@ -111,3 +111,43 @@ def test_inner_and_norm_on_the_device():
     assert abs(tg.norm(v) - orc.norm(theta)) < 1e-12 * orc.norm(theta)
     w = v * 0.5
     assert abs(tg.inner(v, w) - 0.5 * orc.norm(theta) ** 2) < 1e-10 * orc.norm(theta) ** 2
+
+
+@pytest.mark.parametrize('slices', [2, 3, 4, 6, 8])
+def test_split_precision_matvec_accuracy(slices):
+    '''Split bf16 products: the error of the chi = 256 matvec against the FP64 oracle stays within
+    the truncation bound of `slices` 7-bit slices (100 * 2^-7s relative to the largest entry, plus
+    FP64 rounding).'''
+    head, tail, theta = orc.matvec_inputs(256, seed = 21)
+    want = orc.einsum(orc.MATVEC, head, tail, theta)
+    h, t, v = (to_product(x, tg.u1) for x in (head, tail, theta))
+    with tg.precision(slices):
+        got = tg.einsum(orc.MATVEC, h, t, v)
+    err = max_relative(got, want.blocks)
+    assert err < 100 * 2.0 ** (-7 * slices) + 1e-14, err
+    if slices == 8:
+        assert err < 1e-14
+
+
+def test_split_precision_is_deterministic():
+    head, tail, theta = orc.matvec_inputs(128, seed = 23)
+    h, t, v = (to_product(x, tg.u1) for x in (head, tail, theta))
+    with tg.precision(4):
+        a = tg.einsum(orc.MATVEC, h, t, v).data.clone()
+        b = tg.einsum(orc.MATVEC, h, t, v).data.clone()
+    assert torch.equal(a, b)
+
+
+def test_large_blocks_split_over_k():
+    '''Blocks whose K is long enough to be cut into several work items (partial tiles reduced in a
+    fixed order): an SU(2) contraction with multiplicity 8, in FP64 and split precision.'''
+    ocat = orc.su2
+    leg = orc.Leg(ocat, [(j,) for j in range(5)], [8] * 5)
+    gen = torch.Generator().manual_seed(29)
+    a = orc.Tensor(ocat, [leg, leg], [leg, leg], (0,)).fill_random(gen)
+    b = orc.Tensor(ocat, [leg, leg], [leg, leg], (0,)).fill_random(gen)
+    want = orc.einsum('ABcd,DCef->ABef', a, b)
+    pa, pb = to_product(a, tg.su2), to_product(b, tg.su2)
+    assert max_relative(tg.einsum('ABcd,DCef->ABef', pa, pb), want.blocks) < TOL
+    with tg.precision(8):
+        assert max_relative(tg.einsum('ABcd,DCef->ABef', pa, pb), want.blocks) < 1e-14

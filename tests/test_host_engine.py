@@ -169,3 +169,28 @@ def test_einsum_plan_compiles_on_the_host():
     assert plan.flops > 0 and plan.n_ops >= 3
     assert plan.prepared_size(0) > 0 and plan.prepared_size(1) > 0 and plan.prepared_size(2) == 0
     assert plan.out_space.codomain == [bond, phys] and plan.out_space.domain == [phys, bond]
+
+
+def test_every_golden_case_compiles_on_the_host():
+    '''place / contract / einsum plans of every golden case compile and pass the descriptor bounds
+    validation the engine runs on every program.'''
+    from convert import PRODUCT_CATS, case_category
+    import torch
+    for case in load_json('cases.json'):
+        cat = PRODUCT_CATS[case_category(case['inputs'][0]['name'])]
+        ts = [tg.Tensor(cat, legs(cat, e['codomain']), legs(cat, e['domain']), tuple(e['qtotal']),
+                        dtype = torch.float64, device = 'cpu') for e in case['inputs']]
+        if case['op'] == 'place':
+            a, na = _lib.ints32(case['above'])
+            b, nb = _lib.ints32(case['below'])
+            _lib.check(_lib.lib.tt_plan_place(ts[0]._space.id, na, a, nb, b, ctypes.byref(ctypes.c_void_p())))
+        elif case['op'] == 'contract':
+            l, n = _lib.ints32(case['left_legs'])
+            r, _ = _lib.ints32(case['right_legs'])
+            _lib.check(_lib.lib.tt_plan_contract(ts[0]._space.id, ts[1]._space.id, n, l, r, 1, case['charge'][0],
+                                                 ctypes.byref(ctypes.c_void_p())))
+        else:
+            oc = case.get('outcharge')
+            plan = tg.linalg.plan_of(case['spec'], *ts, outcharge = tuple(oc) if oc else None)
+            assert plan.out_space.keys == [tg.BlockKey(*k) for k in
+                                           sorted((tuple(k[0]), tuple(k[1]), k[2]) for k in case['output']['keys'])]
