@@ -151,3 +151,22 @@ def test_large_blocks_split_over_k():
     assert max_relative(tg.einsum('ABcd,DCef->ABef', pa, pb), want.blocks) < TOL
     with tg.precision(8):
         assert max_relative(tg.einsum('ABcd,DCef->ABef', pa, pb), want.blocks) < 1e-14
+
+
+@pytest.mark.parametrize('dtype', [torch.float64, torch.complex128])
+def test_device_dot_products(dtype):
+    '''tt_dots: <a_j, b> for several arenas in one pass, no host synchronisation, against torch.'''
+    import ctypes
+    from tentorch_gb300 import _lib
+    n, count = 100_003, 5
+    gen = torch.Generator(device = 'cuda').manual_seed(31)
+    make = lambda: torch.randn(n, dtype = dtype, device = 'cuda', generator = gen)
+    arenas, b = [make() for _ in range(count)], make()
+    table = torch.tensor([a.data_ptr() for a in arenas], dtype = torch.int64, device = 'cuda')
+    scratch = torch.empty(2 * 120 * count, dtype = torch.float64, device = 'cuda')
+    out = torch.empty(2 * count, dtype = torch.float64, device = 'cuda')
+    _lib.check(_lib.lib.tt_dots(0 if dtype == torch.float64 else 1, count, table.data_ptr(), b.data_ptr(), n,
+                                scratch.data_ptr(), out.data_ptr(), torch.cuda.current_stream().cuda_stream))
+    got = torch.complex(out[0::2], out[1::2]).cpu()
+    want = torch.stack([torch.vdot(a, b) for a in arenas]).to(torch.complex128).cpu()
+    assert torch.allclose(got, want, rtol = 1e-12, atol = 1e-10)
