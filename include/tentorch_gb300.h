@@ -137,6 +137,16 @@ int32_t tt_chain(int32_t space, int32_t nabove, const int32_t *above, int32_t nb
 int32_t tt_dots(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *scratch,
                 double *out, void *stream);
 
+/* tt_dots without caller scratch, for callers that cannot allocate device memory where they need
+ * the dot products (a host framework that forbids allocation inside its solver loop, or one whose
+ * memory pool belongs to another runtime).  It has no counterpart in the reference.  The partial
+ * sums live in a static device array of this library (120 KiB on every GPU that loads it, held
+ * until the process exits), so `count` is at most 64 (TT_EINVAL beyond).  The first call on a
+ * device looks up that array's device address (make it before any stream capture); calls whose
+ * work overlaps on the GPU share the array and race.  Otherwise the same contract as tt_dots. */
+int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *out,
+                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif

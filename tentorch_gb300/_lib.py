@@ -56,6 +56,7 @@ _declare('tt_plan_prepare', vp, i32, i32, vp, vp, vp, vp)
 _declare('tt_step_plan', i32, i32, i32, i64, i64, i32, i64, P(i64), i64, P(f64), P(i64), P(i64))
 _declare('tt_chain', i32, i32, P(i32), i32, P(i32), i32, P(i32), P(i32))
 _declare('tt_dots', i32, i32, vp, vp, i64, vp, vp, vp)
+_declare('tt_dots_noalloc', i32, i32, vp, vp, i64, vp, vp)
 
 _ERRORS = {1: ValueError, 2: IndexError, 3: RuntimeError, 4: RuntimeError}
 
@@ -86,4 +87,4 @@ EXPORTED = ['tt_last_error', 'tt_version', 'tt_category', 'tt_outcomes', 'tt_dua
             'tt_R_symbol', 'tt_leg', 'tt_leg_blocks', 'tt_reachable_charges', 'tt_fusion_trees', 'tt_space',
             'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_contract', 'tt_plan_einsum',
             'tt_plan_info', 'tt_plan_prepared_size', 'tt_plan_execute', 'tt_plan_execute_timed', 'tt_plan_prepare', 'tt_step_plan', 'tt_chain',
-            'tt_dots']
+            'tt_dots', 'tt_dots_noalloc']

@@ -124,6 +124,11 @@ namespace
   }
 } // namespace
 
+namespace ttg
+{
+  int32_t report(int32_t code, const std::string &message) { return fail(code, message); }
+} // namespace ttg
+
 extern "C"
 {
   const char *tt_last_error(void) { return last_error.c_str(); }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "gemm.h"
@@ -60,6 +61,9 @@ namespace ttg
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream);
   cudaError_t upload_gemm(const Program &p, DeviceTables &t);
+
+  // Record a failure for tt_last_error() and return its status code (capi.cpp).
+  int32_t report(int32_t code, const std::string &message);
 
   constexpr int kDotParts = 120;
   // out[2j], out[2j+1] = re, im of <a_j, b> for j < count; partial holds 2*kDotParts*count doubles.

@@ -356,3 +356,67 @@ namespace ttg
   }
 
 } // namespace ttg
+
+// ---------------------------------------------------------------------------------------------
+// tt_dots_noalloc: the dot products of tt_dots with their partial sums in a static device array
+// ---------------------------------------------------------------------------------------------
+//
+// For callers that cannot allocate device memory at the point they need a Krylov dot product:
+// a solver step running under a host framework that forbids allocation in its inner loop (a
+// real-time or embedded host, or one whose memory pool is owned by another runtime and exposes
+// no allocator through the FFI), or code that must not touch the allocator between a warm-up and
+// a timed or replayed sequence.  tt_dots needs `scratch` from the caller; this variant keeps the
+// partial sums in the array below, which every GPU that loads this library holds until the
+// process exits.
+
+namespace
+{
+  // At most this many vectors per call: 2 doubles per (vector, CTA) and kDotParts CTAs per vector
+  // (64 * 120 * 16 bytes = 120 KiB per device).
+  constexpr int32_t kNoAllocMaxVectors = 64;
+  constexpr int kNoAllocMaxDevices = 64;
+}
+
+static __device__ __align__(256) double tt_dots_noalloc_scratch[2 * ttg::kDotParts * kNoAllocMaxVectors];
+
+namespace
+{
+  std::mutex noalloc_mutex;
+  double *noalloc_scratch[kNoAllocMaxDevices] = {};
+}
+
+extern "C" int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n,
+                                   double *out, void *stream)
+{
+  if (count <= 0) return 0;
+  if (count > kNoAllocMaxVectors)
+    return ttg::report(1, "tt_dots_noalloc takes at most " + std::to_string(kNoAllocMaxVectors) + " vectors, got " +
+                            std::to_string(count) + "; call tt_dots with caller-provided scratch instead");
+  if (dtype != 0 && dtype != 1) return ttg::report(1, "unknown dtype");
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return ttg::report(4, std::string("CUDA: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= kNoAllocMaxDevices) return ttg::report(1, "device index beyond the static table");
+  double *scratch = nullptr;
+  {
+    // set-up, once per device, with that device current: the device address of the array (host
+    // code only knows a host-side stand-in for it)
+    std::lock_guard<std::mutex> lock(noalloc_mutex);
+    if (!noalloc_scratch[device])
+    {
+      void *address = nullptr;
+      e = cudaGetSymbolAddress(&address, tt_dots_noalloc_scratch);
+      if (e != cudaSuccess) return ttg::report(4, std::string("CUDA: ") + cudaGetErrorString(e));
+      noalloc_scratch[device] = static_cast<double *>(address);
+    }
+    scratch = noalloc_scratch[device];
+  }
+  // Every partial sum a call reads is written earlier in the same call, so nothing has to start at
+  // zero; two calls whose work overlaps on the GPU share the array and race.
+  const bool complex = dtype == 1;
+  e = ttg::arena_dots(reinterpret_cast<const double *const *>(as), count, static_cast<const double *>(b),
+                      n * (complex ? 2 : 1), complex, scratch, out, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return ttg::report(4, std::string("CUDA: ") + cudaGetErrorString(e));
+  return 0;
+}
+
