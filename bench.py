@@ -276,7 +276,7 @@ def run_gpu(args, rank, world):
         op_ms += np.maximum(np.array(ms_arr[:n_ops]), 0.0)
         kinds = list(kind_arr[:n_ops])
     op_ms /= samples
-    names = {0: 'zero', 1: 'gather_kernel', 2: 'runs_kernel', 3: 'gemm_f64_kernel' if args.precision == 0 else 'gemm_split_kernel',
+    names = {0: 'zero', 1: 'gather_kernel', 2: 'runs_kernel', 3: 'gemm_dmma_kernel' if args.precision == 0 else 'gemm_split_kernel',
              4: 'add_f64_kernel', 5: 'copy'}
     by_kind = {}
     launches_per_step = 0
@@ -293,7 +293,7 @@ def run_gpu(args, rank, world):
         peak = fp64_peak_tflops(torch, device)
         achieved = plan.flops / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else 0.0
         roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
-                    'traffic': ncu_traffic('gemm_f64_kernel'), 'kernel': 'gemm_f64_kernel',
+                    'traffic': ncu_traffic('gemm_dmma_kernel'), 'kernel': 'gemm_dmma_kernel',
                     'peak_source': 'cuBLAS DGEMM 4096^3 best of 3 measured in this run (MEASURED_PEAKS.json has no FP64)',
                     'algorithmic': f'{plan.flops:.4g} FLOP per launch (sum of 2mkn over the block pairs of both stages)',
                     'kernel_ms': gemm_ms}

@@ -100,6 +100,9 @@ int32_t tt_plan_einsum(const char *spec, int32_t n, const int32_t *spaces, int32
 /* The output space, workspace elements, GEMM flops, recoupled elements and op count of a plan. */
 int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace, double *gemm_flops,
                      int64_t *moved_elements, int32_t *n_ops);
+/* A text listing of the plan's operations and GEMM block shapes (m, n, K per pair), for diagnosis;
+ * writes at most cap-1 characters and a terminating zero, *length the full size. */
+int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length);
 /* Elements of operand `i`'s prepared arena, 0 when the operand needs no preparation. */
 int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements);
 /* Execute on `stream` (a cudaStream_t, 0 for the legacy stream).  precision 0: FP64 block

@@ -342,6 +342,38 @@ extern "C"
     });
   }
 
+  int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length)
+  {
+    return guarded([&] {
+      const ttg::Program &p = *plan->program;
+      static const char *kinds[] = {"zero", "gather", "runs", "gemm", "add", "copy"};
+      std::string out;
+      for (size_t i = 0; i < p.ops.size(); ++i)
+      {
+        const ttg::Op &op = p.ops[i];
+        out += "op " + std::to_string(i) + " " + kinds[static_cast<int>(op.kind)] + " src " + std::to_string(op.src) +
+               " src2 " + std::to_string(op.src2) + " dst " + std::to_string(op.dst) + " phase " + std::to_string(op.phase) +
+               " elements " + std::to_string(op.elements) + " count " + std::to_string(op.count) + "\n";
+        if (op.kind == ttg::OpKind::gemm)
+          for (int64_t b = op.begin; b < op.begin + op.count; ++b)
+          {
+            const ttg::GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(b)];
+            out += "  block m " + std::to_string(blk.m) + " n " + std::to_string(blk.n) + " k";
+            for (int32_t k = 0; k < blk.pair_count; ++k)
+              out += " " + std::to_string(p.gemm_pairs[static_cast<size_t>(blk.pair_begin + k)].k);
+            out += "\n";
+          }
+      }
+      *length = static_cast<int64_t>(out.size());
+      if (cap > 0)
+      {
+        const int64_t n = std::min<int64_t>(cap - 1, static_cast<int64_t>(out.size()));
+        std::memcpy(text, out.data(), static_cast<size_t>(n));
+        text[n] = 0;
+      }
+    });
+  }
+
   int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements)
   {
     return guarded([&] {

@@ -30,10 +30,16 @@ namespace ttg
     {
       GemmItem *items = nullptr;
       GemmReduce *reduces = nullptr;
-      void *lines = nullptr;
-      int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0;
+      int64_t n_items = 0, n_reduces = 0, slots = 0;
     };
-    std::vector<GemmTables> gemm, split;
+    struct SplitTables
+    {
+      void *items = nullptr, *pairs = nullptr, *lines = nullptr;
+      GemmReduce *reduces = nullptr;
+      int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0, slice_a = 0, slice_b = 0, exps = 0, slots = 0;
+    };
+    std::vector<GemmTables> gemm;
+    std::vector<SplitTables> split;
 
     cudaError_t ensure(const Program &p);
     ~DeviceTables();

@@ -1,13 +1,19 @@
-// Grouped block-pair GEMM for sm_103a: the balanced work schedule, the FP64 / complex128 item
-// kernel, the deterministic partial-tile reduction, and the split-precision path (row / column
-// slicing into exact bf16 integers, mma.sync bf16 products with exact fp32 accumulation per
-// K-chunk, FP64 combination).  See gemm.h for the numerical scheme.
+// Grouped block-pair GEMM for sm_103a: balanced work schedules, the persistent FP64 / complex128
+// kernel, the persistent split-precision kernel (exact bf16 slices on mma.sync with exact fp32 level
+// sums, folded into FP64), and the slicing pass.  See gemm.h for the numerical scheme.
+//
+// Both GEMM kernels are persistent: one CTA per SM, held there by its shared-memory request, split
+// into independent workers of 128 threads that claim work items from a list sorted largest first
+// through an atomic counter.  A tile whose K was cut into several items is reduced by the worker that finishes
+// its last item (an atomic ticket per tile): the partials are summed in slot order, so the result
+// is deterministic, and no thread ever waits on another CTA.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
-#include <set>
+#include <map>
+#include <mutex>
 
 #include "executor.h"
 #include "gemm.h"
@@ -18,18 +24,28 @@ namespace ttg
   // schedules (host)
   // ------------------------------------------------------------------------------------------
 
+  namespace
+  {
+    double op_work(const Program &p, const Op &op)
+    {
+      double total = 0;
+      for (int64_t b = op.begin; b < op.begin + op.count; ++b)
+      {
+        const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(b)];
+        for (int32_t k = 0; k < blk.pair_count; ++k)
+          total += static_cast<double>(blk.m) * blk.n * p.gemm_pairs[static_cast<size_t>(blk.pair_begin + k)].k;
+      }
+      return total;
+    }
+
+    int64_t up256(int64_t bytes) { return (bytes + 255) / 256 * 256; }
+  } // namespace
+
   GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn)
   {
     GemmSchedule s;
-    double total = 0;
-    for (int64_t b = op.begin; b < op.begin + op.count; ++b)
-    {
-      const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(b)];
-      for (int32_t k = 0; k < blk.pair_count; ++k)
-        total += static_cast<double>(blk.m) * blk.n * p.gemm_pairs[static_cast<size_t>(blk.pair_begin + k)].k;
-    }
-    // about four items per SM of the 152, never smaller than a tile over 64 of K
-    const double target = std::max(total / (152.0 * 4.0), static_cast<double>(bm) * bn * 64.0);
+    // about two items per worker, never smaller than a tile over 64 of K
+    const double target = std::max(op_work(p, op) / (152.0 * kF64Workers * 2.0), static_cast<double>(bm) * bn * 64.0);
     struct Sized
     {
       GemmItem item;
@@ -53,20 +69,21 @@ namespace ttg
           const int32_t bi = static_cast<int32_t>(b);
           if (chunks == 1)
           {
-            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1}, work});
+            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work});
             continue;
           }
-          const int32_t slot0 = static_cast<int32_t>(s.slots);
+          const int32_t slot0 = static_cast<int32_t>(s.slots), reduce = static_cast<int32_t>(s.reduces.size());
           for (int64_t c = 0; c < chunks; ++c)
           {
             const int64_t k0 = c * kc, k1 = std::min(ktotal, (c + 1) * kc);
-            items.push_back({{bi, m0, n0, static_cast<int32_t>(k0), static_cast<int32_t>(k1), static_cast<int32_t>(s.slots++)},
+            items.push_back({{bi, m0, n0, static_cast<int32_t>(k0), static_cast<int32_t>(k1), static_cast<int32_t>(s.slots++),
+                              reduce, 0},
                              rows * cols * static_cast<double>(k1 - k0)});
           }
           s.reduces.push_back({bi, m0, n0, slot0, static_cast<int32_t>(chunks), 0});
         }
     }
-    // the largest items launch first, so the tail of the grid is made of small ones
+    // the largest items first, so the round robin ends on small ones
     std::stable_sort(items.begin(), items.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
     for (const Sized &it : items) s.items.push_back(it.item);
     return s;
@@ -74,7 +91,7 @@ namespace ttg
 
   void gemm_operands(const Program &p, const Op &op, std::vector<OperandBlock> &left, std::vector<OperandBlock> &right)
   {
-    std::set<int64_t> seen_a, seen_b;
+    std::map<int64_t, int> seen_a, seen_b;
     left.clear();
     right.clear();
     for (int64_t b = op.begin; b < op.begin + op.count; ++b)
@@ -83,21 +100,125 @@ namespace ttg
       for (int32_t k = 0; k < blk.pair_count; ++k)
       {
         const GemmPair &pr = p.gemm_pairs[static_cast<size_t>(blk.pair_begin + k)];
-        if (seen_a.insert(pr.a).second) left.push_back({pr.a, blk.m, pr.k});
-        if (seen_b.insert(pr.b).second) right.push_back({pr.b, pr.k, blk.n});
+        if (seen_a.emplace(pr.a, 0).second) left.push_back({pr.a, blk.m, pr.k});
+        if (seen_b.emplace(pr.b, 0).second) right.push_back({pr.b, pr.k, blk.n});
       }
     }
   }
 
+  SplitSchedule schedule_split(const Program &p, const Op &op)
+  {
+    SplitSchedule s;
+    s.pairs.assign(p.gemm_pairs.size(), SplitPair{0, 0, 0, 0, 0, 0});
+    // slices: every distinct left block as rows of K padded to 32, every distinct right block
+    // transposed the same way; exponents: one per row of A, one per column of B
+    std::map<int64_t, std::pair<int64_t, int32_t>> a_at, b_at;  // arena offset -> (slice offset, exponent base)
+    const auto pad32 = [](int64_t k) { return (k + kSplitStepK - 1) / kSplitStepK * kSplitStepK; };
+    std::vector<SplitLine> b_lines;
+    for (int64_t bi = op.begin; bi < op.begin + op.count; ++bi)
+    {
+      const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(bi)];
+      for (int32_t k = 0; k < blk.pair_count; ++k)
+      {
+        const size_t pi = static_cast<size_t>(blk.pair_begin + k);
+        const GemmPair &pr = p.gemm_pairs[pi];
+        const int64_t kp = pad32(pr.k);
+        auto fa = a_at.find(pr.a);
+        if (fa == a_at.end())
+        {
+          fa = a_at.emplace(pr.a, std::make_pair(s.slice_a, static_cast<int32_t>(s.exps))).first;
+          for (int32_t r = 0; r < blk.m; ++r)
+            s.lines.push_back({pr.a + static_cast<int64_t>(r) * pr.k, s.slice_a + r * kp, pr.k, 1, static_cast<int32_t>(kp),
+                               static_cast<int32_t>(s.exps + r)});
+          s.slice_a += (blk.m * kp + 63) / 64 * 64;
+          s.exps += blk.m;
+        }
+        auto fb = b_at.find(pr.b);
+        if (fb == b_at.end())
+        {
+          fb = b_at.emplace(pr.b, std::make_pair(s.slice_b, static_cast<int32_t>(s.exps))).first;
+          for (int32_t c = 0; c < blk.n; ++c)
+            b_lines.push_back({pr.b + c, s.slice_b + c * kp, pr.k, blk.n, static_cast<int32_t>(kp),
+                               static_cast<int32_t>(s.exps + c)});
+          s.slice_b += (blk.n * kp + 63) / 64 * 64;
+          s.exps += blk.n;
+        }
+        s.pairs[pi] = SplitPair{fa->second.first, fb->second.first, static_cast<int32_t>(kp), fa->second.second,
+                                fb->second.second, 0};
+      }
+    }
+    s.lines_a = static_cast<int64_t>(s.lines.size());
+    s.lines.insert(s.lines.end(), b_lines.begin(), b_lines.end());
+    // items: one pair's K range each (a multiple of 32), about two per worker, never below a tile
+    // over 128 of K
+    const double target =
+      std::max(op_work(p, op) / (152.0 * kSplitWorkers * 2.0), static_cast<double>(kSplitTileM) * kSplitTileN * 128.0);
+    struct Sized
+    {
+      SplitItem item;
+      double work;
+    };
+    std::vector<Sized> items;
+    for (int64_t bi = op.begin; bi < op.begin + op.count; ++bi)
+    {
+      const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(bi)];
+      for (int32_t m0 = 0; m0 < blk.m; m0 += kSplitTileM)
+        for (int32_t n0 = 0; n0 < blk.n; n0 += kSplitTileN)
+        {
+          const double rows = std::min(kSplitTileM, blk.m - m0), cols = std::min(kSplitTileN, blk.n - n0);
+          std::vector<Sized> tile;
+          for (int32_t k = 0; k < blk.pair_count; ++k)
+          {
+            const int32_t pi = blk.pair_begin + k;
+            const int64_t K = p.gemm_pairs[static_cast<size_t>(pi)].k;
+            const double work = rows * cols * static_cast<double>(K);
+            int64_t chunks = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(work / target)));
+            const int64_t kc = pad32((K + chunks - 1) / chunks);
+            chunks = (K + kc - 1) / kc;
+            for (int64_t c = 0; c < chunks; ++c)
+            {
+              const int64_t k0 = c * kc, k1 = std::min<int64_t>(K, (c + 1) * kc);
+              tile.push_back({{static_cast<int32_t>(bi), m0, n0, pi, static_cast<int32_t>(k0), static_cast<int32_t>(k1), 0, -1},
+                              rows * cols * static_cast<double>(k1 - k0)});
+            }
+          }
+          if (tile.size() == 1)
+          {
+            tile[0].item.slot = -1;
+            items.push_back(tile[0]);
+          }
+          else if (tile.empty())
+            items.push_back({{static_cast<int32_t>(bi), m0, n0, -1, 0, 0, -1, -1}, 0.0});  // no pair: zeros
+          else
+          {
+            const int32_t slot0 = static_cast<int32_t>(s.slots), reduce = static_cast<int32_t>(s.reduces.size());
+            for (Sized &t : tile)
+            {
+              t.item.slot = static_cast<int32_t>(s.slots++);
+              t.item.reduce = reduce;
+              items.push_back(t);
+            }
+            s.reduces.push_back({static_cast<int32_t>(bi), m0, n0, slot0, static_cast<int32_t>(tile.size()), 0});
+          }
+        }
+    }
+    std::stable_sort(items.begin(), items.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
+    for (const Sized &it : items) s.items.push_back(it.item);
+    return s;
+  }
+
   namespace
   {
-    int64_t split_scratch(int64_t size_a, int64_t size_b, int64_t slots)
+    // bytes of split scratch: slices of A and of B (bf16), exponents (int16), partial tiles, tickets
+    int64_t split_bytes(const SplitSchedule &s, int slices)
     {
-      // bf16 slices and int16 exponents of both operands, then the FP64 partial tiles, all in
-      // doubles and each part rounded up to 256 bytes
-      const auto up = [](int64_t bytes) { return (bytes + 255) / 256 * 32; };
-      return up(2 * kMaxSlices * size_a) + up(2 * kMaxSlices * size_b) + up(2 * size_a) + up(2 * size_b) +
-             slots * kSplitTileM * kSplitTileN;
+      return up256(2 * slices * s.slice_a) + up256(2 * slices * s.slice_b) + up256(2 * s.exps) +
+             up256(s.slots * kSplitTileM * kSplitTileN * 8) + up256(4 * (static_cast<int64_t>(s.reduces.size()) + 1));
+    }
+    // bytes of FP64 scratch: partial tiles (two doubles an entry for complex), tickets
+    int64_t f64_bytes(const GemmSchedule &s)
+    {
+      return up256(s.slots * kF64TileM * kF64TileN * 16) + up256(4 * (static_cast<int64_t>(s.reduces.size()) + 1));
     }
   } // namespace
 
@@ -107,13 +228,8 @@ namespace ttg
     for (const Op &op : p.ops)
     {
       if (op.kind != OpKind::gemm) continue;
-      const GemmSchedule f = schedule_gemm(p, op, kF64TileM, kF64TileN);
-      const GemmSchedule s = schedule_gemm(p, op, kSplitTileM, kSplitTileN);
-      const int64_t size_a = p.buffers[static_cast<size_t>(op.src)].size;
-      const int64_t size_b = p.buffers[static_cast<size_t>(op.src2)].size;
-      // complex partials take two doubles an entry
-      need = std::max(need, 2 * f.slots * kF64TileM * kF64TileN);
-      need = std::max(need, split_scratch(size_a, size_b, s.slots));
+      need = std::max(need, (f64_bytes(schedule_gemm(p, op, kF64TileM, kF64TileN)) + 7) / 8);
+      need = std::max(need, (split_bytes(schedule_split(p, op), kMaxSlices) + 7) / 8);
     }
     return need;
   }
@@ -134,6 +250,11 @@ namespace ttg
       int64_t a, b;
       int32_t k, pad;
     };
+    struct DevSplitPair
+    {
+      int64_t sa, sb;
+      int32_t kp, ea, eb, pad;
+    };
 
     __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c)
     {
@@ -152,128 +273,292 @@ namespace ttg
     __device__ __forceinline__ double add_t(double a, double b) { return a + b; }
     __device__ __forceinline__ double2 add_t(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
-    // One work item: a 32x32 output tile over a K range, 64 threads of 4x4 entries, K staged 16 at
-    // a time through shared memory.  FP64 on this part issues about two DFMA per SM clock, which
-    // small balanced items keep busy on every SM.
-    template <typename T>
-    __global__ void __launch_bounds__(64) gemm_items_kernel(const T *__restrict__ A, const T *__restrict__ B,
-                                                            T *__restrict__ C, const DevBlock *__restrict__ blocks,
-                                                            const DevPair *__restrict__ pairs,
-                                                            const GemmItem *__restrict__ items, T *__restrict__ partial)
+    // a barrier over one worker's 128 threads (named barrier 1 + worker)
+    __device__ __forceinline__ void worker_sync(int worker)
     {
-      constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16, TM = 4, TN = 4, THREADS = 64;
-      __shared__ T as[BK][BM];
-      __shared__ T bs[BK][BN + 1];
-      const GemmItem it = items[blockIdx.x];
-      const DevBlock blk = blocks[it.block];
-      const int tx = threadIdx.x % (BN / TN), ty = threadIdx.x / (BN / TN);
-      T acc[TM][TN];
+      asm volatile("bar.sync %0, %1;\n" ::"r"(worker + 1), "r"(kWorkerThreads) : "memory");
+    }
+
+    // The next item for a worker: its first thread draws from the launch's counter (the word after
+    // the tile tickets, zeroed before the launch), so faster SMs simply take more items.
+    __device__ __forceinline__ int64_t claim(int worker, int lt, int *slot, int *counter)
+    {
+      if (lt == 0) *slot = atomicAdd(counter, 1);
+      worker_sync(worker);
+      const int64_t idx = *slot;
+      worker_sync(worker);
+      return idx;
+    }
+
+    // After a worker has written a partial tile: take the tile's ticket; the worker holding the last
+    // ticket sums every partial of the tile in slot order into C.  The fences order the partial
+    // writes before the ticket and the ticket before the reads (reads bypass L1).
+    template <typename T, int BM, int BN>
+    __device__ void finish_partial(int worker, int lt, int *flag, int *tickets, const GemmReduce *reduces, int reduce,
+                                   const DevBlock *blocks, const T *partial, T *C)
+    {
+      __threadfence();
+      worker_sync(worker);
+      const GemmReduce r = reduces[reduce];
+      if (lt == 0) *flag = atomicAdd(tickets + reduce, 1) == r.nslots - 1;
+      worker_sync(worker);
+      const bool last = *flag;
+      worker_sync(worker);
+      if (!last) return;
+      __threadfence();
+      const DevBlock blk = blocks[r.block];
+      // every entry of the tile sums its slots in slot order; the loads of four slots for all of the
+      // thread's entries are issued together, so a deep split costs a few L2 round trips, not one
+      // per slot
+      constexpr int PER = BM * BN / kWorkerThreads;
+      T sum[PER];
 #pragma unroll
-      for (int i = 0; i < TM; ++i)
-#pragma unroll
-        for (int j = 0; j < TN; ++j) acc[i][j] = zero_t<T>();
-      int32_t kbase = 0;
-      for (int32_t pi = 0; pi < blk.pair_count; ++pi)
+      for (int k = 0; k < PER; ++k) sum[k] = zero_t<T>();
+      const T *base = partial + static_cast<int64_t>(r.slot0) * BM * BN + lt;
+      int s = 0;
+      for (; s + 4 <= r.nslots; s += 4)
       {
-        const DevPair pr = pairs[blk.pair_begin + pi];
-        const int K = pr.k;
-        const int lo = max(it.k0 - kbase, 0), hi = min(it.k1 - kbase, K);
-        kbase += K;
-        if (lo >= hi) continue;
-        const T *a = A + pr.a;
-        const T *b = B + pr.b;
-        for (int k0 = lo; k0 < hi; k0 += BK)
-        {
-          for (int i = threadIdx.x; i < BM * BK; i += THREADS)
-          {
-            const int r = i / BK, kk = i % BK;
-            const int gm = it.m0 + r, gk = k0 + kk;
-            as[kk][r] = (gm < blk.m && gk < hi) ? a[static_cast<int64_t>(gm) * K + gk] : zero_t<T>();
-          }
-          for (int i = threadIdx.x; i < BK * BN; i += THREADS)
-          {
-            const int kk = i / BN, cc = i % BN;
-            const int gk = k0 + kk, gn = it.n0 + cc;
-            bs[kk][cc] = (gk < hi && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : zero_t<T>();
-          }
-          __syncthreads();
+        T v[4][PER];
 #pragma unroll
-          for (int kk = 0; kk < BK; ++kk)
-          {
-            T av[TM], bv[TN];
+        for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int i = 0; i < TM; ++i) av[i] = as[kk][ty * TM + i];
+          for (int k = 0; k < PER; ++k) v[u][k] = __ldcg(base + static_cast<int64_t>(s + u) * BM * BN + k * kWorkerThreads);
 #pragma unroll
-            for (int j = 0; j < TN; ++j) bv[j] = bs[kk][tx * TN + j];
+        for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int i = 0; i < TM; ++i)
-#pragma unroll
-              for (int j = 0; j < TN; ++j) acc[i][j] = fma_t(av[i], bv[j], acc[i][j]);
-          }
-          __syncthreads();
-        }
+          for (int k = 0; k < PER; ++k) sum[k] = add_t(sum[k], v[u][k]);
       }
-      if (it.slot >= 0)
+      for (; s < r.nslots; ++s)
+#pragma unroll
+        for (int k = 0; k < PER; ++k) sum[k] = add_t(sum[k], __ldcg(base + static_cast<int64_t>(s) * BM * BN + k * kWorkerThreads));
+#pragma unroll
+      for (int k = 0; k < PER; ++k)
       {
-        T *out = partial + static_cast<int64_t>(it.slot) * BM * BN;
+        const int e = lt + k * kWorkerThreads;
+        const int gm = r.m0 + e / BN, gn = r.n0 + e % BN;
+        if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = sum[k];
+      }
+      const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
+      if (lt == 0 && r.m0 + BM >= blk.m && r.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
+    }
+
+    // ---------------------------------------------------------------------------------------
+    // FP64 / complex128
+    // ---------------------------------------------------------------------------------------
+
+    // Persistent: kF64Workers workers of 128 threads, each computing 32 x 32 tiles over a K range
+    // with 2 x 4 entries per thread, K staged 16 at a time through its own shared memory (A padded
+    // to 33 columns so the k-fast, coalesced stores hit distinct banks).  FP64 retires about 0.44
+    // DFMA per clock per SM sub-partition on this part: the workers keep all four busy.
+    template <typename T>
+    __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1)
+      gemm_f64_kernel(const T *__restrict__ A, const T *__restrict__ B, T *__restrict__ C,
+                      const DevBlock *__restrict__ blocks, const DevPair *__restrict__ pairs,
+                      const GemmItem *__restrict__ items, int64_t n_items, const GemmReduce *__restrict__ reduces,
+                      int64_t n_reduces, T *__restrict__ partial, int *__restrict__ tickets)
+    {
+      constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16, TM = 2, TN = 4;
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
+      T(*as)[BM + 1] = reinterpret_cast<T(*)[BM + 1]>(smem_raw + worker * 2 * BK * (BM + 1) * sizeof(T));
+      T(*bs)[BN + 1] = reinterpret_cast<T(*)[BN + 1]>(smem_raw + (worker * 2 + 1) * BK * (BM + 1) * sizeof(T));
+      __shared__ int flags[kF64Workers];
+      const int tx = lt % (BN / TN), ty = lt / (BN / TN);
+      __shared__ int next[kF64Workers];
+      int *counter = tickets + n_reduces;  // workers per CTA = blockDim.x / 128, chosen at launch
+      for (int64_t idx = claim(worker, lt, next + worker, counter); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      {
+        const GemmItem it = items[idx];
+        const DevBlock blk = blocks[it.block];
+        T acc[TM][TN];
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
-          for (int j = 0; j < TN; ++j) out[(ty * TM + i) * BN + tx * TN + j] = acc[i][j];
-        return;
-      }
-#pragma unroll
-      for (int i = 0; i < TM; ++i)
-      {
-        const int gm = it.m0 + ty * TM + i;
-        if (gm >= blk.m) continue;
-#pragma unroll
-        for (int j = 0; j < TN; ++j)
+          for (int j = 0; j < TN; ++j) acc[i][j] = zero_t<T>();
+        int32_t kbase = 0;
+        for (int32_t pi = 0; pi < blk.pair_count; ++pi)
         {
-          const int gn = it.n0 + tx * TN + j;
-          if (gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[i][j];
+          const DevPair pr = pairs[blk.pair_begin + pi];
+          const int K = pr.k;
+          const int lo = max(it.k0 - kbase, 0), hi = min(it.k1 - kbase, K);
+          kbase += K;
+          if (lo >= hi) continue;
+          const T *a = A + pr.a;
+          const T *b = B + pr.b;
+          for (int k0 = lo; k0 < hi; k0 += BK)
+          {
+            for (int i = lt; i < BM * BK; i += kWorkerThreads)
+            {
+              const int r = i / BK, kk = i % BK;
+              const int gm = it.m0 + r, gk = k0 + kk;
+              as[kk][r] = (gm < blk.m && gk < hi) ? a[static_cast<int64_t>(gm) * K + gk] : zero_t<T>();
+            }
+            for (int i = lt; i < BK * BN; i += kWorkerThreads)
+            {
+              const int kk = i / BN, cc = i % BN;
+              const int gk = k0 + kk, gn = it.n0 + cc;
+              bs[kk][cc] = (gk < hi && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : zero_t<T>();
+            }
+            worker_sync(worker);
+#pragma unroll
+            for (int kk = 0; kk < BK; ++kk)
+            {
+              T av[TM], bv[TN];
+#pragma unroll
+              for (int i = 0; i < TM; ++i) av[i] = as[kk][ty * TM + i];
+#pragma unroll
+              for (int j = 0; j < TN; ++j) bv[j] = bs[kk][tx * TN + j];
+#pragma unroll
+              for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) acc[i][j] = fma_t(av[i], bv[j], acc[i][j]);
+            }
+            worker_sync(worker);
+          }
         }
+        if (it.slot >= 0)
+        {
+          T *out = partial + static_cast<int64_t>(it.slot) * BM * BN;
+#pragma unroll
+          for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) out[(ty * TM + i) * BN + tx * TN + j] = acc[i][j];
+          finish_partial<T, BM, BN>(worker, lt, flags + worker, tickets, reduces, it.reduce, blocks, partial, C);
+          continue;
+        }
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+        {
+          const int gm = it.m0 + ty * TM + i;
+          if (gm >= blk.m) continue;
+#pragma unroll
+          for (int j = 0; j < TN; ++j)
+          {
+            const int gn = it.n0 + tx * TN + j;
+            if (gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[i][j];
+          }
+        }
+        // the alignment pad after an odd-sized block reads as zero in arena-wide sums
+        const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
+        if (lt == 0 && it.m0 + BM >= blk.m && it.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
       }
-      // the alignment pad after an odd-sized block reads as zero in arena-wide sums
-      const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (threadIdx.x == 0 && it.m0 + BM >= blk.m && it.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
     }
 
-    // The partial tiles of one split tile, summed in slot order into C.
-    template <typename T>
-    __global__ void reduce_kernel(T *__restrict__ C, const DevBlock *__restrict__ blocks,
-                                  const GemmReduce *__restrict__ reduces, const T *__restrict__ partial, int bm, int bn)
+    __device__ __forceinline__ void dmma(double (&c)[2], double a, double b)
     {
-      const GemmReduce r = reduces[blockIdx.x];
-      const DevBlock blk = blocks[r.block];
-      for (int e = threadIdx.x; e < bm * bn; e += blockDim.x)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+                   : "+d"(c[0]), "+d"(c[1])
+                   : "d"(a), "d"(b));
+    }
+
+    // The float64 form of gemm_f64_kernel on the FP64 tensor instruction (mma m8n8k4 f64): each of
+    // a worker's 4 warps owns a 16 x 16 quarter of the 32 x 32 tile as 2 x 2 m8n8 accumulators; per
+    // K step of 16 staged in shared memory a warp issues 16 DMMA.
+    __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1)
+      gemm_dmma_kernel(const double *__restrict__ A, const double *__restrict__ B, double *__restrict__ C,
+                       const DevBlock *__restrict__ blocks, const DevPair *__restrict__ pairs,
+                       const GemmItem *__restrict__ items, int64_t n_items, const GemmReduce *__restrict__ reduces,
+                       int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
+    {
+      constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16;
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
+      // rows of 36 doubles: a warp's m8n8k4 fragment loads (k = lane % 4, row = lane / 4) then fall on
+      // distinct bank pairs within each half warp
+      constexpr int P = 36;
+      double(*as)[P] = reinterpret_cast<double(*)[P]>(smem_raw + worker * 2 * BK * P * sizeof(double));
+      double(*bs)[P] = reinterpret_cast<double(*)[P]>(smem_raw + (worker * 2 + 1) * BK * P * sizeof(double));
+      __shared__ int flags[kF64Workers];
+      const int warp = lt >> 5, lane = lt & 31;
+      const int wm = warp >> 1, wn = warp & 1;
+      const int fr = lane >> 2, fk = lane & 3;  // fragment row (or column) and k of this lane
+      __shared__ int next[kF64Workers];
+      int *counter = tickets + n_reduces;  // workers per CTA = blockDim.x / 128, chosen at launch
+      for (int64_t idx = claim(worker, lt, next + worker, counter); idx < n_items; idx = claim(worker, lt, next + worker, counter))
       {
-        const int i = e / bn, j = e % bn;
-        const int gm = r.m0 + i, gn = r.n0 + j;
-        if (gm >= blk.m || gn >= blk.n) continue;
-        T sum = zero_t<T>();
-        for (int s = 0; s < r.nslots; ++s) sum = add_t(sum, partial[static_cast<int64_t>(r.slot0 + s) * bm * bn + e]);
-        C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = sum;
+        const GemmItem it = items[idx];
+        const DevBlock blk = blocks[it.block];
+        double acc[2][2][2] = {};
+        int32_t kbase = 0;
+        for (int32_t pi = 0; pi < blk.pair_count; ++pi)
+        {
+          const DevPair pr = pairs[blk.pair_begin + pi];
+          const int K = pr.k;
+          const int lo = max(it.k0 - kbase, 0), hi = min(it.k1 - kbase, K);
+          kbase += K;
+          if (lo >= hi) continue;
+          const double *a = A + pr.a;
+          const double *b = B + pr.b;
+          for (int k0 = lo; k0 < hi; k0 += BK)
+          {
+            for (int i = lt; i < BM * BK; i += kWorkerThreads)
+            {
+              const int r = i / BK, kk = i % BK;
+              const int gm = it.m0 + r, gk = k0 + kk;
+              as[kk][r] = (gm < blk.m && gk < hi) ? a[static_cast<int64_t>(gm) * K + gk] : 0.0;
+            }
+            for (int i = lt; i < BK * BN; i += kWorkerThreads)
+            {
+              const int kk = i / BN, cc = i % BN;
+              const int gk = k0 + kk, gn = it.n0 + cc;
+              bs[kk][cc] = (gk < hi && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : 0.0;
+            }
+            worker_sync(worker);
+#pragma unroll
+            for (int kb = 0; kb < BK; kb += 4)
+            {
+              double af[2], bf[2];
+#pragma unroll
+              for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
+#pragma unroll
+              for (int j = 0; j < 2; ++j) bf[j] = bs[kb + fk][wn * 16 + j * 8 + fr];
+#pragma unroll
+              for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j) dmma(acc[i][j], af[i], bf[j]);
+            }
+            worker_sync(worker);
+          }
+        }
+        if (it.slot >= 0)
+        {
+          double *out = partial + static_cast<int64_t>(it.slot) * BM * BN;
+#pragma unroll
+          for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+              for (int h = 0; h < 2; ++h) out[(wm * 16 + i * 8 + fr) * BN + wn * 16 + j * 8 + fk * 2 + h] = acc[i][j][h];
+          finish_partial<double, BM, BN>(worker, lt, flags + worker, tickets, reduces, it.reduce, blocks, partial, C);
+          continue;
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+          for (int j = 0; j < 2; ++j)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+            {
+              const int gm = it.m0 + wm * 16 + i * 8 + fr, gn = it.n0 + wn * 16 + j * 8 + fk * 2 + h;
+              if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[i][j][h];
+            }
+        const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
+        if (lt == 0 && it.m0 + BM >= blk.m && it.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = 0.0;
       }
-      const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (threadIdx.x == 0 && r.m0 + bm >= blk.m && r.n0 + bn >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
     }
 
     // ---------------------------------------------------------------------------------------
     // split precision
     // ---------------------------------------------------------------------------------------
 
-    struct SplitLine
-    {
-      int64_t src, dst, exp;
-      int32_t len, src_stride;
-    };
-
-    // One warp per line (a row of A or a column of B): the power of two that bounds the line,
-    // then `slices` 7-bit integer slices of every entry, exact in bf16.
-    __global__ void split_lines_kernel(const double *__restrict__ src, uint16_t *__restrict__ slices,
-                                       int16_t *__restrict__ exps, int64_t slice_stride,
-                                       const SplitLine *__restrict__ lines, int64_t n_lines, int slices_n)
+    // One warp per line (a row of A or a column of B), lines of A from `a` and lines of B from `b`:
+    // the power of two 2^e that bounds the line, then each entry as the integer round(x 2^(56-e))
+    // cut into `slices` balanced 7-bit digits (|q_1| <= 128, |q_t| <= 64 after it), exact in bf16,
+    // written to a row padded with zeros to a multiple of 32.  Loads are issued eight at a time.
+    __global__ void split_lines_kernel(const double *__restrict__ a, const double *__restrict__ b,
+                                       uint16_t *__restrict__ slices_a, uint16_t *__restrict__ slices_b,
+                                       int16_t *__restrict__ exps, int64_t stride_a, int64_t stride_b,
+                                       const SplitLine *__restrict__ lines, int64_t lines_a, int64_t n_lines, int slices_n)
     {
       const int lane = threadIdx.x & 31;
       const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -281,83 +566,145 @@ namespace ttg
       for (int64_t l = warp; l < n_lines; l += warps)
       {
         const SplitLine line = lines[l];
+        const bool left = l < lines_a;
+        const double *src = (left ? a : b) + line.src;
+        uint16_t *dst = (left ? slices_a : slices_b) + line.dst;
+        const int64_t stride = left ? stride_a : stride_b;
         double big = 0.0;
-        for (int i = lane; i < line.len; i += 32) big = fmax(big, fabs(src[line.src + static_cast<int64_t>(i) * line.src_stride]));
+        for (int i0 = 0; i0 < line.len; i0 += 256)
+        {
+          double v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+          {
+            const int i = i0 + u * 32 + lane;
+            v[u] = i < line.len ? fabs(src[static_cast<int64_t>(i) * line.src_stride]) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) big = fmax(big, v[u]);
+        }
         for (int off = 16; off > 0; off >>= 1) big = fmax(big, __shfl_xor_sync(0xffffffffu, big, off));
         int e = 0;
         if (big > 0.0) frexp(big, &e);  // big = f 2^e with f in [0.5, 1): every |entry| / 2^e < 1
         if (lane == 0) exps[line.exp] = static_cast<int16_t>(e);
-        for (int i = lane; i < line.len; i += 32)
+        for (int i0 = 0; i0 < line.padded; i0 += 128)
         {
-          double x = ldexp(src[line.src + static_cast<int64_t>(i) * line.src_stride], -e);
-          for (int t = 0; t < slices_n; ++t)
+          long long x[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
           {
-            x *= 128.0;
-            const double q = rint(x);
-            x -= q;  // exact: q is the nearest integer to x
-            slices[t * slice_stride + line.dst + i] = __bfloat16_as_ushort(__double2bfloat16(q));
+            const int i = i0 + u * 32 + lane;
+            x[u] = i < line.len ? __double2ll_rn(ldexp(src[static_cast<int64_t>(i) * line.src_stride], 56 - e)) : 0ll;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+          {
+            const int i = i0 + u * 32 + lane;
+            if (i >= line.padded) continue;
+            long long r = x[u];
+            for (int t = 0; t < slices_n; ++t)
+            {
+              const int shift = 49 - 7 * t;  // digit t weighs 2^(49 - 7t) of the 2^56 scale
+              long long q;
+              if (shift > 0)
+              {
+                q = (r + (1ll << (shift - 1))) >> shift;  // nearest integer, halves up
+                r -= q << shift;
+              }
+              else
+                q = r;
+              dst[t * stride + i] = __bfloat16_as_ushort(__float2bfloat16_rn(static_cast<float>(q)));
+            }
           }
         }
       }
     }
 
-    __device__ __forceinline__ uint32_t pack2(uint16_t lo, uint16_t hi)
-    {
-      return static_cast<uint32_t>(lo) | (static_cast<uint32_t>(hi) << 16);
-    }
-
-    __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+    __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
     {
       asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
                    "{%0,%1,%2,%3};\n"
                    : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                   : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+                   : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
     }
 
-    // One work item: a 64x32 tile over a K range, 8 warps of 16x16 (one m16 x two n8 MMA tiles).
-    // For every K-chunk of <= 256, the products of slices t and u are summed exactly in fp32 per
-    // level t + u, then folded into FP64 with the weight 2^-7(t+u+2) and the pair's row and column
-    // scales.  S slices keep the levels t + u <= S - 1.
-    template <int S>
-    __global__ void __launch_bounds__(256, 1) gemm_split_kernel(const uint16_t *__restrict__ sa, const int16_t *__restrict__ ea,
-                                                             int64_t stride_a, const uint16_t *__restrict__ sb,
-                                                             const int16_t *__restrict__ eb, int64_t stride_b,
-                                                             double *__restrict__ C, const DevBlock *__restrict__ blocks,
-                                                             const DevPair *__restrict__ pairs,
-                                                             const GemmItem *__restrict__ items, double *__restrict__ partial)
+    __device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void *smem)
     {
-      const GemmItem it = items[blockIdx.x];
-      const DevBlock blk = blocks[it.block];
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      const uint32_t at = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+      asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                   : "r"(at));
+    }
+
+    // 16 bytes global -> shared; `bytes` 0 writes zeros and reads nothing
+    __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int bytes)
+    {
+      const uint32_t at = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(at), "l"(gmem), "r"(bytes));
+    }
+    __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+    template <int N>
+    __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+    constexpr int kRow = kSplitStepK + 8;  // shared row of 32 slice entries plus 8 of padding (80 bytes)
+
+    template <int S>
+    __host__ __device__ constexpr int split_worker_bytes() { return 2 * S * (kSplitTileM + kSplitTileN) * kRow * 2; }
+
+    // Persistent: kSplitWorkers workers of 128 threads (4 warps of 16 x 16), each computing 32 x 32
+    // tiles of one pair over a K range.  All S slices of a 32-wide K step are staged in the worker's
+    // shared memory with 16-byte cp.async, double buffered; every A and B slice fragment of a k16
+    // step is loaded once with ldmatrix and reused for the S(S+1)/2 products.  Level sums stay exact
+    // in fp32 for 256 of K and are then folded into FP64 with the pair's row and column scales: the
+    // four leading levels exactly, the rest (weights <= 2^-42 of the first) through one fp32 sum.
+    template <int S>
+    __global__ void __launch_bounds__(kSplitWorkers * kWorkerThreads, 1)
+      gemm_split_kernel(const uint16_t *__restrict__ sa_all, const uint16_t *__restrict__ sb_all,
+                        const int16_t *__restrict__ exps, int64_t stride_a, int64_t stride_b, double *__restrict__ C,
+                        const DevBlock *__restrict__ blocks, const DevSplitPair *__restrict__ spairs,
+                        const SplitItem *__restrict__ items, int64_t n_items, const GemmReduce *__restrict__ reduces,
+                        int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
+    {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
+      uint16_t *sA = reinterpret_cast<uint16_t *>(smem_raw + worker * split_worker_bytes<S>());  // [2][S][32][kRow]
+      uint16_t *sB = sA + 2 * S * kSplitTileM * kRow;                                           // [2][S][32][kRow]
+      __shared__ int flags[kSplitWorkers];
+      const int warp = lt >> 5, lane = lt & 31;
       const int g = lane >> 2, tig = lane & 3;
-      const int wm = warp >> 1, wn = warp & 1;        // 4 x 2 warps of 16 x 16
-      const int row0 = it.m0 + wm * 16 + g;           // and row0 + 8
-      const int colb = it.n0 + wn * 16 + tig * 2;     // + nsub * 8 + {0, 1}
-      double acc[2][4] = {};                          // [nsub][c0..c3]
-      int32_t kbase = 0;
-      for (int32_t pi = 0; pi < blk.pair_count; ++pi)
+      const int wm = warp >> 1, wn = warp & 1;
+      __shared__ int next[kSplitWorkers];
+      int *counter = tickets + n_reduces;
+      for (int64_t idx = claim(worker, lt, next + worker, counter); idx < n_items; idx = claim(worker, lt, next + worker, counter))
       {
-        const DevPair pr = pairs[blk.pair_begin + pi];
-        const int K = pr.k;
-        const int lo = max(it.k0 - kbase, 0), hi = min(it.k1 - kbase, K);
-        kbase += K;
-        if (lo >= hi) continue;
-        // the pair's scales of this thread's two rows and four columns
-        const bool r0ok = row0 < blk.m, r1ok = row0 + 8 < blk.m;
-        const int er0 = r0ok ? ea[pr.a + static_cast<int64_t>(row0) * K] : 0;
-        const int er1 = r1ok ? ea[pr.a + static_cast<int64_t>(row0 + 8) * K] : 0;
-        int ec[2][2];
-#pragma unroll
-        for (int ns = 0; ns < 2; ++ns)
-#pragma unroll
-          for (int h = 0; h < 2; ++h)
-          {
-            const int col = colb + ns * 8 + h;
-            ec[ns][h] = col < blk.n ? eb[pr.b + col] : 0;
-          }
-        for (int kc = lo; kc < hi; kc += kExactChunk)
+        const SplitItem it = items[idx];
+        const DevBlock blk = blocks[it.block];
+        double acc[2][4] = {};
+        const int r0 = it.m0 + wm * 16 + g, c0 = it.n0 + wn * 16 + tig * 2;
+        if (it.pair >= 0 && it.k1 > it.k0)
         {
-          const int kend = min(kc + kExactChunk, hi);
+          const DevSplitPair sp = spairs[it.pair];
+          const int rows = min(kSplitTileM, blk.m - it.m0), cols = min(kSplitTileN, blk.n - it.n0);
+          const uint16_t *ga = sa_all + sp.sa + static_cast<int64_t>(it.m0) * sp.kp;
+          const uint16_t *gb = sb_all + sp.sb + static_cast<int64_t>(it.n0) * sp.kp;
+          const auto load = [&](int stage, int k) {
+            for (int c = lt; c < S * kSplitTileM * 4; c += kWorkerThreads)
+            {
+              const int t = c / (kSplitTileM * 4), r = (c / 4) % kSplitTileM, q = c % 4;
+              const bool ok = r < rows;
+              cp_async16(sA + ((stage * S + t) * kSplitTileM + r) * kRow + q * 8,
+                         ga + t * stride_a + static_cast<int64_t>(ok ? r : 0) * sp.kp + k + q * 8, ok ? 16 : 0);
+            }
+            for (int c = lt; c < S * kSplitTileN * 4; c += kWorkerThreads)
+            {
+              const int u = c / (kSplitTileN * 4), r = (c / 4) % kSplitTileN, q = c % 4;
+              const bool ok = r < cols;
+              cp_async16(sB + ((stage * S + u) * kSplitTileN + r) * kRow + q * 8,
+                         gb + u * stride_b + static_cast<int64_t>(ok ? r : 0) * sp.kp + k + q * 8, ok ? 16 : 0);
+            }
+            cp_async_commit();
+          };
+          const int steps = (it.k1 - it.k0 + kSplitStepK - 1) / kSplitStepK;
           float lev[S][2][4];
 #pragma unroll
           for (int l = 0; l < S; ++l)
@@ -365,86 +712,129 @@ namespace ttg
             for (int ns = 0; ns < 2; ++ns)
 #pragma unroll
               for (int q = 0; q < 4; ++q) lev[l][ns][q] = 0.0f;
-          for (int k = kc; k < kend; k += 16)
+          const int er0 = r0 < blk.m ? exps[sp.ea + r0] : 0, er1 = r0 + 8 < blk.m ? exps[sp.ea + r0 + 8] : 0;
+          int ec[2][2];
+#pragma unroll
+          for (int ns = 0; ns < 2; ++ns)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) ec[ns][h] = c0 + ns * 8 + h < blk.n ? exps[sp.eb + c0 + ns * 8 + h] : 0;
+          load(0, it.k0);
+          for (int step = 0; step < steps; ++step)
           {
-            const int ka = k + tig * 2;  // this thread's first k in each half of the step
-#pragma unroll
-            for (int t = 0; t < S; ++t)
+            const int stage = step & 1;
+            if (step + 1 < steps)
             {
-              const uint16_t *at = sa + t * stride_a + pr.a;
-              uint32_t afrag[4];
-              const auto ld_a = [&](int row, int kk) -> uint16_t {
-                return (row < blk.m && kk < kend) ? at[static_cast<int64_t>(row) * K + kk] : uint16_t(0);
-              };
-              afrag[0] = pack2(ld_a(row0, ka), ld_a(row0, ka + 1));
-              afrag[1] = pack2(ld_a(row0 + 8, ka), ld_a(row0 + 8, ka + 1));
-              afrag[2] = pack2(ld_a(row0, ka + 8), ld_a(row0, ka + 9));
-              afrag[3] = pack2(ld_a(row0 + 8, ka + 8), ld_a(row0 + 8, ka + 9));
+              load(stage ^ 1, it.k0 + (step + 1) * kSplitStepK);
+              cp_async_wait<1>();
+            }
+            else
+              cp_async_wait<0>();
+            worker_sync(worker);
 #pragma unroll
-              for (int u = 0; u + t < S; ++u)
+            for (int kk = 0; kk < kSplitStepK; kk += 16)
+            {
+              uint32_t af[S][4], bf[S][4];
+#pragma unroll
+              for (int t = 0; t < S; ++t)
               {
-                const uint16_t *bt = sb + u * stride_b + pr.b;
-#pragma unroll
-                for (int ns = 0; ns < 2; ++ns)
-                {
-                  const int col = it.n0 + wn * 16 + ns * 8 + g;
-                  const auto ld_b = [&](int kk) -> uint16_t {
-                    return (col < blk.n && kk < kend) ? bt[static_cast<int64_t>(col) * K + kk] : uint16_t(0);
-                  };
-                  uint32_t bfrag[2] = {pack2(ld_b(ka), ld_b(ka + 1)), pack2(ld_b(ka + 8), ld_b(ka + 9))};
-                  mma_bf16(lev[t + u][ns], afrag, bfrag);
-                }
+                ldmatrix_x4(af[t], sA + ((stage * S + t) * kSplitTileM + wm * 16 + (lane & 15)) * kRow + kk + (lane >> 4) * 8);
+                ldmatrix_x4(bf[t], sB + ((stage * S + t) * kSplitTileN + wn * 16 + (lane & 7) + ((lane >> 4) << 3)) * kRow +
+                                     kk + ((lane >> 3) & 1) * 8);
               }
+#pragma unroll
+              for (int t = 0; t < S; ++t)
+#pragma unroll
+                for (int u = 0; u + t < S; ++u)
+                {
+                  mma_bf16(lev[t + u][0], af[t], bf[u][0], bf[u][1]);
+                  mma_bf16(lev[t + u][1], af[t], bf[u][2], bf[u][3]);
+                }
+            }
+            worker_sync(worker);
+            if ((step + 1) % (kExactChunk / kSplitStepK) == 0 || step + 1 == steps)
+            {
+#pragma unroll
+              for (int ns = 0; ns < 2; ++ns)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                  float tail = 0.0f;
+#pragma unroll
+                  for (int l = S - 1; l >= 4; --l) tail = fmaf(lev[l][ns][q], ldexpf(1.0f, -7 * (l - 4)), tail);
+                  double v = static_cast<double>(tail) * ldexp(1.0, -42);
+#pragma unroll
+                  for (int l = (S < 4 ? S : 4) - 1; l >= 0; --l)
+                    v = fma(static_cast<double>(lev[l][ns][q]), ldexp(1.0, -7 * (l + 2)), v);
+#pragma unroll
+                  for (int l = 0; l < S; ++l) lev[l][ns][q] = 0.0f;
+                  acc[ns][q] = fma(v, ldexp(1.0, (q < 2 ? er0 : er1) + ec[ns][q & 1]), acc[ns][q]);
+                }
             }
           }
-          // fold the exact level sums into FP64
+        }
+        if (it.slot >= 0)
+        {
+          double *out = partial + static_cast<int64_t>(it.slot) * kSplitTileM * kSplitTileN;
 #pragma unroll
           for (int ns = 0; ns < 2; ++ns)
 #pragma unroll
             for (int q = 0; q < 4; ++q)
-            {
-              double s = 0.0;
-#pragma unroll
-              for (int l = S - 1; l >= 0; --l) s = fma(static_cast<double>(lev[l][ns][q]), ldexp(1.0, -7 * (l + 2)), s);
-              const int er = q < 2 ? er0 : er1;
-              acc[ns][q] = fma(s, ldexp(1.0, er + ec[ns][q & 1]), acc[ns][q]);
-            }
+              out[(wm * 16 + g + (q >= 2 ? 8 : 0)) * kSplitTileN + wn * 16 + ns * 8 + tig * 2 + (q & 1)] = acc[ns][q];
+          finish_partial<double, kSplitTileM, kSplitTileN>(worker, lt, flags + worker, tickets, reduces, it.reduce, blocks,
+                                                           partial, C);
+          continue;
         }
-      }
-      if (it.slot >= 0)
-      {
-        double *out = partial + static_cast<int64_t>(it.slot) * kSplitTileM * kSplitTileN;
 #pragma unroll
         for (int ns = 0; ns < 2; ++ns)
 #pragma unroll
           for (int q = 0; q < 4; ++q)
           {
-            const int r = wm * 16 + g + (q >= 2 ? 8 : 0), c = wn * 16 + ns * 8 + tig * 2 + (q & 1);
-            out[r * kSplitTileN + c] = acc[ns][q];
+            const int gm = r0 + (q >= 2 ? 8 : 0), gn = c0 + ns * 8 + (q & 1);
+            if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[ns][q];
           }
-        return;
+        const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
+        if (lt == 0 && it.m0 + kSplitTileM >= blk.m && it.n0 + kSplitTileN >= blk.n && (entries & 1)) C[blk.c + entries] = 0.0;
       }
-#pragma unroll
-      for (int ns = 0; ns < 2; ++ns)
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-        {
-          const int gm = row0 + (q >= 2 ? 8 : 0), gn = colb + ns * 8 + (q & 1);
-          if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[ns][q];
-        }
-      const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (threadIdx.x == 0 && it.m0 + kSplitTileM >= blk.m && it.n0 + kSplitTileN >= blk.n && (entries & 1))
-        C[blk.c + entries] = 0.0;
+    }
+
+    // the persistent grid: one CTA per SM (or fewer when there are fewer items than workers)
+    int sm_count()
+    {
+      static int count = 0;
+      if (!count)
+      {
+        int device = 0;
+        cudaGetDevice(&device);
+        if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || count <= 0) count = 152;
+      }
+      return count;
+    }
+
+    // Shared memory that holds one CTA per SM: at least 120 KiB, so a second never fits beside it.
+    constexpr int kPinBytes = 120 * 1024;
+
+    template <typename K>
+    cudaError_t configure(K kernel, int bytes, std::once_flag &once)
+    {
+      cudaError_t e = cudaSuccess;
+      std::call_once(once, [&] { e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
+      return e;
     }
 
     template <int S>
-    cudaError_t launch_split_s(const uint16_t *sa, const int16_t *ea, int64_t stride_a, const uint16_t *sb,
-                               const int16_t *eb, int64_t stride_b, double *C, const DevBlock *blocks,
-                               const DevPair *pairs, const GemmItem *items, int64_t n_items, double *partial,
-                               cudaStream_t stream)
+    cudaError_t launch_split_s(const uint16_t *sa, const uint16_t *sb, const int16_t *exps, int64_t stride_a,
+                               int64_t stride_b, double *C, const DevBlock *blocks, const DevSplitPair *spairs,
+                               const SplitItem *items, int64_t n_items, const GemmReduce *reduces, int64_t n_reduces,
+                               double *partial, int *tickets, cudaStream_t stream)
     {
-      gemm_split_kernel<S><<<static_cast<unsigned>(n_items), 256, 0, stream>>>(sa, ea, stride_a, sb, eb, stride_b, C,
-                                                                              blocks, pairs, items, partial);
+      const int bytes = std::max(kSplitWorkers * split_worker_bytes<S>(), kPinBytes);
+      static std::once_flag once;
+      cudaError_t e = configure(gemm_split_kernel<S>, bytes, once);
+      if (e != cudaSuccess) return e;
+      const int grid = static_cast<int>(std::min<int64_t>(sm_count(), n_items));
+      const int workers = static_cast<int>(std::clamp<int64_t>((n_items + grid - 1) / grid, 1, kSplitWorkers));
+      gemm_split_kernel<S><<<grid, workers * kWorkerThreads, bytes, stream>>>(
+        sa, sb, exps, stride_a, stride_b, C, blocks, spairs, items, n_items, reduces, n_reduces, partial, tickets);
       return cudaGetLastError();
     }
   } // namespace
@@ -456,79 +846,96 @@ namespace ttg
   cudaError_t launch_gemm_f64(const Program &p, DeviceTables &t, size_t op_index, const void *A, const void *B, void *C,
                               bool complex, void *scratch, cudaStream_t stream)
   {
+    (void)p;
     const auto &sched = t.gemm[op_index];
     if (sched.n_items == 0) return cudaSuccess;
     const auto *blocks = reinterpret_cast<const DevBlock *>(t.blocks);
     const auto *pairs = reinterpret_cast<const DevPair *>(t.pairs);
+    char *base = static_cast<char *>(scratch);
+    void *partial = base;
+    int *tickets = reinterpret_cast<int *>(base + up256(sched.slots * kF64TileM * kF64TileN * 16));
+    cudaError_t e = cudaSuccess;
+    e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces + 1) * 4, stream);  // tickets and the item counter
+    if (e != cudaSuccess) return e;
+    // spread the items over every SM first: workers per CTA = items / SMs, at most kF64Workers
+    const int grid = static_cast<int>(std::min<int64_t>(sm_count(), sched.n_items));
+    const int workers = static_cast<int>(std::clamp<int64_t>((sched.n_items + grid - 1) / grid, 1, kF64Workers));
     if (complex)
     {
-      gemm_items_kernel<double2><<<static_cast<unsigned>(sched.n_items), 64, 0, stream>>>(
+      const int bytes = std::max<int>(kF64Workers * 2 * 16 * (kF64TileM + 1) * 16, kPinBytes);
+      static std::once_flag once;
+      if ((e = configure(gemm_f64_kernel<double2>, bytes, once)) != cudaSuccess) return e;
+      gemm_f64_kernel<double2><<<grid, workers * kWorkerThreads, bytes, stream>>>(
         static_cast<const double2 *>(A), static_cast<const double2 *>(B), static_cast<double2 *>(C), blocks, pairs,
-        sched.items, static_cast<double2 *>(scratch));
-      if (sched.n_reduces)
-        reduce_kernel<double2><<<static_cast<unsigned>(sched.n_reduces), 256, 0, stream>>>(
-          static_cast<double2 *>(C), blocks, sched.reduces, static_cast<const double2 *>(scratch), kF64TileM, kF64TileN);
+        sched.items, sched.n_items, sched.reduces, sched.n_reduces, static_cast<double2 *>(partial), tickets);
     }
     else
     {
-      gemm_items_kernel<double><<<static_cast<unsigned>(sched.n_items), 64, 0, stream>>>(
+      const int bytes = std::max<int>(kF64Workers * 2 * 16 * 36 * 8, kPinBytes);
+      static std::once_flag once;
+      if ((e = configure(gemm_dmma_kernel, bytes, once)) != cudaSuccess) return e;
+      gemm_dmma_kernel<<<grid, workers * kWorkerThreads, bytes, stream>>>(
         static_cast<const double *>(A), static_cast<const double *>(B), static_cast<double *>(C), blocks, pairs,
-        sched.items, static_cast<double *>(scratch));
-      if (sched.n_reduces)
-        reduce_kernel<double><<<static_cast<unsigned>(sched.n_reduces), 256, 0, stream>>>(
-          static_cast<double *>(C), blocks, sched.reduces, static_cast<const double *>(scratch), kF64TileM, kF64TileN);
+        sched.items, sched.n_items, sched.reduces, sched.n_reduces, static_cast<double *>(partial), tickets);
     }
-    (void)p;
     return cudaGetLastError();
   }
 
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream)
   {
+    (void)p;
+    (void)op;
     const auto &sched = t.split[op_index];
     if (sched.n_items == 0) return cudaSuccess;
-    const int64_t size_a = p.buffers[static_cast<size_t>(op.src)].size;
-    const int64_t size_b = p.buffers[static_cast<size_t>(op.src2)].size;
-    const auto up = [](int64_t bytes) { return (bytes + 255) / 256 * 256; };
     char *base = static_cast<char *>(scratch);
     auto *sa = reinterpret_cast<uint16_t *>(base);
-    base += up(2 * kMaxSlices * size_a);
+    base += up256(2 * kMaxSlices * sched.slice_a);
     auto *sb = reinterpret_cast<uint16_t *>(base);
-    base += up(2 * kMaxSlices * size_b);
-    auto *ea = reinterpret_cast<int16_t *>(base);
-    base += up(2 * size_a);
-    auto *eb = reinterpret_cast<int16_t *>(base);
-    base += up(2 * size_b);
+    base += up256(2 * kMaxSlices * sched.slice_b);
+    auto *exps = reinterpret_cast<int16_t *>(base);
+    base += up256(2 * sched.exps);
     auto *partial = reinterpret_cast<double *>(base);
-    const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
-    if (sched.n_lines_a)
-      split_lines_kernel<<<static_cast<unsigned>(std::min<int64_t>((sched.n_lines_a + 7) / 8, 152 * 16)), 256, 0, stream>>>(
-        A, sa, ea, size_a, lines, sched.n_lines_a, slices);
-    if (sched.n_lines_b)
-      split_lines_kernel<<<static_cast<unsigned>(std::min<int64_t>((sched.n_lines_b + 7) / 8, 152 * 16)), 256, 0, stream>>>(
-        B, sb, eb, size_b, lines + sched.n_lines_a, sched.n_lines_b, slices);
-    cudaError_t e = cudaGetLastError();
+    base += up256(sched.slots * kSplitTileM * kSplitTileN * 8);
+    auto *tickets = reinterpret_cast<int *>(base);
+    cudaError_t e = cudaSuccess;
+    e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces + 1) * 4, stream);  // tickets and the item counter
     if (e != cudaSuccess) return e;
+    const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
+    const int64_t n_lines = sched.n_lines_a + sched.n_lines_b;
+    if (n_lines)
+      split_lines_kernel<<<static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((n_lines + 7) / 8, 152 * 16))), 256, 0,
+                           stream>>>(A, B, sa, sb, exps, sched.slice_a, sched.slice_b, lines, sched.n_lines_a, n_lines, slices);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const auto *blocks = reinterpret_cast<const DevBlock *>(t.blocks);
-    const auto *pairs = reinterpret_cast<const DevPair *>(t.pairs);
+    const auto *spairs = reinterpret_cast<const DevSplitPair *>(sched.pairs);
+    const auto *items = reinterpret_cast<const SplitItem *>(sched.items);
     switch (slices)
     {
-    case 1: e = launch_split_s<1>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 2: e = launch_split_s<2>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 3: e = launch_split_s<3>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 4: e = launch_split_s<4>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 5: e = launch_split_s<5>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 6: e = launch_split_s<6>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 7: e = launch_split_s<7>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
-    case 8: e = launch_split_s<8>(sa, ea, size_a, sb, eb, size_b, C, blocks, pairs, sched.items, sched.n_items, partial, stream); break;
+#define TTG_SPLIT(S)                                                                                                    \
+  case S:                                                                                                               \
+    e = launch_split_s<S>(sa, sb, exps, sched.slice_a, sched.slice_b, C, blocks, spairs, items, sched.n_items,          \
+                          sched.reduces, sched.n_reduces, partial, tickets, stream);                                   \
+    break;
+      TTG_SPLIT(1) TTG_SPLIT(2) TTG_SPLIT(3) TTG_SPLIT(4) TTG_SPLIT(5) TTG_SPLIT(6) TTG_SPLIT(7) TTG_SPLIT(8)
+#undef TTG_SPLIT
     default: return cudaErrorInvalidValue;
     }
-    if (e != cudaSuccess) return e;
-    if (sched.n_reduces)
-      reduce_kernel<double><<<static_cast<unsigned>(sched.n_reduces), 256, 0, stream>>>(C, blocks, sched.reduces, partial,
-                                                                                       kSplitTileM, kSplitTileN);
-    return cudaGetLastError();
+    return e;
   }
+
+  namespace
+  {
+    template <typename T>
+    cudaError_t put(const std::vector<T> &host, void **dev)
+    {
+      *dev = nullptr;
+      if (host.empty()) return cudaSuccess;
+      cudaError_t e = cudaMalloc(dev, host.size() * sizeof(T));
+      if (e == cudaSuccess) e = cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
+      return e;
+    }
+  } // namespace
 
   // The device copies of every GEMM op's schedules and slicing lines.
   cudaError_t upload_gemm(const Program &p, DeviceTables &t)
@@ -539,46 +946,30 @@ namespace ttg
     {
       const Op &op = p.ops[i];
       if (op.kind != OpKind::gemm) continue;
-      for (int which = 0; which < 2; ++which)
+      cudaError_t e;
       {
-        const GemmSchedule s = schedule_gemm(p, op, which ? kSplitTileM : kF64TileM, which ? kSplitTileN : kF64TileN);
-        DeviceTables::GemmTables &dst = which ? t.split[i] : t.gemm[i];
+        const GemmSchedule s = schedule_gemm(p, op, kF64TileM, kF64TileN);
+        DeviceTables::GemmTables &dst = t.gemm[i];
         dst.n_items = static_cast<int64_t>(s.items.size());
         dst.n_reduces = static_cast<int64_t>(s.reduces.size());
-        cudaError_t e = cudaSuccess;
-        if (!s.items.empty())
-        {
-          e = cudaMalloc(&dst.items, s.items.size() * sizeof(GemmItem));
-          if (e == cudaSuccess) e = cudaMemcpy(dst.items, s.items.data(), s.items.size() * sizeof(GemmItem), cudaMemcpyHostToDevice);
-        }
-        if (e == cudaSuccess && !s.reduces.empty())
-        {
-          e = cudaMalloc(&dst.reduces, s.reduces.size() * sizeof(GemmReduce));
-          if (e == cudaSuccess)
-            e = cudaMemcpy(dst.reduces, s.reduces.data(), s.reduces.size() * sizeof(GemmReduce), cudaMemcpyHostToDevice);
-        }
-        if (e != cudaSuccess) return e;
-        if (!which) continue;
-        // slicing lines: every row of every left block, every column of every right block
-        std::vector<OperandBlock> left, right;
-        gemm_operands(p, op, left, right);
-        std::vector<SplitLine> lines;
-        for (const OperandBlock &a : left)
-          for (int32_t r = 0; r < a.rows; ++r)
-            lines.push_back({a.offset + static_cast<int64_t>(r) * a.cols, a.offset + static_cast<int64_t>(r) * a.cols,
-                             a.offset + static_cast<int64_t>(r) * a.cols, a.cols, 1});
-        dst.n_lines_a = static_cast<int64_t>(lines.size());
-        for (const OperandBlock &b : right)
-          for (int32_t c = 0; c < b.cols; ++c)
-            lines.push_back({b.offset + c, b.offset + static_cast<int64_t>(c) * b.rows, b.offset + c, b.rows, b.cols});
-        dst.n_lines_b = static_cast<int64_t>(lines.size()) - dst.n_lines_a;
-        if (!lines.empty())
-        {
-          e = cudaMalloc(&dst.lines, lines.size() * sizeof(SplitLine));
-          if (e == cudaSuccess) e = cudaMemcpy(dst.lines, lines.data(), lines.size() * sizeof(SplitLine), cudaMemcpyHostToDevice);
-          if (e != cudaSuccess) return e;
-        }
+        dst.slots = s.slots;
+        if ((e = put(s.items, reinterpret_cast<void **>(&dst.items))) != cudaSuccess) return e;
+        if ((e = put(s.reduces, reinterpret_cast<void **>(&dst.reduces))) != cudaSuccess) return e;
       }
+      const SplitSchedule s = schedule_split(p, op);
+      DeviceTables::SplitTables &dst = t.split[i];
+      dst.n_items = static_cast<int64_t>(s.items.size());
+      dst.n_reduces = static_cast<int64_t>(s.reduces.size());
+      dst.n_lines_a = s.lines_a;
+      dst.n_lines_b = static_cast<int64_t>(s.lines.size()) - s.lines_a;
+      dst.slice_a = s.slice_a;
+      dst.slice_b = s.slice_b;
+      dst.exps = s.exps;
+      dst.slots = s.slots;
+      if ((e = put(s.items, &dst.items)) != cudaSuccess) return e;
+      if ((e = put(s.reduces, reinterpret_cast<void **>(&dst.reduces))) != cudaSuccess) return e;
+      if ((e = put(s.pairs, &dst.pairs)) != cudaSuccess) return e;
+      if ((e = put(s.lines, &dst.lines)) != cudaSuccess) return e;
     }
     return cudaSuccess;
   }

@@ -26,6 +26,7 @@ namespace ttg
   struct GemmItem
   {
     int32_t block, m0, n0, k0, k1, slot;  // slot -1: the item covers its tile and writes C
+    int32_t reduce, pad;                   // the tile's GemmReduce when slot >= 0
   };
   struct GemmReduce
   {
@@ -38,9 +39,43 @@ namespace ttg
     int64_t slots = 0;  // partial tiles of bm x bn doubles
   };
 
+  // Split precision works pair by pair: an item is one pair's K range (a multiple of 32 long, but
+  // for the pair's last one), so a tile with several pairs or chunks always goes through partials.
+  struct SplitItem
+  {
+    int32_t block, m0, n0, pair, k0, k1, slot, reduce;
+  };
+  // Where a pair's slices and exponents sit in scratch: A slices rows of `kp` (K padded to 32),
+  // B slices transposed, one row of `kp` per column.
+  struct SplitPair
+  {
+    int64_t sa, sb;
+    int32_t kp, ea, eb, pad;
+  };
+  struct SplitLine
+  {
+    int64_t src, dst;
+    int32_t len, src_stride, padded, exp;
+  };
+  struct SplitSchedule
+  {
+    std::vector<SplitItem> items;
+    std::vector<GemmReduce> reduces;
+    std::vector<SplitPair> pairs;  // one per GemmPair of the program (only this op's are filled)
+    std::vector<SplitLine> lines;  // rows of A then columns of B
+    int64_t lines_a = 0;
+    int64_t slice_a = 0, slice_b = 0;  // elements of one slice of all A (B) rows
+    int64_t exps = 0;                  // int16 exponents
+    int64_t slots = 0;
+  };
+  SplitSchedule schedule_split(const Program &p, const Op &op);
+
   // Tile sizes of the two kernels.
   constexpr int kF64TileM = 32, kF64TileN = 32;
-  constexpr int kSplitTileM = 64, kSplitTileN = 32;
+  constexpr int kSplitTileM = 32, kSplitTileN = 32, kSplitStepK = 32;
+  // Persistent launches: one CTA per SM (held there by its shared memory), several workers of 128
+  // threads per CTA taking items round robin.
+  constexpr int kF64Workers = 4, kSplitWorkers = 2, kWorkerThreads = 128;
   constexpr int kMaxSlices = 8;
   constexpr int kExactChunk = 256;  // K over which fp32 sums of slice products stay exact
 

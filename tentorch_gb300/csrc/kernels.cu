@@ -122,10 +122,12 @@ namespace ttg
     for (void *p : {static_cast<void *>(gather), static_cast<void *>(chunks), static_cast<void *>(terms),
                     static_cast<void *>(blocks), static_cast<void *>(pairs)})
       if (p) cudaFree(p);
-    for (auto *tables : {&gemm, &split})
-      for (GemmTables &g : *tables)
-        for (void *p : {static_cast<void *>(g.items), static_cast<void *>(g.reduces), g.lines})
-          if (p) cudaFree(p);
+    for (GemmTables &g : gemm)
+      for (void *p : {static_cast<void *>(g.items), static_cast<void *>(g.reduces)})
+        if (p) cudaFree(p);
+    for (SplitTables &g : split)
+      for (void *p : {g.items, g.pairs, g.lines, static_cast<void *>(g.reduces)})
+        if (p) cudaFree(p);
   }
 
   namespace

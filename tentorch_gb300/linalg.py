@@ -68,6 +68,14 @@ class Plan:
         self.workspace, self.flops, self.moved, self.n_ops = ws.value, flops.value, moved.value, ops.value
         self.prepared = []
 
+    def describe(self) -> str:
+        '''The plan's operations and GEMM block shapes, as text.'''
+        n = i64()
+        check(lib.tt_plan_describe(self.handle, 0, None, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value + 1)
+        check(lib.tt_plan_describe(self.handle, n.value + 1, buf, ctypes.byref(n)))
+        return buf.value.decode()
+
     def prepared_size(self, operand: int) -> int:
         n = i64()
         check(lib.tt_plan_prepared_size(self.handle, operand, ctypes.byref(n)))
