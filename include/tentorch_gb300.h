@@ -39,6 +39,8 @@ extern "C" {
 #define TT_DTYPE_FLOAT64 0
 #define TT_DTYPE_COMPLEX128 1
 
+#define TT_PRECISION_PER_BLOCK (-1) /* tt_plan_execute: one cuBLAS call per block pair */
+
 typedef struct tt_plan tt_plan;
 
 /* The message of the last failure on this thread. */
@@ -103,10 +105,18 @@ int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace
 /* A text listing of the plan's operations and GEMM block shapes (m, n, K per pair), for diagnosis;
  * writes at most cap-1 characters and a terminating zero, *length the full size. */
 int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length);
+/* The gather index of operation `op` when it is a gather (a composed chain of leg moves whose F and
+ * R symbols are all 1): output entry i reads input entry index[i], -1 writes zero.  *count is the
+ * number of entries; nothing is copied when cap < *count.  For checking compiled leg moves against
+ * the reference's per-step plans (tentorch/tensors/place.cpp:199-247). */
+int32_t tt_plan_gather(const tt_plan *plan, int32_t op, int64_t cap, int32_t *index, int64_t *count);
 /* Elements of operand `i`'s prepared arena, 0 when the operand needs no preparation. */
 int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements);
 /* Execute on `stream` (a cudaStream_t, 0 for the legacy stream).  precision 0: FP64 block
- * products; k >= 1: split products on the tensor cores with k bf16 slices per operand.
+ * products in the grouped persistent kernels; k >= 1: split products on the tensor cores with k
+ * bf16 slices per operand; TT_PRECISION_PER_BLOCK (-1): the plain per-block FP64 form, one cuBLAS
+ * call per block pair as the reference issues them on a CUDA device
+ * (tentorch/linalg/graded/contract.cpp:148-163), the comparison arm of the grouped kernels.
  * `prepared` (may be NULL, or hold NULLs) gives operands' prepared arenas from tt_plan_prepare. */
 int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                         const void *const *prepared, void *output, void *workspace, void *stream);

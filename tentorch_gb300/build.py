@@ -74,7 +74,7 @@ def build(verbose: bool = False) -> str:
             handle.write(f'== {os.path.basename(src)}\n{text}\n')
     objects = [os.path.join(OBJ, os.path.basename(s) + '.o') for s in sources]
     if jobs or not os.path.exists(LIBRARY) or os.path.getmtime(LIBRARY) < max(os.path.getmtime(o) for o in objects):
-        link = [_nvcc(), *ARCH, '-shared', '-o', LIBRARY, *objects, '-lcudart']
+        link = [_nvcc(), *ARCH, '-shared', '-o', LIBRARY, *objects, '-lcublas', '-lcudart']
         result = subprocess.run(link, capture_output = True, text = True)
         if result.returncode != 0:
             raise RuntimeError(f'linking failed:\n{result.stdout}{result.stderr}')

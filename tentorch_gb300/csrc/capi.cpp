@@ -342,6 +342,21 @@ extern "C"
     });
   }
 
+  int32_t tt_plan_gather(const tt_plan *plan, int32_t op, int64_t cap, int32_t *index, int64_t *count)
+  {
+    return guarded([&] {
+      if (!plan) throw ttg::InvalidArgument("no plan");
+      const ttg::Program &p = *plan->program;
+      if (op < 0 || static_cast<size_t>(op) >= p.ops.size())
+        throw ttg::OutOfRange("the plan has no operation " + std::to_string(op));
+      const ttg::Op &o = p.ops[static_cast<size_t>(op)];
+      if (o.kind != ttg::OpKind::gather) throw ttg::InvalidArgument("operation " + std::to_string(op) + " is not a gather");
+      *count = o.count;
+      if (cap >= o.count && o.count > 0)
+        std::memcpy(index, p.gather_index.data() + o.begin, static_cast<size_t>(o.count) * sizeof(int32_t));
+    });
+  }
+
   int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length)
   {
     return guarded([&] {
@@ -389,7 +404,8 @@ extern "C"
   {
     if (!plan) return fail(TT_EINVAL, "no plan");
     if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128) return fail(TT_EINVAL, "unknown dtype");
-    if (precision < 0 || precision > 8) return fail(TT_EINVAL, "precision is 0 (FP64) or 1..8 slices");
+    if (precision < TT_PRECISION_PER_BLOCK || precision > 8)
+      return fail(TT_EINVAL, "precision is 0 (FP64), 1..8 slices, or -1 (per-block FP64)");
     if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
       return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
     ttg::ExecArgs args;
@@ -415,7 +431,8 @@ extern "C"
                                 float *op_ms, int32_t *op_kind)
   {
     if (!plan) return fail(TT_EINVAL, "no plan");
-    if (precision < 0 || precision > 8) return fail(TT_EINVAL, "precision is 0 (FP64) or 1..8 slices");
+    if (precision < TT_PRECISION_PER_BLOCK || precision > 8)
+      return fail(TT_EINVAL, "precision is 0 (FP64), 1..8 slices, or -1 (per-block FP64)");
     if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
       return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
     const ttg::Program &p = *plan->program;

@@ -185,6 +185,13 @@ namespace ttg
 
   const std::vector<Outcome> &Category::outcomes(const Sector &a, const Sector &b) const
   {
+    if (a.size == 1 && b.size == 1 && a[0] == static_cast<int32_t>(a[0]) && b[0] == static_cast<int32_t>(b[0]))
+    {
+      const uint64_t packed = (static_cast<uint64_t>(static_cast<uint32_t>(a[0])) << 32) | static_cast<uint32_t>(b[0]);
+      auto hit = outcomes_packed_.find(packed);
+      if (hit == outcomes_packed_.end()) hit = outcomes_packed_.emplace(packed, compute_outcomes(a, b)).first;
+      return hit->second;
+    }
     const auto k = std::make_pair(a, b);
     auto found = outcomes_.find(k);
     if (found == outcomes_.end()) found = outcomes_.emplace(k, compute_outcomes(a, b)).first;
@@ -463,6 +470,33 @@ namespace ttg
       if (coupled == cat.trivial()) out.push_back(Tree{{}, {}, {}, coupled});
       return out;
     }
+    // The walk below visits the trees in the reference's order; it only enters a partial fusion
+    // that can still reach `coupled` through the legs left, found by one pass forward (the
+    // partial fusions there are) and one backward (those that reach the root).
+    std::vector<std::set<Sector>> alive(n + 1);
+    {
+      std::vector<std::set<Sector>> reach(n + 1);
+      reach[1].insert(legs[0]->sectors.begin(), legs[0]->sectors.end());
+      for (size_t k = 1; k < n; ++k)
+        for (const Sector &x : reach[k])
+          for (const Sector &s : legs[k]->sectors)
+            for (const Outcome &o : cat.outcomes(x, s)) reach[k + 1].insert(o.sector);
+      if (reach[n].count(coupled)) alive[n].insert(coupled);
+      for (size_t k = n - 1; k >= 1; --k)
+        for (const Sector &x : reach[k])
+        {
+          bool reaches = false;
+          for (size_t j = 0; j < legs[k]->sectors.size() && !reaches; ++j)
+            for (const Outcome &o : cat.outcomes(x, legs[k]->sectors[j]))
+              if (alive[k + 1].count(o.sector))
+              {
+                reaches = true;
+                break;
+              }
+          if (reaches) alive[k].insert(x);
+        }
+    }
+    if (alive[n].empty()) return out;
     Tree tree;
     tree.sectors.resize(n);
     tree.inner.resize(n >= 2 ? n - 2 : 0);
@@ -479,13 +513,14 @@ namespace ttg
           {
             if (s == coupled) out.push_back(tree);
           }
-          else
+          else if (alive[1].count(s))
             walk(1, s);
           continue;
         }
         for (const Outcome &o : cat.outcomes(previous, s))
         {
           if (leg + 1 == n && !(o.sector == coupled)) continue;
+          if (leg + 1 < n && !alive[leg + 1].count(o.sector)) continue;
           if (leg + 1 < n) tree.inner[leg - 1] = o.sector;
           for (int32_t copy = 0; copy < o.multiplicity; ++copy)
           {
@@ -837,6 +872,21 @@ namespace ttg
     const std::vector<Leg> &giving = from_codomain ? codomain : domain;
     const std::vector<Leg> &taking = from_codomain ? domain : codomain;
     const Leg moved_leg = giving.back();
+    // The bent leg keeps its blocks and its sector reads as the dual one on the other side, so the
+    // copies of a sector land in the rows of its dual: the two have to carry the same multiplets.
+    // The reference assumes it (tentorch/linalg/graded/svd.cpp:97-100) and writes past its blocks
+    // when it does not hold; here it is an error.
+    for (size_t b = 0; b < moved_leg->sectors.size(); ++b)
+    {
+      const Sector d = cat.dual(moved_leg->sectors[b]);
+      const auto it = std::lower_bound(moved_leg->sectors.begin(), moved_leg->sectors.end(), d);
+      if (it != moved_leg->sectors.end() && *it == d &&
+          moved_leg->mult[static_cast<size_t>(it - moved_leg->sectors.begin())] != moved_leg->mult[b])
+        throw InvalidArgument("a leg bent across the tensor needs each sector and its dual to carry the same "
+                              "multiplets, but " + moved_leg->sectors[b].str() + " has " +
+                              std::to_string(moved_leg->mult[b]) + " and " + d.str() + " has " +
+                              std::to_string(moved_leg->mult[static_cast<size_t>(it - moved_leg->sectors.begin())]));
+    }
     const std::vector<Leg> kept_giving(giving.begin(), giving.end() - 1);
     std::vector<Leg> kept_taking = taking;
     kept_taking.push_back(moved_leg);
@@ -947,6 +997,19 @@ namespace ttg
     return plan;
   }
 
+  // tentorch/tensors/place.cpp:199-214: the leading domain legs a place leaves where they are
+  // (none when a codomain leg goes below)
+  int32_t chain_kept(int32_t height, int32_t depth, const std::vector<int32_t> &below)
+  {
+    bool descends = false;
+    for (size_t at = 0; !descends && at < below.size(); ++at) descends = below[at] < height;
+    int32_t kept = 0;
+    while (!descends && kept < depth && kept < static_cast<int32_t>(below.size()) &&
+           below[static_cast<size_t>(kept)] == height + kept)
+      ++kept;
+    return kept;
+  }
+
   // tentorch/tensors/place.cpp:41-107,199-247
   std::vector<Step> chain(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
   {
@@ -992,12 +1055,7 @@ namespace ttg
       }
       add(from_codomain ? 1 : 2, 0);
     };
-    bool descends = false;
-    for (size_t at = 0; !descends && at < below.size(); ++at) descends = below[at] < height;
-    int32_t kept = 0;
-    while (!descends && kept < depth && kept < static_cast<int32_t>(below.size()) &&
-           below[static_cast<size_t>(kept)] == height + kept)
-      ++kept;
+    const int32_t kept = chain_kept(height, depth, below);
     for (int32_t at = kept; at < depth; ++at) fold(false);
     const auto position_of = [height, depth](int32_t leg)
     { return leg < height ? leg : height + (depth - 1 - (leg - height)); };

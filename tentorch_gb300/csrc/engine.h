@@ -128,6 +128,8 @@ namespace ttg
     int64_t param_;
     std::string name_;
     mutable std::map<std::pair<Sector, Sector>, std::vector<Outcome>> outcomes_;
+    // the same cache for single-label sectors with labels in 32 bits, keyed by the packed pair
+    mutable std::unordered_map<uint64_t, std::vector<Outcome>> outcomes_packed_;
     mutable std::map<std::array<Sector, 4>, Matrix> f_;
     mutable std::map<std::pair<Sector, Sector>, Matrix> r_;
   };
@@ -262,6 +264,9 @@ namespace ttg
   };
   // The chain of tentorch/tensors/place.cpp:199-247: fold the domain tail up, bubble sort, fold down.
   std::vector<Step> chain(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below);
+  // The leading domain legs the chain leaves in place: the others are bent up first, and every leg
+  // of below[kept:] is bent down last.
+  int32_t chain_kept(int32_t height, int32_t depth, const std::vector<int32_t> &below);
 
   // All shifts of one step for one block of its `before` space, cached.
   const std::vector<Shift> &step_plan(const Step &step, const BlockKey &key);

@@ -48,7 +48,8 @@ namespace ttg
   struct ExecArgs
   {
     bool complex = false;                  // complex128 arenas (else float64)
-    int32_t precision = 0;                 // 0: FP64 products; k > 0: split products with k slices
+    int32_t precision = 0;                 // 0: FP64 products; k > 0: split products with k slices;
+                                           // -1: the plain per-block FP64 form (one cuBLAS call per pair)
     const void *const *inputs = nullptr;   // one arena per operand
     const void *const *prepared = nullptr; // per operand: its prepared arena, or null
     void *output = nullptr;
@@ -67,6 +68,9 @@ namespace ttg
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream);
   cudaError_t upload_gemm(const Program &p, DeviceTables &t);
+  // The plain per-block form (per_block.cu): one cuBLAS call per block pair.
+  cudaError_t launch_gemm_per_block(const Program &p, const Op &op, const void *A, const void *B, void *C, bool complex,
+                                    cudaStream_t stream);
 
   // Record a failure for tt_last_error() and return its status code (capi.cpp).
   int32_t report(int32_t code, const std::string &message);

@@ -82,15 +82,11 @@ namespace ttg
         const Category &cat = *v.space->cat;
         if (cat.trivial_symbols())
         {
-          std::shared_ptr<std::vector<int32_t>> current = v.pending;
-          for (const Step &step : steps)
-          {
-            std::vector<int32_t> back = permutation_of(step);
-            if (current)
-              for (int32_t &b : back) b = b >= 0 ? (*current)[static_cast<size_t>(b)] : -1;
-            current = std::make_shared<std::vector<int32_t>>(std::move(back));
-          }
-          return Value{v.buffer, steps.back().after, current, v.phase};
+          std::vector<int32_t> back = relabel(v.space, above, below, steps.back().after);
+          if (v.pending)
+            for (int32_t &b : back) b = b >= 0 ? (*v.pending)[static_cast<size_t>(b)] : -1;
+          return Value{v.buffer, steps.back().after,
+                       std::make_shared<std::vector<int32_t>>(std::move(back)), v.phase};
         }
         Value at = materialize(v);
         for (const Step &step : steps)
@@ -251,30 +247,145 @@ namespace ttg
     private:
       void emit(const Op &op) { p_.ops.push_back(op); }
 
-      // The gather index of one step whose coefficients are all 1: after[i] = before[index[i]].
-      std::vector<int32_t> permutation_of(const Step &step)
+      // The composed gather index of a whole chain of leg moves when every F and R symbol is 1:
+      // after[i] = before[index[i]], -1 for entries nothing writes.  Such a chain only relabels:
+      // the entry at sector s_l, copy c_l of every leg l lands at the same copies of the output
+      // legs, a leg that ends on the other side reading its sector as the dual (each bend reads
+      // the dual sector's rows, tentorch/tensors/regroup.cpp:260-417).  A bent leg that does not
+      // hold the dual of an entry's sector drops the entry, as the chain's bends do; the chain
+      // bends every leg of below[kept:] down and every domain leg past `kept` up.  The result is
+      // the composition of the per-step permutations, built in one pass over the entries instead
+      // of one pass per step.
+      std::vector<int32_t> relabel(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below,
+                                   Space out)
       {
-        Space before = step.before, after = step.after;
-        if (after->size > std::numeric_limits<int32_t>::max() || before->size > std::numeric_limits<int32_t>::max())
+        const Category &cat = *in->cat;
+        if (out->size > std::numeric_limits<int32_t>::max() || in->size > std::numeric_limits<int32_t>::max())
           throw InvalidArgument("an arena of more than 2^31 entries");
-        std::vector<int32_t> back(static_cast<size_t>(after->size), -1);
-        for (const Block &blk : before->blocks)
-          for (const Shift &shift : step_plan(step, blk.key))
+        const int32_t h = static_cast<int32_t>(in->codomain.size()), d = static_cast<int32_t>(in->domain.size());
+        const int32_t n = h + d;
+        const std::vector<Leg> legs = in->legs();
+        const int32_t kept = chain_kept(h, d, below);
+        std::vector<bool> bent(static_cast<size_t>(n), false), switched(static_cast<size_t>(n), false);
+        for (int32_t l = h + kept; l < n; ++l) bent[static_cast<size_t>(l)] = true;
+        for (size_t j = static_cast<size_t>(kept); j < below.size(); ++j) bent[static_cast<size_t>(below[j])] = true;
+        for (const int32_t l : above) switched[static_cast<size_t>(l)] = l >= h;
+        for (const int32_t l : below) switched[static_cast<size_t>(l)] = l < h;
+        // per leg and block of that leg: whether an entry survives the bends, and the paired
+        // multiplets a bend needs (the check bend_plan makes)
+        std::vector<std::vector<bool>> survives(static_cast<size_t>(n));
+        for (int32_t l = 0; l < n; ++l)
+        {
+          const Leg leg = legs[static_cast<size_t>(l)];
+          survives[static_cast<size_t>(l)].assign(leg->sectors.size(), true);
+          if (!bent[static_cast<size_t>(l)]) continue;
+          for (size_t b = 0; b < leg->sectors.size(); ++b)
           {
-            const int32_t t = after->find(shift.to);
-            if (t < 0) throw LogicError("a move lands outside the tensor it builds");
-            const int64_t ot = after->blocks[static_cast<size_t>(t)].offset;
-            for (const Piece &piece : shift.pieces)
+            const Sector dual = cat.dual(leg->sectors[b]);
+            const auto it = std::lower_bound(leg->sectors.begin(), leg->sectors.end(), dual);
+            if (it == leg->sectors.end() || !(*it == dual))
             {
-              if (piece.coefficient != cplx(1.0, 0.0)) throw LogicError("a permutation step with a coefficient");
-              for (int64_t i = 0; i < piece.run; ++i)
+              survives[static_cast<size_t>(l)][b] = false;
+              continue;
+            }
+            const int64_t other = leg->mult[static_cast<size_t>(it - leg->sectors.begin())];
+            if (other != leg->mult[b] && !in->blocks.empty())
+              throw InvalidArgument("a leg bent across the tensor needs each sector and its dual to carry the same "
+                                    "multiplets, but " + leg->sectors[b].str() + " has " +
+                                    std::to_string(leg->mult[b]) + " and " + dual.str() + " has " +
+                                    std::to_string(other));
+          }
+        }
+        // the output trees by their sector tuples: (root, first row) on each side
+        const std::vector<Leg> out_cod = out->codomain, out_dom = out->domain;
+        std::map<std::vector<Sector>, std::pair<Sector, int64_t>> rows_of, cols_of;
+        for (const Block &ob : out->blocks)
+        {
+          for (const auto &[side, root, table] :
+               {std::make_tuple(&out_cod, ob.key.codomain, &rows_of), std::make_tuple(&out_dom, ob.key.domain, &cols_of)})
+          {
+            const Layout &lay = layout_of(cat, *side, root);
+            for (size_t t = 0; t < lay.trees.size(); ++t) table->emplace(lay.trees[t].sectors, std::make_pair(root, lay.offsets[t]));
+          }
+        }
+        std::vector<int32_t> back(static_cast<size_t>(out->size), -1);
+        std::vector<Sector> sec(static_cast<size_t>(n)), cod_out(above.size()), dom_out(below.size());
+        std::vector<int64_t> extent(static_cast<size_t>(n)), in_stride(static_cast<size_t>(n)),
+          out_stride(static_cast<size_t>(n)), copy(static_cast<size_t>(n));
+        std::vector<int32_t> order(static_cast<size_t>(n));  // legs in output order, the last fastest
+        for (size_t i = 0; i < above.size(); ++i) order[i] = above[i];
+        for (size_t j = 0; j < below.size(); ++j) order[above.size() + j] = below[j];
+        for (const Block &blk : in->blocks)
+        {
+          const Layout &rl = layout_of(cat, in->codomain, blk.key.codomain);
+          const Layout &cl = layout_of(cat, in->domain, blk.key.domain);
+          for (size_t rt = 0; rt < rl.trees.size(); ++rt)
+            for (size_t ct = 0; ct < cl.trees.size(); ++ct)
+            {
+              bool keep = true;
+              for (int32_t l = 0; l < n && keep; ++l)
               {
-                int32_t &slot = back[static_cast<size_t>(ot + piece.last + i * piece.to_step)];
-                if (slot >= 0) throw LogicError("a permutation step writes one entry twice");
-                slot = static_cast<int32_t>(blk.offset + piece.first + i * piece.from_step);
+                const Sector &s = l < h ? rl.trees[rt].sectors[static_cast<size_t>(l)]
+                                        : cl.trees[ct].sectors[static_cast<size_t>(l - h)];
+                sec[static_cast<size_t>(l)] = s;
+                const int64_t at = legs[static_cast<size_t>(l)]->index_of(s);
+                keep = survives[static_cast<size_t>(l)][static_cast<size_t>(at)];
+                extent[static_cast<size_t>(l)] = legs[static_cast<size_t>(l)]->mult[static_cast<size_t>(at)];
+              }
+              if (!keep) continue;
+              const auto label = [&](int32_t l)
+              { return switched[static_cast<size_t>(l)] ? cat.dual(sec[static_cast<size_t>(l)]) : sec[static_cast<size_t>(l)]; };
+              for (size_t i = 0; i < above.size(); ++i) cod_out[i] = label(above[i]);
+              for (size_t j = 0; j < below.size(); ++j) dom_out[j] = label(below[j]);
+              const auto r = rows_of.find(cod_out);
+              const auto c = cols_of.find(dom_out);
+              if (r == rows_of.end() || c == cols_of.end()) continue;
+              const int32_t ob_at = out->find(BlockKey{r->second.first, c->second.first, 0});
+              if (ob_at < 0) continue;
+              const Block &ob = out->blocks[static_cast<size_t>(ob_at)];
+              // strides: input rows and columns with the last leg of each side fastest; the same
+              // for the output sides
+              int64_t run = blk.cols;
+              for (int32_t l = h - 1; l >= 0; --l) in_stride[static_cast<size_t>(l)] = run, run *= extent[static_cast<size_t>(l)];
+              run = 1;
+              for (int32_t l = n - 1; l >= h; --l) in_stride[static_cast<size_t>(l)] = run, run *= extent[static_cast<size_t>(l)];
+              run = ob.cols;
+              for (size_t i = above.size(); i-- > 0;)
+                out_stride[static_cast<size_t>(above[i])] = run, run *= extent[static_cast<size_t>(above[i])];
+              run = 1;
+              for (size_t j = below.size(); j-- > 0;)
+                out_stride[static_cast<size_t>(below[j])] = run, run *= extent[static_cast<size_t>(below[j])];
+              const int64_t in_base = blk.offset + rl.offsets[rt] * blk.cols + cl.offsets[ct];
+              const int64_t out_base = ob.offset + r->second.second * ob.cols + c->second.second;
+              // walk every copy tuple in output order, the last output leg innermost
+              std::fill(copy.begin(), copy.end(), 0);
+              int64_t src = in_base, dst = out_base;
+              const int32_t inner = order[static_cast<size_t>(n - 1)];
+              const int64_t inner_extent = n ? extent[static_cast<size_t>(inner)] : 1;
+              const int64_t inner_in = n ? in_stride[static_cast<size_t>(inner)] : 0;
+              const int64_t inner_out = n ? out_stride[static_cast<size_t>(inner)] : 0;
+              while (true)
+              {
+                for (int64_t k = 0; k < inner_extent; ++k)
+                  back[static_cast<size_t>(dst + k * inner_out)] = static_cast<int32_t>(src + k * inner_in);
+                int32_t at = n - 2;
+                for (; at >= 0; --at)
+                {
+                  const size_t l = static_cast<size_t>(order[static_cast<size_t>(at)]);
+                  if (++copy[l] < extent[l])
+                  {
+                    src += in_stride[l];
+                    dst += out_stride[l];
+                    break;
+                  }
+                  src -= (extent[l] - 1) * in_stride[l];
+                  dst -= (extent[l] - 1) * out_stride[l];
+                  copy[l] = 0;
+                }
+                if (at < 0) break;
               }
             }
-          }
+        }
         return back;
       }
 

@@ -1,0 +1,81 @@
+'''
+The Lanczos eigensolver of the reference (tentorch/linalg/lanczos.py:8-64) over the engine's
+block-sparse tensors, kept on the GPU.
+
+Every Krylov step runs on device-resident scalars: the projections alpha and the norms beta stay
+0-d device tensors, and the two full reorthogonalisation passes project against the whole basis at
+once (one matrix-vector product for the coefficients and one for the update, over the stacked
+arenas).  The host reads the tridiagonal matrix once, after the last step, and applies the
+reference's early stop (a step whose beta falls below `tol` ends the space) to what it reads: the
+steps computed after such a stop are discarded, so the result is the reference's.
+'''
+from __future__ import annotations
+
+import math
+from typing import Callable
+
+import numpy as np
+import torch
+
+from tentorch_gb300.linalg import inner_device, norm
+from tentorch_gb300.tensor import Tensor
+
+
+def lanczos(action: Callable[[Tensor], Tensor], start: Tensor, n_iter: int = 5,
+            tol: float = 1e-12) -> tuple[float, Tensor]:
+    '''
+    The lowest eigenpair of a Hermitian action, by Lanczos with full reorthogonalisation (twice).
+
+    Args:
+      action: v -> H v on tensors with the legs of `start`.
+      start: the starting vector, any normalisation.
+      n_iter: the number of Krylov steps.
+      tol: the norm below which a step ends the Krylov space.
+    Returns:
+      The lowest Ritz value and its Ritz vector, normalised.
+    Raises:
+      ValueError: when `n_iter` is below one or `start` has zero norm.
+    '''
+    if n_iter < 1:
+        raise ValueError(f'Lanczos needs at least one step, not {n_iter}.')
+    scale = norm(start)
+    if scale == 0.0:
+        raise ValueError('Lanczos needs a starting vector of non-zero norm.')
+    space = start._space
+    data = start.data
+    basis = torch.empty((n_iter + 1, data.numel()), dtype = data.dtype, device = data.device)
+    basis[0] = data * (1.0 / scale)
+    alphas, betas = [], []
+    for step in range(n_iter):
+        vector = Tensor._wrap(space, basis[step])
+        image = action(vector).data
+        alpha = torch.vdot(basis[step], image).real
+        alphas.append(alpha)
+        image = image - basis[step] * alpha
+        if step > 0:
+            image = image - basis[step - 1] * betas[-1]
+        # full reorthogonalisation, twice, against every vector so far
+        used = basis[:step + 1]
+        for _ in range(2):
+            coefficients = torch.mv(used.conj(), image)
+            image = image - torch.mv(used.transpose(0, 1), coefficients)
+        beta = torch.linalg.vector_norm(image)
+        betas.append(beta)
+        # a beta below tol ends the space on the host afterwards; dividing by it here only fills a
+        # row that is then discarded
+        basis[step + 1] = image / torch.clamp(beta, min = 1e-300)
+    host_alpha = torch.stack(alphas).cpu().numpy().astype(np.float64)
+    host_beta = torch.stack(betas).cpu().numpy().astype(np.float64)
+    size = n_iter
+    for step in range(n_iter):
+        if host_beta[step] < tol:
+            size = step + 1
+            break
+    matrix = np.diag(host_alpha[:size])
+    for step in range(size - 1):
+        matrix[step, step + 1] = matrix[step + 1, step] = host_beta[step]
+    values, vectors = np.linalg.eigh(matrix)
+    coefficients = torch.as_tensor(vectors[:, 0], dtype = data.dtype, device = data.device)
+    result = torch.mv(basis[:size].transpose(0, 1), coefficients)
+    result = result / torch.linalg.vector_norm(result)
+    return float(values[0]), Tensor._wrap(space, result.contiguous())

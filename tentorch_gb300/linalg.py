@@ -29,13 +29,16 @@ from tentorch_gb300.tensor import BlockKey, Space, Tensor
 
 _DTYPE = {torch.float64: 0, torch.complex128: 1}
 _precision = 0
+PER_BLOCK = -1  # the plain per-block FP64 form: one cuBLAS call per block pair
 
 
 def set_precision(slices: int) -> None:
-    '''0: FP64 block products; k in 1..8: split products with k bf16 slices per operand.'''
+    '''0: FP64 block products in the grouped kernels; k in 1..8: split products with k bf16 slices
+    per operand; PER_BLOCK (-1): the plain per-block FP64 form, one cuBLAS call per block pair, as
+    the reference issues its block products on a CUDA device (tentorch/linalg/graded/contract.cpp:148-163).'''
     global _precision
-    if not 0 <= int(slices) <= 8:
-        raise ValueError(f'precision is 0 (FP64) or 1..8 slices, not {slices}')
+    if not PER_BLOCK <= int(slices) <= 8:
+        raise ValueError(f'precision is 0 (FP64), 1..8 slices or -1 (per-block FP64), not {slices}')
     _precision = int(slices)
 
 

@@ -1,0 +1,119 @@
+'''The callers of the contraction path on the GPU against the reference: the Lanczos solver and the
+two-site DMRG of the Heisenberg chain, in the reference's float64 harness (float64 MPS blocks drawn
+N(0, 1) in block-key order from `torch.Generator().manual_seed(seed)`, float64 MPO and identities).
+Every sweep energy of the reference (L = 4, 6, 8 with bond 64; L = 16 with bond 32) is met within
+1e-10, the bond dimensions exactly, and the final energies within 1e-10 of exact diagonalisation
+where the bond is not truncating; the split-precision matvec (8 bf16 slices) gives the same
+energies within 1e-10.'''
+import numpy as np
+import pytest
+import torch
+
+import tentorch_gb300 as tg
+from tentorch_gb300 import networks as nw
+from tentorch_gb300.lanczos import lanczos
+from golden_io import load_json
+
+pytestmark = pytest.mark.gpu
+ENERGY_TOL = 1e-10
+
+
+def _driver(length, bond, seed = 0, precision = 0, n_iter = 5):
+    return nw.DMRG(nw.Model(length, cat = tg.u1), max_bond_dim = bond, n_iter = n_iter, seed = seed,
+                   dtype = torch.float64, device = 'cuda', generator = torch.Generator().manual_seed(seed),
+                   precision = precision)
+
+
+@pytest.mark.parametrize('length', [4, 6, 8])
+def test_small_chains_match_the_reference_and_exact_diagonalisation(length):
+    golden = load_json('dmrg.json')
+    want = golden['small'][str(length)]
+    driver = _driver(length, 64)
+    energies = [driver.sweep()[0] for _ in range(4)]
+    assert np.max(np.abs(np.array(energies) - np.array(want['sweeps']))) < ENERGY_TOL, energies
+    final = driver.energy()
+    assert abs(final.real - want['energy']) < ENERGY_TOL
+    assert abs(final.imag) < 1e-12
+    assert abs(final.real - golden['exact'][str(length)]) < ENERGY_TOL
+
+
+def _config1(precision):
+    golden = load_json('dmrg.json')['config1']
+    driver = _driver(golden['length'], golden['max_bond_dim'], golden['seed'], precision, golden['n_iter'])
+    out = []
+    for want in golden['sweeps']:
+        energy, lost = driver.sweep()
+        out.append((energy, lost, driver.state.bond_dims, want))
+    return out, golden
+
+
+def test_sixteen_sites_bond_32_matches_the_reference_sweep_by_sweep():
+    sweeps, golden = _config1(0)
+    for energy, lost, bonds, want in sweeps:
+        assert abs(energy - want['energy']) < ENERGY_TOL, (energy, want['energy'])
+        assert bonds == want['bond']
+        assert abs(lost - want['discarded']) < 1e-12
+    assert sweeps[-1][0] - golden['exact'] < 1e-8
+
+
+def test_split_precision_sweeps_keep_the_fp64_energies():
+    sweeps, _ = _config1(8)
+    for energy, lost, bonds, want in sweeps:
+        assert abs(energy - want['energy']) < ENERGY_TOL, (energy, want['energy'])
+        assert bonds == want['bond']
+
+
+def test_lanczos_finds_the_lowest_eigenvalue_of_a_dense_operator():
+    '''tentorch/linalg/lanczos.py:8-64 on a Hermitian action with a known spectrum: with as many
+    steps as the dimension the Krylov space is the whole space.'''
+    cat = tg.u1
+    leg = tg.Leg(cat, [(0,)], [6])
+    start = tg.Tensor(cat, [leg], [], (0,), dtype = torch.complex128, device = 'cuda')
+    gen = torch.Generator().manual_seed(3)
+    start.data.copy_(torch.randn(start.data.shape, dtype = torch.complex128, generator = gen))
+    a = torch.randn(6, 6, dtype = torch.complex128, generator = gen)
+    h = (a + a.conj().T).cuda()
+
+    def action(v):
+        return tg.Tensor._wrap(v._space, h @ v.data)
+    energy, vector = lanczos(action, start, 6)
+    exact = torch.linalg.eigvalsh(h)[0].item()
+    assert abs(energy - exact) < 1e-10
+    residual = h @ vector.data - energy * vector.data
+    assert torch.linalg.vector_norm(residual).item() < 1e-8
+    assert abs(tg.norm(vector) - 1.0) < 1e-12
+
+
+def test_lanczos_stops_when_the_krylov_space_closes():
+    '''A start inside a two-dimensional invariant subspace: the third beta is zero, the reference
+    stops there, and the eigenpair is that subspace's.'''
+    cat = tg.u1
+    leg = tg.Leg(cat, [(0,)], [4])
+    start = tg.Tensor(cat, [leg], [], (0,), dtype = torch.float64, device = 'cuda')
+    start.data.copy_(torch.tensor([1.0, 1.0, 0.0, 0.0], dtype = torch.float64))
+    h = torch.diag(torch.tensor([-2.0, 1.0, 5.0, 7.0], dtype = torch.float64)).cuda()
+
+    def action(v):
+        return tg.Tensor._wrap(v._space, h @ v.data)
+    energy, vector = lanczos(action, start, 4)
+    assert abs(energy + 2.0) < 1e-12
+    assert torch.allclose(vector.data.abs().cpu(), torch.tensor([1.0, 0.0, 0.0, 0.0], dtype = torch.float64),
+                          atol = 1e-12)
+
+
+def test_lanczos_argument_errors():
+    cat = tg.u1
+    leg = tg.Leg(cat, [(0,)], [2])
+    start = tg.Tensor(cat, [leg], [], (0,), dtype = torch.float64, device = 'cuda')
+    with pytest.raises(ValueError, match = 'at least one step'):
+        lanczos(lambda v: v, start, 0)
+    with pytest.raises(ValueError, match = 'non-zero norm'):
+        lanczos(lambda v: v, start, 3)
+
+
+def test_mps_expectation_of_the_heisenberg_chain_is_the_dmrg_energy():
+    driver = _driver(6, 64)
+    for _ in range(3):
+        driver.sweep()
+    value = driver.state.expectation(driver.operator)
+    assert abs(value.real - load_json('dmrg.json')['exact']['6']) < ENERGY_TOL

@@ -194,3 +194,107 @@ def test_every_golden_case_compiles_on_the_host():
             plan = tg.linalg.plan_of(case['spec'], *ts, outcharge = tuple(oc) if oc else None)
             assert plan.out_space.keys == [tg.BlockKey(*k) for k in
                                            sorted((tuple(k[0]), tuple(k[1]), k[2]) for k in case['output']['keys'])]
+
+
+def test_bending_a_leg_with_unpaired_dual_multiplets_is_an_error():
+    '''A bent leg's sector reads as its dual on the other side, so a sector and its dual must carry
+    the same multiplets (the reference's assumption, tentorch/linalg/graded/svd.cpp:97-100; it
+    writes past its blocks when the assumption fails).  The engine refuses the plan.'''
+    import torch
+    cat = tg.u1
+    bond = tg.Leg(cat, [(0,)], [3])
+    unpaired = tg.Leg(cat, [(-1,), (1,)], [2, 3])
+    w = tg.Leg(cat, [(0,), (2,), (-2,)], [3, 1, 1])
+    phys = tg.Leg(cat, [(1,), (-1,)], [1, 1])
+    T = lambda cod, dom: tg.Tensor(cat, cod, dom, (0,), dtype = torch.float64, device = 'cpu')
+    left, mps, site = T([bond, w], [bond]), T([bond, phys], [unpaired]), T([w, phys], [phys, w])
+    with pytest.raises(ValueError, match = 'same multiplets'):
+        tg.linalg.plan_of('EIa,Feq,aPb,IqPj->FJb', left, mps.conj(), mps, site)
+    paired = tg.Leg(cat, [(-1,), (1,)], [3, 3])
+    mps = T([bond, phys], [paired])
+    tg.linalg.plan_of('EIa,Feq,aPb,IqPj->FJb', left, mps.conj(), mps, site)
+
+
+def _composed_chain_index(space, above, below):
+    '''The gather index of a place composed from the per-step plans of its chain (tt_chain and
+    tt_step_plan, which match the reference's plans bit for bit): after[i] = before[index[i]].'''
+    a, na = _lib.ints32(above)
+    b, nb = _lib.ints32(below)
+    steps, n = (ctypes.c_int32 * 3 * 256)(), ctypes.c_int32()
+    _lib.check(_lib.lib.tt_chain(space.id, na, a, nb, b, 256, ctypes.cast(steps, ctypes.POINTER(ctypes.c_int32)),
+                                 ctypes.byref(n)))
+    flat = ctypes.cast(steps, ctypes.POINTER(ctypes.c_int32))
+    current = np.arange(space.size, dtype = np.int64)
+    before = space
+    for i in range(n.value):
+        kind, arm, after_id = flat[3 * i], flat[3 * i + 1], flat[3 * i + 2]
+        after = Space._load(space.cat, after_id)
+        back = np.full(after.size, -1, dtype = np.int64)
+        for key, offset in zip(before.keys, before.offsets):
+            for _, to, _, _, pieces in step_plan(before.id, kind, arm, (key[0], key[1], key[2])):
+                ot = after.offsets[after.index[tg.BlockKey(to[0:1], to[1:2], to[2])]]
+                for first, last, from_step, to_step, run, re_, im_ in pieces:
+                    assert (re_, im_) == (1.0, 0.0)
+                    for k in range(int(run)):
+                        slot = ot + int(last) + k * int(to_step)
+                        assert back[slot] < 0
+                        back[slot] = offset + int(first) + k * int(from_step)
+        current = np.where(back >= 0, current[np.maximum(back, 0)], -1)
+        before = after
+    return current
+
+
+def _compiled_gather(space, above, below):
+    from tentorch_gb300 import linalg as la
+    a, na = _lib.ints32(above)
+    b, nb = _lib.ints32(below)
+    plan = la._plan(('place', space.id, tuple(above), tuple(below)),
+                    lambda out: _lib.lib.tt_plan_place(space.id, na, a, nb, b, out), space.cat)
+    text = ctypes.create_string_buffer(1 << 16)
+    length = ctypes.c_int64()
+    _lib.check(_lib.lib.tt_plan_describe(plan.handle, len(text), text, ctypes.byref(length)))
+    gathers = [int(m.group(1)) for m in re.finditer(r'op (\d+) gather', text.value.decode())]
+    if not gathers:
+        return None
+    assert len(gathers) == 1
+    count = ctypes.c_int64()
+    _lib.check(_lib.lib.tt_plan_gather(plan.handle, gathers[0], 0, None, ctypes.byref(count)))
+    index = (ctypes.c_int32 * max(count.value, 1))()
+    _lib.check(_lib.lib.tt_plan_gather(plan.handle, gathers[0], count.value, index, ctypes.byref(count)))
+    return np.array(index[:count.value], dtype = np.int64)
+
+
+def test_compiled_leg_moves_are_the_composed_step_plans():
+    '''For categories whose symbols are all 1 a place compiles to one gather, built in one pass over
+    the entries; it equals the composition of the chain's per-step plans, including legs that do
+    not hold the dual of a sector (their entries are dropped by the bends) and qtotal != 0.'''
+    rng = np.random.default_rng(5)
+    checked = 0
+    for cat, pool in ((tg.u1, [-3, -2, -1, 0, 1, 2, 3]), (tg.z_n(3), [0, 1, 2]), (tg.no_symmetry, [0])):
+        for trial in range(12):
+            nlegs = int(rng.integers(2, 5))
+            legs = []
+            for _ in range(nlegs):
+                sectors = sorted(rng.choice(pool, size = int(rng.integers(1, len(pool) + 1)), replace = False).tolist())
+                mult = {}
+                for s in sectors:
+                    d = (-s) % 3 if cat is not tg.u1 and cat is not tg.no_symmetry else -s
+                    mult[s] = mult.get(d, int(rng.integers(1, 4)))
+                legs.append(tg.Leg(cat, [(s,) for s in sectors], [mult[s] for s in sectors]))
+            height = int(rng.integers(0, nlegs + 1))
+            charges = sorted({s[0] for l in legs for s in l.sectors})
+            qtotal = (int(rng.choice(charges)) if cat is tg.u1 else 0,)
+            space = Space.of(cat, legs[:height], legs[height:], qtotal)
+            if space.size == 0:
+                continue
+            order = rng.permutation(nlegs).tolist()
+            cut = int(rng.integers(0, nlegs + 1))
+            above, below = order[:cut], order[cut:]
+            want = _composed_chain_index(space, above, below)
+            got = _compiled_gather(space, above, below)
+            if got is None:
+                assert np.array_equal(want, np.arange(space.size))
+                continue
+            assert np.array_equal(got, want), (cat.name, legs, height, above, below)
+            checked += 1
+    assert checked >= 20
