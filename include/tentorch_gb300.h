@@ -105,9 +105,10 @@ int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace
 /* A text listing of the plan's operations and GEMM block shapes (m, n, K per pair), for diagnosis;
  * writes at most cap-1 characters and a terminating zero, *length the full size. */
 int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length);
-/* The gather index of operation `op` when it is a gather (a composed chain of leg moves whose F and
- * R symbols are all 1): output entry i reads input entry index[i], -1 writes zero.  *count is the
- * number of entries; nothing is copied when cap < *count.  For checking compiled leg moves against
+/* The gather index of operation `op` when it is a gather or a tiles pass (a composed chain of leg
+ * moves whose F and R symbols are all 1; tiles are expanded entry by entry): output entry i reads
+ * input entry index[i], -1 writes zero.  *count is the number of entries; nothing is written when
+ * cap < *count.  For checking compiled leg moves against
  * the reference's per-step plans (tentorch/tensors/place.cpp:199-247). */
 int32_t tt_plan_gather(const tt_plan *plan, int32_t op, int64_t cap, int32_t *index, int64_t *count);
 /* Elements of operand `i`'s prepared arena, 0 when the operand needs no preparation. */
@@ -122,7 +123,7 @@ int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, c
                         const void *const *prepared, void *output, void *workspace, void *stream);
 /* The same, synchronously, recording a CUDA event pair around every operation on `stream`: per op
  * its device milliseconds (-1 when it did not run) and its kind (0 zero, 1 gather, 2 runs, 3 gemm,
- * 4 add, 5 copy).  For measurement; the caller's stream is synchronised before it returns. */
+ * 4 add, 5 copy, 6 tiles).  For measurement; the caller's stream is synchronised before it returns. */
 int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                               const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
                               float *op_ms, int32_t *op_kind);

@@ -350,10 +350,36 @@ extern "C"
       if (op < 0 || static_cast<size_t>(op) >= p.ops.size())
         throw ttg::OutOfRange("the plan has no operation " + std::to_string(op));
       const ttg::Op &o = p.ops[static_cast<size_t>(op)];
-      if (o.kind != ttg::OpKind::gather) throw ttg::InvalidArgument("operation " + std::to_string(op) + " is not a gather");
-      *count = o.count;
-      if (cap >= o.count && o.count > 0)
-        std::memcpy(index, p.gather_index.data() + o.begin, static_cast<size_t>(o.count) * sizeof(int32_t));
+      if (o.kind == ttg::OpKind::gather)
+      {
+        *count = o.count;
+        if (cap >= o.count && o.count > 0)
+          std::memcpy(index, p.gather_index.data() + o.begin, static_cast<size_t>(o.count) * sizeof(int32_t));
+        return;
+      }
+      if (o.kind != ttg::OpKind::tiles)
+        throw ttg::InvalidArgument("operation " + std::to_string(op) + " is neither a gather nor tiles");
+      // the index the tiles amount to, entry by entry
+      *count = o.elements;
+      if (cap < o.elements) return;
+      std::fill(index, index + o.elements, -1);
+      for (int64_t c = o.begin; c < o.begin + o.count; ++c)
+      {
+        const ttg::TileChunk &ch = p.tile_chunks[static_cast<size_t>(c)];
+        const ttg::Tile &t = p.tiles[static_cast<size_t>(ch.tile)];
+        if (t.in_base < 0) continue;  // a zero pad entry
+        for (int32_t r = ch.row0; r < ch.row0 + ch.nrows; ++r)
+          for (int32_t col = 0; col < t.cols; ++col)
+          {
+            int64_t in = t.in_base;
+            int32_t rest = r;
+            for (int32_t l = t.n_row - 1; l >= 0; --l) in += static_cast<int64_t>(rest % t.extent[l]) * t.stride[l], rest /= t.extent[l];
+            rest = col;
+            for (int32_t l = t.n_row + t.n_col - 1; l >= t.n_row; --l)
+              in += static_cast<int64_t>(rest % t.extent[l]) * t.stride[l], rest /= t.extent[l];
+            index[t.out_base + static_cast<int64_t>(r) * t.out_ld + col] = static_cast<int32_t>(in);
+          }
+      }
     });
   }
 
@@ -361,7 +387,7 @@ extern "C"
   {
     return guarded([&] {
       const ttg::Program &p = *plan->program;
-      static const char *kinds[] = {"zero", "gather", "runs", "gemm", "add", "copy"};
+      static const char *kinds[] = {"zero", "gather", "runs", "gemm", "add", "copy", "tiles"};
       std::string out;
       for (size_t i = 0; i < p.ops.size(); ++i)
       {

@@ -1011,11 +1011,10 @@ namespace ttg
   }
 
   // tentorch/tensors/place.cpp:41-107,199-247
-  std::vector<Step> chain(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
+  // tentorch/tensors/place.cpp:183-197: every leg named exactly once
+  void check_place(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
   {
-    const int32_t height = static_cast<int32_t>(space->codomain.size());
-    const int32_t depth = static_cast<int32_t>(space->domain.size());
-    const int32_t total = height + depth;
+    const int32_t total = space->nlegs();
     std::vector<bool> named(static_cast<size_t>(total), false);
     for (const std::vector<int32_t> *side : {&above, &below})
       for (const int32_t leg : *side)
@@ -1032,6 +1031,34 @@ namespace ttg
       while (named[static_cast<size_t>(left_out)]) ++left_out;
       throw InvalidArgument("the leg " + std::to_string(left_out) + " is named on neither side");
     }
+  }
+
+  Space placed_space(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
+  {
+    check_place(space, above, below);
+    const std::vector<Leg> legs = space->legs();
+    std::vector<Leg> cod, dom;
+    for (const int32_t l : above) cod.push_back(legs[static_cast<size_t>(l)]);
+    for (const int32_t l : below) dom.push_back(legs[static_cast<size_t>(l)]);
+    return make_space(space->cat, std::move(cod), std::move(dom), space->qtotal);
+  }
+
+  bool place_is_identity(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
+  {
+    const int32_t height = static_cast<int32_t>(space->codomain.size());
+    if (static_cast<int32_t>(above.size()) != height) return false;
+    for (int32_t i = 0; i < height; ++i)
+      if (above[static_cast<size_t>(i)] != i) return false;
+    for (size_t j = 0; j < below.size(); ++j)
+      if (below[j] != height + static_cast<int32_t>(j)) return false;
+    return true;
+  }
+
+  std::vector<Step> chain(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
+  {
+    const int32_t height = static_cast<int32_t>(space->codomain.size());
+    const int32_t depth = static_cast<int32_t>(space->domain.size());
+    check_place(space, above, below);
     std::vector<Step> steps;
     std::vector<Leg> cod = space->codomain, dom = space->domain;
     Space current = space;

@@ -264,6 +264,12 @@ namespace ttg
   };
   // The chain of tentorch/tensors/place.cpp:199-247: fold the domain tail up, bubble sort, fold down.
   std::vector<Step> chain(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below);
+  // Raise the reference's errors for a place that does not name every leg exactly once.
+  void check_place(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below);
+  // The space a place lands in (the chain's last space), without the spaces in between.
+  Space placed_space(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below);
+  // Whether a place (already checked) leaves every leg where it is: the chain has no step.
+  bool place_is_identity(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below);
   // The leading domain legs the chain leaves in place: the others are bent up first, and every leg
   // of below[kept:] is bent down last.
   int32_t chain_kept(int32_t height, int32_t depth, const std::vector<int32_t> &below);

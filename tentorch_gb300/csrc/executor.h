@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -13,13 +14,36 @@
 
 namespace ttg
 {
+  // Host tables gathered into one device allocation: each add() reserves a 256-byte aligned slot
+  // and records where its device address goes; commit() makes one cudaMalloc and one copy.
+  struct TableStaging
+  {
+    std::vector<char> host;
+    std::vector<std::pair<size_t, void **>> slots;
+
+    template <typename T>
+    void add(const std::vector<T> &table, void **device)
+    {
+      *device = nullptr;
+      if (table.empty()) return;
+      const size_t at = (host.size() + 255) / 256 * 256;
+      host.resize(at + table.size() * sizeof(T));
+      std::memcpy(host.data() + at, table.data(), table.size() * sizeof(T));
+      slots.emplace_back(at, device);
+    }
+    cudaError_t commit(void **base);
+  };
+
   // The descriptor tables of one program, uploaded on first execution (plan-compile time, never
-  // inside a timed or captured region once warmed up).
+  // inside a timed or captured region once warmed up), all in one device allocation.
   struct DeviceTables
   {
     std::mutex mutex;
     bool ready = false;
+    void *base = nullptr;
     int32_t *gather = nullptr;
+    Tile *tiles = nullptr;
+    TileChunk *tile_chunks = nullptr;
     Chunk *chunks = nullptr;
     Term *terms = nullptr;
     GemmBlock *blocks = nullptr;
@@ -67,7 +91,7 @@ namespace ttg
                               bool complex, void *scratch, cudaStream_t stream);
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream);
-  cudaError_t upload_gemm(const Program &p, DeviceTables &t);
+  void stage_gemm(const Program &p, DeviceTables &t, TableStaging &staging);
   // The plain per-block form (per_block.cu): one cuBLAS call per block pair.
   cudaError_t launch_gemm_per_block(const Program &p, const Op &op, const void *A, const void *B, void *C, bool complex,
                                     cudaStream_t stream);

@@ -158,7 +158,7 @@ namespace ttg
       SplitItem item;
       double work;
     };
-    std::vector<Sized> items;
+    std::vector<Sized> items, tile;
     for (int64_t bi = op.begin; bi < op.begin + op.count; ++bi)
     {
       const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(bi)];
@@ -166,7 +166,7 @@ namespace ttg
         for (int32_t n0 = 0; n0 < blk.n; n0 += kSplitTileN)
         {
           const double rows = std::min(kSplitTileM, blk.m - m0), cols = std::min(kSplitTileN, blk.n - n0);
-          std::vector<Sized> tile;
+          tile.clear();
           for (int32_t k = 0; k < blk.pair_count; ++k)
           {
             const int32_t pi = blk.pair_begin + k;
@@ -222,15 +222,22 @@ namespace ttg
     }
   } // namespace
 
-  int64_t gemm_scratch(const Program &p)
+  int64_t plan_gemms(Program &p)
   {
+    auto plans = std::make_shared<GemmPlans>();
+    plans->f64.resize(p.ops.size());
+    plans->split.resize(p.ops.size());
     int64_t need = 0;
-    for (const Op &op : p.ops)
+    for (size_t i = 0; i < p.ops.size(); ++i)
     {
+      const Op &op = p.ops[i];
       if (op.kind != OpKind::gemm) continue;
-      need = std::max(need, (f64_bytes(schedule_gemm(p, op, kF64TileM, kF64TileN)) + 7) / 8);
-      need = std::max(need, (split_bytes(schedule_split(p, op), kMaxSlices) + 7) / 8);
+      plans->f64[i] = schedule_gemm(p, op, kF64TileM, kF64TileN);
+      plans->split[i] = schedule_split(p, op);
+      need = std::max(need, (f64_bytes(plans->f64[i]) + 7) / 8);
+      need = std::max(need, (split_bytes(plans->split[i], kMaxSlices) + 7) / 8);
     }
+    p.gemm_plans = std::move(plans);
     return need;
   }
 
@@ -924,39 +931,26 @@ namespace ttg
     return e;
   }
 
-  namespace
-  {
-    template <typename T>
-    cudaError_t put(const std::vector<T> &host, void **dev)
-    {
-      *dev = nullptr;
-      if (host.empty()) return cudaSuccess;
-      cudaError_t e = cudaMalloc(dev, host.size() * sizeof(T));
-      if (e == cudaSuccess) e = cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
-      return e;
-    }
-  } // namespace
-
-  // The device copies of every GEMM op's schedules and slicing lines.
-  cudaError_t upload_gemm(const Program &p, DeviceTables &t)
+  // The device copies of every GEMM op's schedules and slicing lines, staged into the program's
+  // one table allocation.
+  void stage_gemm(const Program &p, DeviceTables &t, TableStaging &staging)
   {
     t.gemm.assign(p.ops.size(), {});
     t.split.assign(p.ops.size(), {});
+    if (!p.gemm_plans) return;
     for (size_t i = 0; i < p.ops.size(); ++i)
     {
-      const Op &op = p.ops[i];
-      if (op.kind != OpKind::gemm) continue;
-      cudaError_t e;
+      if (p.ops[i].kind != OpKind::gemm) continue;
       {
-        const GemmSchedule s = schedule_gemm(p, op, kF64TileM, kF64TileN);
+        const GemmSchedule &s = p.gemm_plans->f64[i];
         DeviceTables::GemmTables &dst = t.gemm[i];
         dst.n_items = static_cast<int64_t>(s.items.size());
         dst.n_reduces = static_cast<int64_t>(s.reduces.size());
         dst.slots = s.slots;
-        if ((e = put(s.items, reinterpret_cast<void **>(&dst.items))) != cudaSuccess) return e;
-        if ((e = put(s.reduces, reinterpret_cast<void **>(&dst.reduces))) != cudaSuccess) return e;
+        staging.add(s.items, reinterpret_cast<void **>(&dst.items));
+        staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
       }
-      const SplitSchedule s = schedule_split(p, op);
+      const SplitSchedule &s = p.gemm_plans->split[i];
       DeviceTables::SplitTables &dst = t.split[i];
       dst.n_items = static_cast<int64_t>(s.items.size());
       dst.n_reduces = static_cast<int64_t>(s.reduces.size());
@@ -966,12 +960,11 @@ namespace ttg
       dst.slice_b = s.slice_b;
       dst.exps = s.exps;
       dst.slots = s.slots;
-      if ((e = put(s.items, &dst.items)) != cudaSuccess) return e;
-      if ((e = put(s.reduces, reinterpret_cast<void **>(&dst.reduces))) != cudaSuccess) return e;
-      if ((e = put(s.pairs, &dst.pairs)) != cudaSuccess) return e;
-      if ((e = put(s.lines, &dst.lines)) != cudaSuccess) return e;
+      staging.add(s.items, &dst.items);
+      staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
+      staging.add(s.pairs, &dst.pairs);
+      staging.add(s.lines, &dst.lines);
     }
-    return cudaSuccess;
   }
 
 } // namespace ttg

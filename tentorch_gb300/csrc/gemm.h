@@ -83,7 +83,15 @@ namespace ttg
 
   // Scratch doubles a program's GEMM ops need at most (FP64 partials, or slices + exponents +
   // partials for split precision), laid out per op from offset 0.
-  int64_t gemm_scratch(const Program &p);
+  // Per op of a program (empty for the ops that are not GEMMs): the FP64 and the split schedules.
+  struct GemmPlans
+  {
+    std::vector<GemmSchedule> f64;
+    std::vector<SplitSchedule> split;
+  };
+  // Schedule every GEMM op of the program into p.gemm_plans and return the scratch elements the
+  // launches need (partial tiles, tickets, slices).
+  int64_t plan_gemms(Program &p);
 
   // The distinct left blocks (offset, rows, cols) and right blocks of one GEMM op.
   struct OperandBlock

@@ -103,6 +103,50 @@ namespace ttg
       }
     }
 
+    // One chunk of a tile per CTA: a warp per output row, the row's part of the input offset
+    // computed once by its warp and the columns' part per entry (mixed radix over the copies of
+    // the output domain legs, the last fastest).  Writes are coalesced along the columns.
+    template <typename T>
+    __global__ void __launch_bounds__(256) tiles_kernel(const T *__restrict__ src, T *__restrict__ dst,
+                                                        const Tile *__restrict__ tiles,
+                                                        const TileChunk *__restrict__ chunks)
+    {
+      const TileChunk ch = chunks[blockIdx.x];
+      const Tile &t = tiles[ch.tile];
+      if (t.in_base < 0)
+      {
+        // the zero pad entry of an odd block
+        if (threadIdx.x == 0) dst[t.out_base] = T{};
+        return;
+      }
+      const int32_t n_row = t.n_row, n_col = t.n_col, cols = t.cols;
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int32_t r = ch.row0 + warp; r < ch.row0 + ch.nrows; r += 8)
+      {
+        int64_t row_in = t.in_base;
+        int32_t rest = r;
+        for (int32_t l = n_row - 1; l >= 0; --l)
+        {
+          const int32_t e = t.extent[l];
+          row_in += static_cast<int64_t>(rest % e) * t.stride[l];
+          rest /= e;
+        }
+        T *out = dst + t.out_base + static_cast<int64_t>(r) * t.out_ld;
+        for (int32_t c = lane; c < cols; c += 32)
+        {
+          int64_t in = row_in;
+          int32_t rc = c;
+          for (int32_t l = n_row + n_col - 1; l >= n_row; --l)
+          {
+            const int32_t e = t.extent[l];
+            in += static_cast<int64_t>(rc % e) * t.stride[l];
+            rc /= e;
+          }
+          out[c] = src[in];
+        }
+      }
+    }
+
     int grid_for(int64_t n, int threads)
     {
       // enough CTAs to cover the arena, capped at 8 waves of the 152 SMs
@@ -119,41 +163,35 @@ namespace ttg
 
   DeviceTables::~DeviceTables()
   {
-    for (void *p : {static_cast<void *>(gather), static_cast<void *>(chunks), static_cast<void *>(terms),
-                    static_cast<void *>(blocks), static_cast<void *>(pairs)})
-      if (p) cudaFree(p);
-    for (GemmTables &g : gemm)
-      for (void *p : {static_cast<void *>(g.items), static_cast<void *>(g.reduces)})
-        if (p) cudaFree(p);
-    for (SplitTables &g : split)
-      for (void *p : {g.items, g.pairs, g.lines, static_cast<void *>(g.reduces)})
-        if (p) cudaFree(p);
+    if (base) cudaFree(base);
   }
 
-  namespace
+  cudaError_t TableStaging::commit(void **base)
   {
-    template <typename T>
-    cudaError_t upload(const std::vector<T> &host, T **dev)
-    {
-      *dev = nullptr;
-      if (host.empty()) return cudaSuccess;
-      cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dev), host.size() * sizeof(T));
-      if (e != cudaSuccess) return e;
-      return cudaMemcpy(*dev, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
-    }
-  } // namespace
+    *base = nullptr;
+    if (host.empty()) return cudaSuccess;
+    cudaError_t e = cudaMalloc(base, host.size());
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemcpy(*base, host.data(), host.size(), cudaMemcpyHostToDevice)) != cudaSuccess) return e;
+    for (const auto &[at, device] : slots) *device = static_cast<char *>(*base) + at;
+    return cudaSuccess;
+  }
 
   cudaError_t DeviceTables::ensure(const Program &p)
   {
     std::lock_guard<std::mutex> lock(mutex);
     if (ready) return cudaSuccess;
-    cudaError_t e;
-    if ((e = upload(p.gather_index, &gather)) != cudaSuccess) return e;
-    if ((e = upload(p.chunks, &chunks)) != cudaSuccess) return e;
-    if ((e = upload(p.terms, &terms)) != cudaSuccess) return e;
-    if ((e = upload(p.gemm_blocks, &blocks)) != cudaSuccess) return e;
-    if ((e = upload(p.gemm_pairs, &pairs)) != cudaSuccess) return e;
-    if ((e = upload_gemm(p, *this)) != cudaSuccess) return e;
+    TableStaging staging;
+    staging.add(p.gather_index, reinterpret_cast<void **>(&gather));
+    staging.add(p.tiles, reinterpret_cast<void **>(&tiles));
+    staging.add(p.tile_chunks, reinterpret_cast<void **>(&tile_chunks));
+    staging.add(p.chunks, reinterpret_cast<void **>(&chunks));
+    staging.add(p.terms, reinterpret_cast<void **>(&terms));
+    staging.add(p.gemm_blocks, reinterpret_cast<void **>(&blocks));
+    staging.add(p.gemm_pairs, reinterpret_cast<void **>(&pairs));
+    stage_gemm(p, *this, staging);
+    const cudaError_t e = staging.commit(&base);
+    if (e != cudaSuccess) return e;
     ready = true;
     return cudaSuccess;
   }
@@ -223,6 +261,18 @@ namespace ttg
           gather_kernel<double><<<grid_for(op.elements, 256), 256, 0, args.stream>>>(
             reinterpret_cast<const double *>(src), reinterpret_cast<double *>(dst), t.gather + op.begin, op.elements);
         e = check_launch();
+        break;
+      case OpKind::tiles:
+        if (op.count > 0)
+        {
+          if (args.complex)
+            tiles_kernel<double2><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
+              reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst), t.tiles, t.tile_chunks + op.begin);
+          else
+            tiles_kernel<double><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
+              reinterpret_cast<const double *>(src), reinterpret_cast<double *>(dst), t.tiles, t.tile_chunks + op.begin);
+          e = check_launch();
+        }
         break;
       case OpKind::runs:
         if (op.count > 0)

@@ -17,12 +17,21 @@ namespace ttg
   {
     // A value the program computes: an arena of `space`, read from `buffer` through an optional
     // pending gather (a composed chain of permutations not yet written out).
+    // The tiles of a pending relabelling move and how many output entries they cover (the rest,
+    // padding and dropped entries, is zero).
+    struct TileMap
+    {
+      std::vector<Tile> tiles;
+      int64_t covered = 0;
+    };
+
     struct Value
     {
       int32_t buffer = -1;
       Space space = nullptr;
       std::shared_ptr<std::vector<int32_t>> pending;
       int32_t phase = -1;  // operand whose prepare phase computes it, -1 for the core
+      std::shared_ptr<TileMap> tiled;  // a pending move as tiles (never together with `pending`)
     };
 
     class Builder
@@ -53,6 +62,25 @@ namespace ttg
       // Write a value out into a buffer of its own (or `into` when given).
       Value materialize(const Value &v, int32_t into = -1)
       {
+        if (v.tiled)
+        {
+          const int32_t dst = into >= 0 ? into : temp(v.space);
+          if (v.tiled->covered < v.space->size) emit(Op{OpKind::zero, -1, -1, dst, 0, 0, v.space->size, v.phase});
+          Op op{OpKind::tiles, v.buffer, -1, dst, static_cast<int64_t>(p_.tile_chunks.size()), 0, v.space->size, v.phase};
+          const int32_t first_tile = static_cast<int32_t>(p_.tiles.size());
+          for (size_t i = 0; i < v.tiled->tiles.size(); ++i)
+          {
+            const Tile &t = v.tiled->tiles[i];
+            const int32_t step = std::max<int32_t>(1, 2048 / std::max<int32_t>(1, t.cols));
+            for (int32_t r = 0; r < t.rows; r += step)
+              p_.tile_chunks.push_back(TileChunk{first_tile + static_cast<int32_t>(i), r, std::min(step, t.rows - r), 0});
+          }
+          p_.tiles.insert(p_.tiles.end(), v.tiled->tiles.begin(), v.tiled->tiles.end());
+          op.count = static_cast<int64_t>(p_.tile_chunks.size()) - op.begin;
+          p_.moved_elements += v.tiled->covered;
+          if (op.count > 0) emit(op);
+          return Value{dst, v.space, nullptr, v.phase};
+        }
         if (!v.pending)
         {
           if (into < 0 || into == v.buffer) return v;
@@ -77,17 +105,23 @@ namespace ttg
       // gather for categories whose symbols are all 1, and one RUNS pass per step otherwise.
       Value place(const Value &v, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
       {
-        const std::vector<Step> steps = chain(v.space, above, below);
-        if (steps.empty()) return v;
         const Category &cat = *v.space->cat;
         if (cat.trivial_symbols())
         {
-          std::vector<int32_t> back = relabel(v.space, above, below, steps.back().after);
+          // a relabelling needs the space it lands in, not the chain's spaces in between
+          const Space after = placed_space(v.space, above, below);
+          if (place_is_identity(v.space, above, below)) return v;
+          if (!v.pending && !v.tiled && v.space->nlegs() <= kTileLegs)
+            return Value{v.buffer, after, nullptr, v.phase,
+                         std::make_shared<TileMap>(relabel_tiles(v.space, above, below, after))};
+          if (v.tiled) return place(materialize(v), above, below);
+          std::vector<int32_t> back = relabel(v.space, above, below, after);
           if (v.pending)
             for (int32_t &b : back) b = b >= 0 ? (*v.pending)[static_cast<size_t>(b)] : -1;
-          return Value{v.buffer, steps.back().after,
-                       std::make_shared<std::vector<int32_t>>(std::move(back)), v.phase};
+          return Value{v.buffer, after, std::make_shared<std::vector<int32_t>>(std::move(back)), v.phase};
         }
+        const std::vector<Step> steps = chain(v.space, above, below);
+        if (steps.empty()) return v;
         Value at = materialize(v);
         for (const Step &step : steps)
         {
@@ -256,8 +290,18 @@ namespace ttg
       // bends every leg of below[kept:] down and every domain leg past `kept` up.  The result is
       // the composition of the per-step permutations, built in one pass over the entries instead
       // of one pass per step.
-      std::vector<int32_t> relabel(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below,
-                                   Space out)
+      // One piece of a relabelling move: an (input row tree, input column tree) part of an input
+      // block and the rectangle of an output block it lands in.  Strides and extents are per
+      // input leg; out_stride is within the output block (rows times its columns, or columns).
+      struct MovePiece
+      {
+        int64_t in_base, out_base, out_ld;
+        const std::vector<int64_t> *extent, *in_stride, *out_stride;
+      };
+
+      template <typename Fn>
+      int64_t walk_pieces(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below, Space out,
+                          Fn &&fn)
       {
         const Category &cat = *in->cat;
         if (out->size > std::numeric_limits<int32_t>::max() || in->size > std::numeric_limits<int32_t>::max())
@@ -308,13 +352,10 @@ namespace ttg
             for (size_t t = 0; t < lay.trees.size(); ++t) table->emplace(lay.trees[t].sectors, std::make_pair(root, lay.offsets[t]));
           }
         }
-        std::vector<int32_t> back(static_cast<size_t>(out->size), -1);
         std::vector<Sector> sec(static_cast<size_t>(n)), cod_out(above.size()), dom_out(below.size());
         std::vector<int64_t> extent(static_cast<size_t>(n)), in_stride(static_cast<size_t>(n)),
-          out_stride(static_cast<size_t>(n)), copy(static_cast<size_t>(n));
-        std::vector<int32_t> order(static_cast<size_t>(n));  // legs in output order, the last fastest
-        for (size_t i = 0; i < above.size(); ++i) order[i] = above[i];
-        for (size_t j = 0; j < below.size(); ++j) order[above.size() + j] = below[j];
+          out_stride(static_cast<size_t>(n));
+        int64_t covered = 0;
         for (const Block &blk : in->blocks)
         {
           const Layout &rl = layout_of(cat, in->codomain, blk.key.codomain);
@@ -350,43 +391,117 @@ namespace ttg
               run = 1;
               for (int32_t l = n - 1; l >= h; --l) in_stride[static_cast<size_t>(l)] = run, run *= extent[static_cast<size_t>(l)];
               run = ob.cols;
+              int64_t entries = 1;
               for (size_t i = above.size(); i-- > 0;)
                 out_stride[static_cast<size_t>(above[i])] = run, run *= extent[static_cast<size_t>(above[i])];
               run = 1;
               for (size_t j = below.size(); j-- > 0;)
                 out_stride[static_cast<size_t>(below[j])] = run, run *= extent[static_cast<size_t>(below[j])];
-              const int64_t in_base = blk.offset + rl.offsets[rt] * blk.cols + cl.offsets[ct];
-              const int64_t out_base = ob.offset + r->second.second * ob.cols + c->second.second;
-              // walk every copy tuple in output order, the last output leg innermost
-              std::fill(copy.begin(), copy.end(), 0);
-              int64_t src = in_base, dst = out_base;
-              const int32_t inner = order[static_cast<size_t>(n - 1)];
-              const int64_t inner_extent = n ? extent[static_cast<size_t>(inner)] : 1;
-              const int64_t inner_in = n ? in_stride[static_cast<size_t>(inner)] : 0;
-              const int64_t inner_out = n ? out_stride[static_cast<size_t>(inner)] : 0;
-              while (true)
-              {
-                for (int64_t k = 0; k < inner_extent; ++k)
-                  back[static_cast<size_t>(dst + k * inner_out)] = static_cast<int32_t>(src + k * inner_in);
-                int32_t at = n - 2;
-                for (; at >= 0; --at)
-                {
-                  const size_t l = static_cast<size_t>(order[static_cast<size_t>(at)]);
-                  if (++copy[l] < extent[l])
-                  {
-                    src += in_stride[l];
-                    dst += out_stride[l];
-                    break;
-                  }
-                  src -= (extent[l] - 1) * in_stride[l];
-                  dst -= (extent[l] - 1) * out_stride[l];
-                  copy[l] = 0;
-                }
-                if (at < 0) break;
-              }
+              for (int32_t l = 0; l < n; ++l) entries *= extent[static_cast<size_t>(l)];
+              covered += entries;
+              fn(MovePiece{blk.offset + rl.offsets[rt] * blk.cols + cl.offsets[ct],
+                       ob.offset + r->second.second * ob.cols + c->second.second, ob.cols, &extent, &in_stride,
+                       &out_stride});
             }
         }
+        return covered;
+      }
+
+      // The composed gather index of a whole chain of leg moves when every F and R symbol is 1:
+      // after[i] = before[index[i]], -1 for entries nothing writes.  Such a chain only relabels:
+      // the entry at sector s_l, copy c_l of every leg l lands at the same copies of the output
+      // legs, a leg that ends on the other side reading its sector as the dual (each bend reads
+      // the dual sector's rows, tentorch/tensors/regroup.cpp:260-417).  A bent leg that does not
+      // hold the dual of an entry's sector drops the entry, as the chain's bends do; the chain
+      // bends every leg of below[kept:] down and every domain leg past `kept` up.  The result is
+      // the composition of the per-step permutations, built in one pass over the entries instead
+      // of one pass per step.
+      std::vector<int32_t> relabel(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below,
+                                   Space out)
+      {
+        std::vector<int32_t> back(static_cast<size_t>(out->size), -1);
+        const int32_t n = in->nlegs();
+        std::vector<int32_t> order(static_cast<size_t>(n));  // legs in output order, the last fastest
+        for (size_t i = 0; i < above.size(); ++i) order[i] = above[i];
+        for (size_t j = 0; j < below.size(); ++j) order[above.size() + j] = below[j];
+        std::vector<int64_t> copy(static_cast<size_t>(n));
+        walk_pieces(in, above, below, out, [&](const MovePiece &piece)
+        {
+          const std::vector<int64_t> &extent = *piece.extent, &in_stride = *piece.in_stride,
+                                     &out_stride = *piece.out_stride;
+          // walk every copy tuple in output order, the last output leg innermost
+          std::fill(copy.begin(), copy.end(), 0);
+          int64_t src = piece.in_base, dst = piece.out_base;
+          const size_t inner = static_cast<size_t>(order[static_cast<size_t>(n - 1)]);
+          while (true)
+          {
+            for (int64_t k = 0; k < extent[inner]; ++k)
+              back[static_cast<size_t>(dst + k * out_stride[inner])] = static_cast<int32_t>(src + k * in_stride[inner]);
+            int32_t at = n - 2;
+            for (; at >= 0; --at)
+            {
+              const size_t l = static_cast<size_t>(order[static_cast<size_t>(at)]);
+              if (++copy[l] < extent[l])
+              {
+                src += in_stride[l];
+                dst += out_stride[l];
+                break;
+              }
+              src -= (extent[l] - 1) * in_stride[l];
+              dst -= (extent[l] - 1) * out_stride[l];
+              copy[l] = 0;
+            }
+            if (at < 0) break;
+          }
+        });
         return back;
+      }
+
+      // The same move as tiles: one per piece, its rows the copies of the output codomain legs and
+      // its columns those of the output domain legs.
+      TileMap relabel_tiles(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below, Space out)
+      {
+        TileMap map;
+        // the pad entry of every odd block is a tile of its own that writes zero (in_base -1), so
+        // that a move which drops nothing needs no zero pass
+        for (const Block &ob : out->blocks)
+          if ((ob.rows * ob.cols) & 1)
+          {
+            Tile t{};
+            t.in_base = -1;
+            t.out_base = ob.offset + ob.rows * ob.cols;
+            t.out_ld = 1;
+            t.rows = t.cols = 1;
+            map.tiles.push_back(t);
+            ++map.covered;
+          }
+        map.covered += walk_pieces(in, above, below, out, [&](const MovePiece &piece)
+        {
+          Tile t{};
+          t.in_base = piece.in_base;
+          t.out_base = piece.out_base;
+          t.out_ld = static_cast<int32_t>(piece.out_ld);
+          t.n_row = static_cast<int32_t>(above.size());
+          t.n_col = static_cast<int32_t>(below.size());
+          int64_t rows = 1, cols = 1;
+          int32_t at = 0;
+          for (const int32_t l : above)
+          {
+            t.extent[at] = static_cast<int32_t>((*piece.extent)[static_cast<size_t>(l)]);
+            t.stride[at++] = (*piece.in_stride)[static_cast<size_t>(l)];
+            rows *= (*piece.extent)[static_cast<size_t>(l)];
+          }
+          for (const int32_t l : below)
+          {
+            t.extent[at] = static_cast<int32_t>((*piece.extent)[static_cast<size_t>(l)]);
+            t.stride[at++] = (*piece.in_stride)[static_cast<size_t>(l)];
+            cols *= (*piece.extent)[static_cast<size_t>(l)];
+          }
+          t.rows = static_cast<int32_t>(rows);
+          t.cols = static_cast<int32_t>(cols);
+          map.tiles.push_back(t);
+        });
+        return map;
       }
 
       // One step with coefficients: the pieces of every block grouped by destination run.
@@ -517,6 +632,28 @@ namespace ttg
           for (int64_t i = op.begin; i < op.begin + op.count; ++i)
             require(p.gather_index[static_cast<size_t>(i)] < size_of(op.src), "gather source");
           break;
+        case OpKind::tiles:
+          for (int64_t c = op.begin; c < op.begin + op.count; ++c)
+          {
+            const TileChunk &ch = p.tile_chunks[static_cast<size_t>(c)];
+            require(ch.tile >= 0 && static_cast<size_t>(ch.tile) < p.tiles.size(), "tile");
+            const Tile &t = p.tiles[static_cast<size_t>(ch.tile)];
+            require(ch.row0 >= 0 && ch.nrows >= 1 && ch.row0 + ch.nrows <= t.rows, "tile rows");
+            require(t.n_row >= 0 && t.n_col >= 0 && t.n_row + t.n_col <= kTileLegs && t.cols >= 1, "tile legs");
+            require(t.out_base >= 0 && t.out_base + static_cast<int64_t>(t.rows - 1) * t.out_ld + t.cols <= dst,
+                    "tile destination");
+            int64_t last = t.in_base, rows = 1, cols = 1;
+            for (int32_t l = 0; l < t.n_row + t.n_col; ++l)
+            {
+              require(t.extent[l] >= 1 && t.stride[l] >= 0, "tile extent");
+              last += static_cast<int64_t>(t.extent[l] - 1) * t.stride[l];
+              (l < t.n_row ? rows : cols) *= t.extent[l];
+            }
+            require(rows == t.rows && cols == t.cols, "tile shape");
+            require((t.in_base == -1 && t.n_row == 0 && t.n_col == 0) || (t.in_base >= 0 && last < size_of(op.src)),
+                    "tile source");
+          }
+          break;
         case OpKind::runs:
           for (int64_t c = op.begin; c < op.begin + op.count; ++c)
           {
@@ -564,7 +701,7 @@ namespace ttg
       const int32_t out = b.output_buffer(p.output_space);
       // a result computed by the core (or a prepared value) writes straight into the output
       Value first = results.front();
-      if (first.pending)
+      if (first.pending || first.tiled)
         b.materialize(first, out);
       else if (p.buffers[static_cast<size_t>(first.buffer)].kind == BufferKind::temp && first.phase < 0 &&
                !p.ops.empty() && p.ops.back().dst == first.buffer && !read_by_any(p, first.buffer))
@@ -603,7 +740,7 @@ namespace ttg
       for (Op &op : p.ops)
         if (op.phase >= 0 && p.prepared[static_cast<size_t>(op.phase)] < 0) op.phase = -1;
       p.scratch_offset = p.workspace;
-      p.workspace += gemm_scratch(p);
+      p.workspace += plan_gemms(p);
       validate(p);
     }
 

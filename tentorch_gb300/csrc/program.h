@@ -1,8 +1,13 @@
 // The plan compiler: a place, a contraction or a whole einsum compiled once per shape into a
 // device program, a short list of operations over arenas with their descriptor tables.
 //
-//   GATHER   dst[i] = src[index[i]] (index -1 writes 0): a composed chain of leg moves whose every
-//            coefficient is 1 (abelian groups), one pass however many steps the chain has.
+//   TILES    a chain of leg moves whose every coefficient is 1 (abelian groups) as strided
+//            rectangles: each tile is one (row tree, column tree) piece of an input block landing
+//            as a rows x cols rectangle of an output block, its entries found from the copies of
+//            every leg by mixed-radix strides; one pass however many steps the chain has, and a
+//            descriptor per tile instead of an index per entry.
+//   GATHER   dst[i] = src[index[i]] (index -1 writes 0): the same, composed with an earlier move
+//            or for more legs than a tile describes.
 //   RUNS     dst[d + t*ds] (+)= sum_k c_k src[s_k + t*ss_k] over chunks of runs: one leg-move step
 //            (or a trace) with F/R coefficients, grouped by destination so the pass is atomic free.
 //   GEMM     C_blk = sum_pairs A_blk(m x k) B_blk(k x n) over all output blocks of a contraction in
@@ -34,6 +39,7 @@ namespace ttg
     gemm = 3,
     add = 4,
     copy = 5,
+    tiles = 6,
   };
 
   struct Op
@@ -61,6 +67,24 @@ namespace ttg
     double re, im;
   };
   constexpr int32_t kChunk = 128;
+
+  // One piece of a relabelling move: dst[out_base + r * out_ld + c] = src[in_base + sum over the
+  // legs of copy_l * stride_l] for r < rows, c < cols, where r runs over the copies of the n_row
+  // output codomain legs and c over those of the n_col output domain legs, the last leg of each
+  // side fastest (extent[0..n_row) then extent[n_row..n_row+n_col)).
+  constexpr int kTileLegs = 12;
+  struct Tile
+  {
+    int64_t in_base, out_base;
+    int32_t out_ld, rows, cols, n_row, n_col, pad;
+    int32_t extent[kTileLegs];
+    int64_t stride[kTileLegs];
+  };
+  // A launch unit: rows [row0, row0 + nrows) of one tile (about 2K entries).
+  struct TileChunk
+  {
+    int32_t tile, row0, nrows, pad;
+  };
 
   // One output block of a grouped GEMM and the block pairs summed into it.
   struct GemmBlock
@@ -108,6 +132,10 @@ namespace ttg
     std::vector<Term> terms;
     std::vector<GemmBlock> gemm_blocks;
     std::vector<GemmPair> gemm_pairs;
+    std::vector<Tile> tiles;
+    std::vector<TileChunk> tile_chunks;
+    // the work schedules of the GEMM ops (gemm.h), computed once with the program
+    std::shared_ptr<const struct GemmPlans> gemm_plans;
     // bookkeeping for the roofline: useful flops of the GEMMs, elements moved by recouplings
     double gemm_flops = 0;
     int64_t moved_elements = 0;
