@@ -43,9 +43,13 @@ def parse():
     p.add_argument('--steps', type = int, default = 1000)
     p.add_argument('--warmup', type = int, default = 10)
     p.add_argument('--impl', default = 'gb300', choices = ['gb300', 'reference'])
-    p.add_argument('--precision', type = int, default = 0, help = '0: FP64 block products; k: bf16 slices')
+    p.add_argument('--precision', type = int, default = 8,
+                   help = 'the headline form: k bf16 slices (1..8) or 0 for FP64 block products')
     p.add_argument('--chi', type = int, default = CHI)
     p.add_argument('--cpu-sample', type = int, default = 20, help = 'matvecs in the CPU baseline sample')
+    p.add_argument('--dmrg-length', type = int, default = 64, help = 'chain of the DMRG sweep timing (0: skip)')
+    p.add_argument('--dmrg-iter', type = int, default = 10, help = 'Lanczos steps per window in the DMRG timing')
+    p.add_argument('--dmrg-warm', type = int, default = 2, help = 'FP64 sweeps before the timed sweeps')
     return p.parse_args()
 
 
@@ -173,6 +177,71 @@ def ncu_traffic(kernel):
         return json.load(handle).get(kernel)
 
 
+KIND_NAMES = {0: 'memset', 1: 'gather_kernel', 2: 'runs_kernel', 3: None, 4: 'add_f64_kernel', 5: 'memcpy',
+              6: 'tiles_kernel'}
+
+
+def gemm_kernel_name(precision):
+    return {0: 'gemm_dmma_kernel', -1: 'cublas_dgemm'}.get(precision, 'gemm_split_kernel')
+
+
+def launches_of(kind, precision):
+    """Our kernel launches one op of this kind makes (a GEMM: the grouped kernel, plus the slicing
+    kernel in split precision; the per-block form's cuBLAS calls are not ours)."""
+    if kind == 3:
+        return {0: 1, -1: 0}.get(precision, 2)
+    return 1 if kind in (1, 2, 4, 6) else 0
+
+
+def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
+    """The two-site DMRG of the U(1) Heisenberg chain (tentorch/algorithms/dmrg.py) timed per sweep
+    in three forms from one FP64 state: `warm` FP64 sweeps grow the bond to chi, then each form
+    runs one sweep from a copy of that state, with the plan caches cleared first so that every
+    form compiles its plans inside its sweep.  Forms: split (grouped kernels, the Lanczos matvec in
+    split precision), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one cuBLAS
+    call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
+    around the sweep, the device synchronised on both sides."""
+    from tentorch_gb300 import networks as nw
+    from tentorch_gb300.linalg import PER_BLOCK, clear_plans
+    tg.set_precision(0)
+    driver = nw.DMRG(nw.Model(length, cat = tg.u1), max_bond_dim = chi, n_iter = n_iter, dtype = torch.float64,
+                     device = device, generator = torch.Generator().manual_seed(SEED), precision = 0)
+    start = time.perf_counter()
+    for _ in range(warm):
+        driver.sweep()
+    warm_s = time.perf_counter() - start
+    snapshot = ([t.clone() for t in driver.state.tensors], driver.state.center)
+    out = {}
+    for name, form in (('fp64_grouped', 0), ('split', precision), ('fp64_per_block', PER_BLOCK)):
+        driver.state.tensors = [t.clone() for t in snapshot[0]]
+        driver.state.center = snapshot[1]
+        driver.precision = form
+        tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
+        clear_plans()
+        mv0 = driver.matvecs
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        energy, lost = driver.sweep()
+        torch.cuda.synchronize(device)
+        elapsed = time.perf_counter() - t0
+        tg.set_precision(0)
+        # the energy of the state the sweep left, evaluated in FP64
+        check = driver.energy().real
+        out[name] = {'s_per_sweep': elapsed, 'energy': energy, 'energy_fp64_check': check,
+                     'discarded': lost, 'matvecs': driver.matvecs - mv0, 'max_bond': max(driver.state.bond_dims)}
+    tg.set_precision(0)
+    clear_plans()
+    ref = out['fp64_grouped']['energy']
+    for name in out:
+        out[name]['delta_e_vs_fp64_grouped'] = abs(out[name]['energy'] - ref)
+        out[name]['delta_e_vs_own_fp64_check'] = abs(out[name]['energy'] - out[name]['energy_fp64_check'])
+    return {'length': length, 'chi': chi, 'n_iter': n_iter, 'warm_fp64_sweeps': warm, 'warm_s': warm_s,
+            'forms': out,
+            'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
+            'speedup_split_vs_fp64_grouped': out['fp64_grouped']['s_per_sweep'] / out['split']['s_per_sweep'],
+            'start': f'{warm} FP64 sweeps from the seeded random MPS (N(0,1) float64 blocks in key order, seed {SEED})'}
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -180,6 +249,7 @@ def run_gpu(args, rank, world):
     import tentorch_gb300 as tg
     from oracle import engine as orc
     from tentorch_gb300 import _lib
+    from tentorch_gb300.linalg import PER_BLOCK
 
     local = int(os.environ.get('LOCAL_RANK', 0))
     torch.cuda.set_device(local)
@@ -219,15 +289,17 @@ def run_gpu(args, rank, world):
     def matvec(i):
         return tg.einsum(orc.MATVEC, head, tail, vectors[i % 4])
 
-    # correctness of this very workload before timing it: FP64 against the oracle on rank 0's inputs
+    # correctness of this very workload before timing it, in every form, against the oracle
     want = orc.einsum(orc.MATVEC, head_o, tail_o, theta_o)
-    with tg.precision(args.precision):
-        got = tg.einsum(orc.MATVEC, head, tail, product(theta_o))
     scale = max(np.abs(b).max() for b in want.blocks.values())
-    parity = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.blocks.items()) / scale
+    parity = {}
+    for name, form in (('split', args.precision), ('fp64_grouped', 0), ('fp64_per_block', PER_BLOCK)):
+        with tg.precision(form):
+            got = tg.einsum(orc.MATVEC, head, tail, product(theta_o))
+        parity[name] = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.blocks.items()) / scale
 
-    for precision in sorted({0, args.precision}):
-        tg.set_precision(precision)
+    for form in (args.precision, 0, PER_BLOCK):
+        tg.set_precision(form)
         for i in range(args.warmup):
             matvec(i)
     torch.cuda.synchronize(device)
@@ -252,51 +324,55 @@ def run_gpu(args, rank, world):
     ms_per_step = total_ms / args.steps
     value = world * args.steps / (total_ms / 1e3)
 
-    # plain FP64 on the same GPU, for the split-precision comparison
-    fp64_ms = ms_per_step
-    if args.precision != 0:
-        fp64_ms = sum(timed_loop(args.steps, 0, matvec)) / args.steps
+    # the other forms on the same GPU and the same inputs
+    form_ms = {'split': ms_per_step}
+    form_ms['fp64_grouped'] = ms_per_step if args.precision == 0 else sum(timed_loop(args.steps, 0, matvec)) / args.steps
+    form_ms['fp64_per_block'] = sum(timed_loop(args.steps, PER_BLOCK, matvec)) / args.steps
 
     # --- per-kernel durations inside the step (CUDA events on the launching stream) ----------
-    tg.set_precision(args.precision)
-    n_ops = plan.n_ops
-    op_ms = np.zeros(n_ops)
-    kinds = None
-    samples = min(args.steps, 200)
-    ws = torch.empty(max(plan.workspace, 1), dtype = torch.float64, device = device)
-    prepared = [tg.linalg._prepared_arena(plan, i, t, ws) for i, t in enumerate([head, tail, vectors[0]])]
-    for i in range(samples):
-        flush.zero_()
-        out = torch.empty(plan.out_space.size, dtype = torch.float64, device = device)
-        ms_arr, kind_arr = (_lib.ctypes.c_float * n_ops)(), (_lib.i32 * n_ops)()
-        _lib.check(_lib.lib.tt_plan_execute_timed(
-            plan.handle, 0, args.precision, _lib.pointers([head.data.data_ptr(), tail.data.data_ptr(), vectors[i % 4].data.data_ptr()]),
-            _lib.pointers([p.data_ptr() if p is not None else None for p in prepared]), out.data_ptr(), ws.data_ptr(),
-            stream.cuda_stream, n_ops, ms_arr, kind_arr))
-        op_ms += np.maximum(np.array(ms_arr[:n_ops]), 0.0)
-        kinds = list(kind_arr[:n_ops])
-    op_ms /= samples
-    names = {0: 'zero', 1: 'gather_kernel', 2: 'runs_kernel', 3: 'gemm_dmma_kernel' if args.precision == 0 else 'gemm_split_kernel',
-             4: 'add_f64_kernel', 5: 'copy'}
-    by_kind = {}
-    launches_per_step = 0
-    for ms, k in zip(op_ms, kinds):
-        if ms <= 0:
-            continue
-        by_kind[names[k]] = by_kind.get(names[k], 0.0) + ms
-        if k in (1, 2, 3, 4):
-            launches_per_step += 1 if k != 3 or args.precision == 0 else 3
-    dominant = max(by_kind, key = by_kind.get)
-    gemm_ms = by_kind.get(names[3], 0.0)
+    def op_profile(precision):
+        n_ops = plan.n_ops
+        op_ms = np.zeros(n_ops)
+        kinds = None
+        samples = min(args.steps, 200)
+        ws = torch.empty(max(plan.workspace, 1), dtype = torch.float64, device = device)
+        prepared = [tg.linalg._prepared_arena(plan, i, t, ws) for i, t in enumerate([head, tail, vectors[0]])]
+        for i in range(samples):
+            flush.zero_()
+            out = torch.empty(plan.out_space.size, dtype = torch.float64, device = device)
+            ms_arr, kind_arr = (_lib.ctypes.c_float * n_ops)(), (_lib.i32 * n_ops)()
+            _lib.check(_lib.lib.tt_plan_execute_timed(
+                plan.handle, 0, precision,
+                _lib.pointers([head.data.data_ptr(), tail.data.data_ptr(), vectors[i % 4].data.data_ptr()]),
+                _lib.pointers([p.data_ptr() if p is not None else None for p in prepared]), out.data_ptr(),
+                ws.data_ptr(), stream.cuda_stream, n_ops, ms_arr, kind_arr))
+            op_ms += np.maximum(np.array(ms_arr[:n_ops]), 0.0)
+            kinds = list(kind_arr[:n_ops])
+        op_ms /= samples
+        by_kind, launches = {}, 0
+        for ms, k in zip(op_ms, kinds):
+            if ms <= 0:
+                continue
+            name = KIND_NAMES[k] or gemm_kernel_name(precision)
+            by_kind[name] = by_kind.get(name, 0.0) + ms
+            launches += launches_of(k, precision)
+        return by_kind, launches
+
     peaks, peak_kind = measured_peaks()
+    by_kind, launches_per_step = op_profile(args.precision)
+    gemm_ms = by_kind.get(gemm_kernel_name(args.precision), 0.0)
+    fp64_kinds, _ = op_profile(0)
+    dmma_ms = fp64_kinds.get('gemm_dmma_kernel', 0.0)
+    fp64_peak = fp64_peak_tflops(torch, device)
+    fp64_achieved = plan.flops / (dmma_ms / 1e3) / 1e12 if dmma_ms > 0 else 0.0
+    roofline_fp64 = {'bound': 'fp64', 'achieved': fp64_achieved, 'peak': fp64_peak, 'unit': 'TFLOP/s',
+                     'frac': fp64_achieved / fp64_peak, 'traffic': ncu_traffic('gemm_dmma_kernel'),
+                     'kernel': 'gemm_dmma_kernel', 'kernel_ms': dmma_ms,
+                     'peak_source': 'cuBLAS DGEMM 4096^3 best of 3 measured in this run (MEASURED_PEAKS.json has no FP64)',
+                     'algorithmic': f'{plan.flops:.4g} FLOP per launch (sum of 2mkn over the block pairs of both stages)',
+                     'op_ms': {k: round(v, 6) for k, v in fp64_kinds.items()}}
     if args.precision == 0:
-        peak = fp64_peak_tflops(torch, device)
-        achieved = plan.flops / (gemm_ms / 1e3) / 1e12 if gemm_ms > 0 else 0.0
-        roofline = {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s', 'frac': achieved / peak,
-                    'traffic': ncu_traffic('gemm_dmma_kernel'), 'kernel': 'gemm_dmma_kernel',
-                    'peak_source': 'cuBLAS DGEMM 4096^3 best of 3 measured in this run (MEASURED_PEAKS.json has no FP64)',
-                    'algorithmic': f'{plan.flops:.4g} FLOP per launch (sum of 2mkn over the block pairs of both stages)',
-                    'kernel_ms': gemm_ms}
+        roofline = dict(roofline_fp64)
     else:
         slices = args.precision
         bf16_flops = plan.flops * slices * (slices + 1) / 2
@@ -307,7 +383,7 @@ def run_gpu(args, rank, world):
                     'peak_source': f'{peak_kind} bf16_tflops', 'kernel_ms': gemm_ms,
                     'algorithmic': f'{bf16_flops:.4g} bf16 FLOP per step ({slices}({slices}+1)/2 slice products)'}
     roofline['op_ms'] = {k: round(v, 6) for k, v in by_kind.items()}
-    roofline['dominant'] = dominant
+    roofline['dominant'] = max(by_kind, key = by_kind.get)
 
     # --- end to end through the public API with host buffers ---------------------------------
     host_in = [torch.empty(v.data.shape, dtype = torch.float64, pin_memory = True) for v in vectors]
@@ -321,6 +397,7 @@ def run_gpu(args, rank, world):
         out = tg.einsum(orc.MATVEC, head, tail, staging)
         host_out.copy_(out.data, non_blocking = True)
 
+    tg.set_precision(args.precision)
     for i in range(3):
         e2e_step(i)
     e2e_times = timed_loop(args.steps, args.precision, e2e_step)
@@ -328,7 +405,11 @@ def run_gpu(args, rank, world):
     h2d = host_in[0].numel() * 8
     d2h = host_out.numel() * 8
 
-    line = None
+    dmrg = None
+    if args.dmrg_length > 0 and rank == 0:
+        dmrg = dmrg_sweeps(tg, torch, device, args.precision, args.dmrg_length, args.chi, args.dmrg_iter,
+                           args.dmrg_warm)
+
     if rank == 0:
         cpu_value, cpu_elapsed, cpu_n = cpu_matvecs(args.chi, args.cpu_sample)
         line = {'metric': METRIC, 'value': value, 'unit': 'matvecs/s', 'n_gpus': world, 'steps': args.steps,
@@ -336,10 +417,14 @@ def run_gpu(args, rank, world):
                 'vs_baseline': None, 'dtype': 'f64' if args.precision == 0 else f'bf16x{args.precision}-split/f64',
                 'data': 'synthetic', 'config': config(args, args.precision),
                 'gflops': plan.flops / (ms_per_step / 1e3) / 1e9,
-                'fp64_matvecs_per_s': 1e3 / fp64_ms,
+                'matvecs_per_s': {name: 1e3 / ms for name, ms in form_ms.items()},
+                'speedup_vs_fp64_per_block': form_ms['fp64_per_block'] / ms_per_step,
+                'speedup_vs_fp64_grouped': form_ms['fp64_grouped'] / ms_per_step,
                 'wall_s_timed_region': wall,
                 'parity_vs_oracle': parity,
                 'roofline': roofline,
+                'roofline_fp64_grouped': roofline_fp64,
+                'dmrg': dmrg,
                 'cpu_baseline': {'value': cpu_value, 'unit': 'matvecs/s', 'cores': os.cpu_count(), 'kind': 'port',
                                  'sample': f'{cpu_n} matvecs at chi={args.chi} of the oracle port of tentorch einsum '
                                            f'(numpy; {cpu_elapsed:.1f} s)'},

@@ -99,6 +99,10 @@ int32_t tt_plan_contract(int32_t left, int32_t right, int32_t n, const int32_t *
 /* einsum(spec, *operands, outcharge=) (linalg/graded/einsum.cpp:444-605, bindings.cpp:347-361). */
 int32_t tt_plan_einsum(const char *spec, int32_t n, const int32_t *spaces, int32_t has_charge, int64_t charge,
                        tt_plan **out);
+/* Drop every cached plan and its device tables (plans are cached per shape and live until this
+ * call): every tt_plan pointer handed out before is invalid afterwards.  Synchronises the device
+ * while it frees the tables. */
+int32_t tt_plan_cache_clear(void);
 /* The output space, workspace elements, GEMM flops, recoupled elements and op count of a plan. */
 int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace, double *gemm_flops,
                      int64_t *moved_elements, int32_t *n_ops);
@@ -142,6 +146,33 @@ int32_t tt_step_plan(int32_t space, int32_t kind, int32_t arm, int64_t key_cod, 
 /* The chain of steps of a place: per step (kind, arm, space after). */
 int32_t tt_chain(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
                  int32_t cap, int32_t *steps, int32_t *n);
+
+/* ---- truncating splittings (tentorch/linalg/graded/svd.cpp:41-177) -------------------------- */
+
+/* Thin SVDs of `count` float64 blocks in one launch (one-sided Jacobi, a CTA per block, relative
+ * accuracy for every singular value; replaces the per-block at::linalg_svd of svd.cpp:57-62).
+ * `table` is a DEVICE array of 7 int64 per block: a_off, rows, cols, u_off, s_off, vh_off, ws_off
+ * (offsets in doubles).  Block i is rows x cols row-major at a + a_off; with k = min(rows, cols) it
+ * writes U (rows x k, row-major) at u + u_off, the k singular values in descending order at
+ * s + s_off and Vh (k x cols, row-major) at vh + vh_off.  A block whose W = (the block or its
+ * transpose, max(rows, cols) x k) and V (k x k) do not both fit in tt_svd_shared_doubles() doubles
+ * needs workspace at ws_off: k*k doubles when W alone fits, else max(rows, cols)*k + k*k.  k is at
+ * most 1024.  info[i] (device int32) receives the Jacobi sweeps block i took, -1 when it did not
+ * converge (then its factors are not to be used).  Asynchronous on `stream`. */
+int32_t tt_svd_blocks(int32_t count, const int64_t *table, const double *a, double *u, double *s, double *vh,
+                      double *workspace, int32_t *info, void *stream);
+/* The doubles of shared memory one block's W and V can use in tt_svd_blocks. */
+int32_t tt_svd_shared_doubles(int64_t *doubles);
+/* Write the kept part of the factors of tt_svd_blocks into the two tensors of a split, one CTA per
+ * kept block.  `table` is a DEVICE array of 10 int64 per block: u_off, s_off, vh_off (packed
+ * factors), first_off, second_off (the blocks of the two output arenas), values_off (the kept
+ * values' place in the bond array), then rows, cols, k, kept, first_ld, column, row, absorb as
+ * int32 pairs packed into 4 int64 (rows | cols << 32, k | kept << 32, first_ld | column << 32,
+ * row | absorb << 32).  first[:, column:column+kept] = U[:, :kept], second[row:row+kept, :] =
+ * Vh[:kept, :], values = s[:kept], with the values multiplied into U (absorb 1), Vh (2) or their
+ * square roots into both (3). */
+int32_t tt_svd_keep(int32_t count, const int64_t *table, const double *u, const double *s, const double *vh,
+                    double *first, double *second, double *values, void *stream);
 
 /* ---- Krylov arithmetic on arenas ----------------------------------------------------------- */
 

@@ -383,6 +383,14 @@ extern "C"
     });
   }
 
+  int32_t tt_plan_cache_clear(void)
+  {
+    return guarded([&] {
+      std::lock_guard<std::recursive_mutex> lock(registry_mutex);
+      plan_cache().clear();
+    });
+  }
+
   int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length)
   {
     return guarded([&] {
@@ -590,6 +598,30 @@ extern "C"
         steps[3 * i + 2] = ch[static_cast<size_t>(i)].after->id;
       }
     });
+  }
+
+  int32_t tt_svd_shared_doubles(int64_t *doubles)
+  {
+    return guarded([&] { *doubles = ttg::svd_shared_doubles(); });
+  }
+
+  int32_t tt_svd_blocks(int32_t count, const int64_t *table, const double *a, double *u, double *s, double *vh,
+                        double *workspace, int32_t *info, void *stream)
+  {
+    if (count < 0) return fail(TT_EINVAL, "a negative block count");
+    const cudaError_t e = ttg::svd_blocks(count, table, a, u, s, vh, workspace, info, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+
+  int32_t tt_svd_keep(int32_t count, const int64_t *table, const double *u, const double *s, const double *vh,
+                      double *first, double *second, double *values, void *stream)
+  {
+    if (count < 0) return fail(TT_EINVAL, "a negative block count");
+    const cudaError_t e =
+      ttg::svd_keep(count, table, u, s, vh, first, second, values, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
   }
 
   int32_t tt_dots(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *scratch,

@@ -99,6 +99,16 @@ namespace ttg
   // Record a failure for tt_last_error() and return its status code (capi.cpp).
   int32_t report(int32_t code, const std::string &message);
 
+  // Thin SVDs of float64 blocks in one launch (svd.cu): `table` is a device array of 7 int64 per
+  // block (a_off, rows, cols, u_off, s_off, vh_off, ws_off); info[i] = Jacobi sweeps, -1 when block
+  // i did not converge.  svd_keep writes the kept factors into the split's arenas (12 int64-sized
+  // fields per block, see svd.cu).
+  cudaError_t svd_blocks(int32_t count, const void *table, const double *a, double *u, double *s, double *vh,
+                         double *workspace, int32_t *info, cudaStream_t stream);
+  int64_t svd_shared_doubles();
+  cudaError_t svd_keep(int32_t count, const void *table, const double *u, const double *s, const double *vh,
+                       double *first, double *second, double *values, cudaStream_t stream);
+
   constexpr int kDotParts = 120;
   // out[2j], out[2j+1] = re, im of <a_j, b> for j < count; partial holds 2*kDotParts*count doubles.
   cudaError_t arena_dots(const double *const *dev_as, int32_t count, const double *b, int64_t n_doubles, bool complex,

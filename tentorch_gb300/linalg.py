@@ -90,6 +90,15 @@ _plans = {}
 _prepared = {}
 
 
+def clear_plans() -> None:
+    '''Forget every compiled plan, here and in the engine (their device tables are freed): the next
+    contraction of each shape compiles again.  For bounding memory over a long run whose shapes keep
+    changing, and for timing compilation.'''
+    _plans.clear()
+    _prepared.clear()
+    check(lib.tt_plan_cache_clear())
+
+
 def _plan(key, build, cat) -> Plan:
     plan = _plans.get(key)
     if plan is None:
@@ -131,6 +140,10 @@ def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws) -> Optional[to
     stream = torch.cuda.current_stream(data.device).cuda_stream
     check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
                               ws.data_ptr() if ws is not None else None, stream))
+    if len(_prepared) > 256:
+        # prepared arenas of operands that are gone
+        for stale in [k for k, held in _prepared.items() if held[0]() is None]:
+            del _prepared[stale]
     _prepared[key] = (weakref.ref(data), data._version, arena)
     return arena
 
@@ -261,8 +274,65 @@ def is_close(first: Tensor, second: Tensor, rtol: float = 1e-10, atol: float = 1
 # ---------------------------------------------------------------------------------------------
 
 
+_svd_shared = None
+
+
+def _shared_doubles() -> int:
+    global _svd_shared
+    if _svd_shared is None:
+        value = i64()
+        check(lib.tt_svd_shared_doubles(ctypes.byref(value)))
+        _svd_shared = value.value
+    return _svd_shared
+
+
+def _factor_blocks(arranged: Tensor):
+    """The thin SVD of every non-empty block.  float64 blocks on the GPU go through one launch of
+    the engine's Jacobi SVD (tt_svd_blocks), complex blocks, blocks beyond its size and the
+    per-block comparison form through at::linalg_svd one block at a time, as svd.cpp:57-62 does.
+    Returns [key, u, s, vh, kept, offset] per block (u, s, vh views of packed device arrays in the
+    first case) and the host copy of all singular values, block after block."""
+    space = arranged._space
+    present = [(i, key) for i, key in enumerate(arranged.keys()) if space.shapes[i][0] * space.shapes[i][1] > 0]
+    batched = (arranged.dtype == torch.float64 and arranged.device.type == 'cuda' and _precision != PER_BLOCK and
+               all(min(space.shapes[i]) <= 1024 for i, _ in present))
+    if not batched:
+        factors = []
+        for i, key in present:
+            u, sv, vh = torch.linalg.svd(arranged._view(i), full_matrices = False)
+            factors.append([key, u, sv, vh, 0, 0])
+        host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
+        return factors, host, None
+    shared = _shared_doubles()
+    table, shapes = [], []
+    u_at = s_at = vh_at = ws_at = 0
+    for i, key in present:
+        rows, cols = space.shapes[i]
+        k, length = min(rows, cols), max(rows, cols)
+        need = 0 if length * k + k * k <= shared else (k * k if length * k <= shared else length * k + k * k)
+        table += [space.offsets[i], rows, cols, u_at, s_at, vh_at, ws_at if need else -1]
+        shapes.append((key, rows, cols, k, u_at, s_at, vh_at))
+        u_at, s_at, vh_at, ws_at = u_at + rows * k, s_at + k, vh_at + k * cols, ws_at + (need + 31) // 32 * 32
+    device = arranged.device
+    dev_table = torch.tensor(table, dtype = torch.int64).to(device)
+    u = torch.empty(max(u_at, 1), dtype = torch.float64, device = device)
+    sv = torch.empty(max(s_at, 1), dtype = torch.float64, device = device)
+    vh = torch.empty(max(vh_at, 1), dtype = torch.float64, device = device)
+    ws = torch.empty(max(ws_at, 1), dtype = torch.float64, device = device)
+    info = torch.empty(max(len(present), 1), dtype = torch.int32, device = device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    check(lib.tt_svd_blocks(len(present), dev_table.data_ptr(), arranged._data.data_ptr(), u.data_ptr(), sv.data_ptr(),
+                            vh.data_ptr(), ws.data_ptr(), info.data_ptr(), stream))
+    host = sv[:s_at].cpu().tolist()
+    if present and int(info[:len(present)].min()) < 0:
+        raise RuntimeError('the Jacobi SVD of a block did not converge')
+    factors = [[key, (u_off, rows, k), (s_off, k), (vh_off, k, cols), 0, 0]
+               for key, rows, cols, k, u_off, s_off, vh_off in shapes]
+    return factors, host, (u, sv, vh)
+
+
 def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
-    '''tentorch/linalg/graded/svd.cpp:41-177: per-block SVD on the device, one host read of all the
+    '''tentorch/linalg/graded/svd.cpp:41-177: the SVD of every block, one host read of all the
     singular values, a global ranking, truncation, and the +-q pairing of the bond.'''
     if absorb not in (0, 1, 2, 3):
         raise ValueError(f'absorb has to be 0, 1, 2 or 3, got {absorb}')
@@ -270,17 +340,11 @@ def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
         raise ValueError(f'a bond needs at least one multiplet, got {max_bond}')
     arranged = tensor.place(left) if left is not None else tensor
     cat = arranged.cat
-    factors = []
-    for i, key in enumerate(arranged.keys()):
-        matrix = arranged._view(i)
-        if matrix.numel() == 0:
-            continue
-        u, s, vh = torch.linalg.svd(matrix, full_matrices = False)
-        factors.append([key, u, s, vh, 0, 0])
-    host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
+    factors, host, packed = _factor_blocks(arranged)
     candidates, at = [], 0
     for fi, f in enumerate(factors):
-        for index in range(f[2].numel()):
+        count = f[2][1] if packed is not None else f[2].numel()
+        for index in range(count):
             candidates.append((host[at], fi, index))
             at += 1
     candidates.sort(key = lambda c: -c[0])
@@ -325,6 +389,27 @@ def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
     first = Tensor(cat, arranged.codomain, [bond], arranged.qtotal, arranged.dtype, arranged.device)
     values = torch.zeros(bond.multiplets(), dtype = arranged.dtype, device = arranged.device)
     second = Tensor(cat, [bond], arranged.domain, cat.trivial(), arranged.dtype, arranged.device)
+    if packed is not None:
+        # one launch writes every kept block of both factors and the values
+        u, sv, vh = packed
+        table, count = [], 0
+        for key, (u_off, rows, k), (s_off, _), (vh_off, _, cols), kept, offset in factors:
+            if kept == 0:
+                continue
+            fi = first._space.index[BlockKey(key.codomain, key.domain, key.copy)]
+            si = second._space.index[BlockKey(key.domain, key.domain, 0)]
+            first_ld = first._space.shapes[fi][1]
+            table += [u_off, s_off, vh_off, first._space.offsets[fi], second._space.offsets[si],
+                      placed[key.domain] + offset, rows | cols << 32, k | kept << 32, first_ld | offset << 32,
+                      offset | absorb << 32]
+            count += 1
+        if count:
+            device = arranged.device
+            dev_table = torch.tensor(table, dtype = torch.int64).to(device)
+            stream = torch.cuda.current_stream(device).cuda_stream
+            check(lib.tt_svd_keep(count, dev_table.data_ptr(), u.data_ptr(), sv.data_ptr(), vh.data_ptr(),
+                                  first._data.data_ptr(), second._data.data_ptr(), values.data_ptr(), stream))
+        return first, values, second
     for key, u, s, vh, kept, offset in factors:
         if kept == 0:
             continue

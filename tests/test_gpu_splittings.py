@@ -1,0 +1,117 @@
+'''The truncating splittings on the GPU (tentorch/linalg/graded/svd.cpp): the engine's batched Jacobi
+SVD against the per-block LAPACK-style SVD (at::linalg_svd, the reference's call) on the same
+blocks, the truncation, the +-q pairing and the absorbed values, and QR / RQ.  Singular values
+within 1e-13 relative, factors orthonormal within 1e-13, products within 1e-12.'''
+import numpy as np
+import pytest
+import torch
+
+import tentorch_gb300 as tg
+from tentorch_gb300 import linalg as la
+
+pytestmark = pytest.mark.gpu
+
+
+def _tensor(rows_by_charge, cols_by_charge, seed, scale = None):
+    '''A U(1) matrix-like tensor with one block per charge: codomain [a], domain [b].'''
+    cat = tg.u1
+    charges = sorted(rows_by_charge)
+    a = tg.Leg(cat, [(q,) for q in charges], [rows_by_charge[q] for q in charges])
+    b = tg.Leg(cat, [(q,) for q in charges], [cols_by_charge[q] for q in charges])
+    t = tg.Tensor(cat, [a], [b], (0,), dtype = torch.float64, device = 'cuda')
+    gen = torch.Generator().manual_seed(seed)
+    data = torch.randn(t.data.shape, dtype = torch.float64, generator = gen)
+    if scale is not None:
+        data = data * scale
+    t.data.copy_(data)
+    return t
+
+
+SHAPES = {-3: (1, 1), -2: (1, 5), -1: (5, 1), 0: (60, 90), 1: (90, 60), 2: (117, 117), 3: (130, 140), 4: (300, 200)}
+
+
+def _blocks(t):
+    return {k: v for k, v in t.to_tuple()[3].items()}
+
+
+def test_batched_svd_matches_per_block_svd():
+    t = _tensor({q: r for q, (r, c) in SHAPES.items()}, {q: c for q, (r, c) in SHAPES.items()}, seed = 1)
+    first, values, second = tg.svd(t)
+    with tg.precision(la.PER_BLOCK):
+        first_ref, values_ref, second_ref = tg.svd(t)
+    torch.cuda.synchronize()
+    assert torch.allclose(values, values_ref, rtol = 1e-13, atol = 0)
+    # the factors multiply back to the tensor and are orthonormal
+    product = tg.contract(first, second, [1], [0])
+    assert torch.max(torch.abs(product.data - t.data)).item() < 1e-12 * torch.max(torch.abs(t.data)).item()
+    for key, u in _blocks(first).items():
+        eye = torch.eye(u.shape[1], dtype = torch.float64, device = 'cuda')
+        assert torch.max(torch.abs(u.T @ u - eye)).item() < 1e-13
+    for key, vh in _blocks(second).items():
+        eye = torch.eye(vh.shape[0], dtype = torch.float64, device = 'cuda')
+        assert torch.max(torch.abs(vh @ vh.T - eye)).item() < 1e-13
+
+
+def test_a_spectrum_over_twelve_decades_agrees_with_lapack():
+    """Singular values from 1 down to 1e-12: the Jacobi values agree with LAPACK's on the same
+    block to 1e-14 absolute (both are accurate to a few ulps of the largest value)."""
+    cat = tg.u1
+    leg = tg.Leg(cat, [(0,)], [40])
+    t = tg.Tensor(cat, [leg], [leg], (0,), dtype = torch.float64, device = 'cuda')
+    gen = torch.Generator().manual_seed(3)
+    q1, _ = torch.linalg.qr(torch.randn(40, 40, dtype = torch.float64, generator = gen))
+    q2, _ = torch.linalg.qr(torch.randn(40, 40, dtype = torch.float64, generator = gen))
+    sigma = torch.logspace(0, -12, 40, dtype = torch.float64)
+    t.data[:1600].copy_((q1 @ torch.diag(sigma) @ q2.T).reshape(-1))
+    _, values, _ = tg.svd(t)
+    want = torch.linalg.svdvals(t.data[:1600].reshape(40, 40).cpu())
+    assert torch.max(torch.abs(values.cpu() - want)).item() < 1e-14
+    assert torch.max(torch.abs(values.cpu() - sigma)).item() < 1e-14
+
+
+@pytest.mark.parametrize('absorb', [0, 1, 2, 3])
+def test_truncating_split_matches_the_per_block_form(absorb):
+    rows = {-2: 20, 0: 40, 2: 20}
+    t = _tensor(rows, rows, seed = 2)
+    first, values, second = tg.svd(t, 30, 1e-14, absorb)
+    with tg.precision(la.PER_BLOCK):
+        first_ref, values_ref, second_ref = tg.svd(t, 30, 1e-14, absorb)
+    assert first.domain == first_ref.domain and second.codomain == second_ref.codomain
+    assert torch.allclose(values, values_ref, rtol = 1e-13, atol = 0)
+    # the kept factors agree up to the sign of each singular vector pair
+    product = tg.contract(first, second, [1], [0])
+    product_ref = tg.contract(first_ref, second_ref, [1], [0])
+    assert torch.max(torch.abs(product.data - product_ref.data)).item() < 1e-12
+
+
+def test_split_of_the_two_site_tensor_pairs_the_bond():
+    '''A two-site tensor [bond, phys] -> [phys, bond] with charge-symmetric bonds: the kept bond
+    carries as many multiplets in q as in -q (svd.cpp:97-117).'''
+    cat = tg.u1
+    bond = tg.Leg(cat, [(-2,), (0,), (2,)], [6, 9, 6])
+    phys = tg.Leg(cat, [(-1,), (1,)], [1, 1])
+    t = tg.Tensor(cat, [bond, phys], [phys, bond], (0,), dtype = torch.float64, device = 'cuda')
+    t.data.copy_(torch.randn(t.data.shape, dtype = torch.float64, generator = torch.Generator().manual_seed(4)))
+    first, values, second = tg.svd(t, 11, 1e-14, 2)
+    leg = first.domain[0]
+    mult = {leg.sector(b): leg.multiplicity(b) for b in range(leg.nblocks())}
+    for sector, count in mult.items():
+        assert mult.get((-sector[0],), count) == count
+    with tg.precision(la.PER_BLOCK):
+        first_ref, values_ref, second_ref = tg.svd(t, 11, 1e-14, 2)
+    assert first.domain == first_ref.domain
+    assert torch.allclose(values, values_ref, rtol = 1e-13, atol = 0)
+
+
+def test_qr_and_rq_factor_the_tensor():
+    rows = {-1: 7, 0: 12, 1: 5}
+    cols = {-1: 4, 0: 12, 1: 9}
+    t = _tensor(rows, cols, seed = 5)
+    q, r = tg.qr(t)
+    assert torch.max(torch.abs(tg.contract(q, r, [1], [0]).data - t.data)).item() < 1e-13
+    for u in _blocks(q).values():
+        assert torch.max(torch.abs(u.T @ u - torch.eye(u.shape[1], dtype = torch.float64, device = 'cuda'))).item() < 1e-13
+    l, qq = tg.rq(t)
+    assert torch.max(torch.abs(tg.contract(l, qq, [1], [0]).data - t.data)).item() < 1e-13
+    for v in _blocks(qq).values():
+        assert torch.max(torch.abs(v @ v.T - torch.eye(v.shape[0], dtype = torch.float64, device = 'cuda'))).item() < 1e-13
