@@ -336,7 +336,7 @@ def run_gpu(args, rank, world):
         kinds = None
         samples = min(args.steps, 200)
         ws = torch.empty(max(plan.workspace, 1), dtype = torch.float64, device = device)
-        prepared = [tg.linalg._prepared_arena(plan, i, t, ws) for i, t in enumerate([head, tail, vectors[0]])]
+        prepared = [tg.linalg._prepared_arena(plan, i, t, ws, stream.cuda_stream) for i, t in enumerate([head, tail, vectors[0]])]
         for i in range(samples):
             flush.zero_()
             out = torch.empty(plan.out_space.size, dtype = torch.float64, device = device)

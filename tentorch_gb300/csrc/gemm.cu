@@ -44,8 +44,10 @@ namespace ttg
   GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn)
   {
     GemmSchedule s;
-    // about two items per worker, never smaller than a tile over 64 of K
-    const double target = std::max(op_work(p, op) / (152.0 * kF64Workers * 2.0), static_cast<double>(bm) * bn * 64.0);
+    // The workers of one SM share its FP64 pipe, so what has to balance is the work per SM: items
+    // of about 1/8 of an SM's share (a matvec's stage has only ~10^5 multiply-adds per SM), never
+    // smaller than a tile over 32 of K (below that the partial tiles cost more than they save).
+    const double target = std::max(op_work(p, op) / (152.0 * 8.0), static_cast<double>(bm) * bn * 32.0);
     struct Sized
     {
       GemmItem item;

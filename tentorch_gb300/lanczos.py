@@ -3,21 +3,19 @@ The Lanczos eigensolver of the reference (tentorch/linalg/lanczos.py:8-64) over 
 block-sparse tensors, kept on the GPU.
 
 Every Krylov step runs on device-resident scalars: the projections alpha and the norms beta stay
-0-d device tensors, and the two full reorthogonalisation passes project against the whole basis at
-once (one matrix-vector product for the coefficients and one for the update, over the stacked
-arenas).  The host reads the tridiagonal matrix once, after the last step, and applies the
+0-d device tensors, and each projection runs against the whole basis at once (one matrix-vector
+product for the coefficients and one fused update over the stacked arenas).  The host reads the tridiagonal matrix once, after the last step, and applies the
 reference's early stop (a step whose beta falls below `tol` ends the space) to what it reads: the
 steps computed after such a stop are discarded, so the result is the reference's.
 '''
 from __future__ import annotations
 
-import math
 from typing import Callable
 
 import numpy as np
 import torch
 
-from tentorch_gb300.linalg import inner_device, norm
+from tentorch_gb300.linalg import norm
 from tentorch_gb300.tensor import Tensor
 
 
@@ -49,21 +47,24 @@ def lanczos(action: Callable[[Tensor], Tensor], start: Tensor, n_iter: int = 5,
     for step in range(n_iter):
         vector = Tensor._wrap(space, basis[step])
         image = action(vector).data
-        alpha = torch.vdot(basis[step], image).real
-        alphas.append(alpha)
-        image = image - basis[step] * alpha
-        if step > 0:
-            image = image - basis[step - 1] * betas[-1]
-        # full reorthogonalisation, twice, against every vector so far
         used = basis[:step + 1]
+        # The first projection against every vector so far holds alpha = <v_step, H v_step> as its
+        # last coefficient and removes alpha v_step and beta v_{step-1} (the three-term step of
+        # the reference) together with the round-off components along the older vectors; then
+        # the reference's two full reorthogonalisation passes.  Each pass is one product for the
+        # coefficients and one fused update (addmv), so a step launches a handful of kernels and
+        # never waits for the host.
+        coefficients = torch.mv(used.conj(), image)
+        alphas.append(coefficients[step].real)
+        image = torch.addmv(image, used.transpose(0, 1), coefficients, alpha = -1)
         for _ in range(2):
             coefficients = torch.mv(used.conj(), image)
-            image = image - torch.mv(used.transpose(0, 1), coefficients)
+            image = torch.addmv(image, used.transpose(0, 1), coefficients, alpha = -1)
         beta = torch.linalg.vector_norm(image)
         betas.append(beta)
         # a beta below tol ends the space on the host afterwards; dividing by it here only fills a
         # row that is then discarded
-        basis[step + 1] = image / torch.clamp(beta, min = 1e-300)
+        torch.div(image, torch.clamp(beta, min = 1e-300), out = basis[step + 1])
     host_alpha = torch.stack(alphas).cpu().numpy().astype(np.float64)
     host_beta = torch.stack(betas).cpu().numpy().astype(np.float64)
     size = n_iter

@@ -60,7 +60,8 @@ def precision(slices: int):
 class Plan:
     '''A compiled program: its output space, workspace and the size of each operand's prepared
     arena.'''
-    __slots__ = ('handle', 'cat', 'out_space', 'workspace', 'flops', 'moved', 'n_ops', 'prepared', '__weakref__')
+    __slots__ = ('handle', 'cat', 'out_space', 'workspace', 'flops', 'moved', 'n_ops', 'prepared', 'sizes',
+                 '__weakref__')
 
     def __init__(self, handle, cat):
         self.handle, self.cat = handle, cat
@@ -70,6 +71,7 @@ class Plan:
         self.out_space = Space._load(cat, space.value)
         self.workspace, self.flops, self.moved, self.n_ops = ws.value, flops.value, moved.value, ops.value
         self.prepared = []
+        self.sizes = {}
 
     def describe(self) -> str:
         '''The plan's operations and GEMM block shapes, as text.'''
@@ -80,14 +82,21 @@ class Plan:
         return buf.value.decode()
 
     def prepared_size(self, operand: int) -> int:
-        n = i64()
-        check(lib.tt_plan_prepared_size(self.handle, operand, ctypes.byref(n)))
-        return n.value
+        size = self.sizes.get(operand)
+        if size is None:
+            n = i64()
+            check(lib.tt_plan_prepared_size(self.handle, operand, ctypes.byref(n)))
+            size = self.sizes[operand] = n.value
+        return size
 
 
 _plans = {}
-# (plan handle, operand) -> (weakref to the operand arena, its version, the prepared arena)
+# (plan handle, operand) -> (weakref to the operand arena, its version, the prepared arena or None
+# when the operand has been seen once and not prepared yet)
 _prepared = {}
+# (device index, stream, dtype) -> a workspace arena that grows to the largest plan run on it; the
+# ops of one stream run in order, so consecutive plans share it
+_pools = {}
 
 
 def clear_plans() -> None:
@@ -96,6 +105,7 @@ def clear_plans() -> None:
     changing, and for timing compilation.'''
     _plans.clear()
     _prepared.clear()
+    _pools.clear()
     check(lib.tt_plan_cache_clear())
 
 
@@ -121,13 +131,20 @@ def _check_device(tensors) -> None:
                            '(move them with .to("cuda"))')
 
 
-def _workspace(plan: Plan, tensors) -> Optional[torch.Tensor]:
+def _workspace(plan: Plan, device, dtype, stream) -> Optional[torch.Tensor]:
     if plan.workspace <= 0:
         return None
-    return torch.empty(plan.workspace, dtype = tensors[0].dtype, device = tensors[0].device)
+    key = (device.index, stream, dtype)
+    pool = _pools.get(key)
+    if pool is None or pool.numel() < plan.workspace:
+        pool = _pools[key] = torch.empty(max(plan.workspace, 1 << 16), dtype = dtype, device = device)
+    return pool
 
 
-def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws) -> Optional[torch.Tensor]:
+def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws, stream) -> Optional[torch.Tensor]:
+    """The operand's prepared arena when the same arena (same version) comes back to this plan: the
+    first sighting runs the operand's phase inside the plan and only remembers the arena; the
+    second prepares it once for every call after (the head and tail of a Lanczos window)."""
     size = plan.prepared_size(operand)
     if size <= 0:
         return None
@@ -135,30 +152,33 @@ def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws) -> Optional[to
     held = _prepared.get(key)
     data = tensor._data
     if held is not None and held[0]() is data and held[1] == data._version:
-        return held[2]
-    arena = torch.empty(size, dtype = data.dtype, device = data.device)
-    stream = torch.cuda.current_stream(data.device).cuda_stream
-    check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
-                              ws.data_ptr() if ws is not None else None, stream))
+        if held[2] is not None:
+            return held[2]
+        arena = torch.empty(size, dtype = data.dtype, device = data.device)
+        check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
+                                  ws.data_ptr() if ws is not None else None, stream))
+        _prepared[key] = (held[0], held[1], arena)
+        return arena
     if len(_prepared) > 256:
-        # prepared arenas of operands that are gone
-        for stale in [k for k, held in _prepared.items() if held[0]() is None]:
+        # operands that are gone
+        for stale in [k for k, entry in _prepared.items() if entry[0]() is None]:
             del _prepared[stale]
-    _prepared[key] = (weakref.ref(data), data._version, arena)
-    return arena
+    _prepared[key] = (weakref.ref(data), data._version, None)
+    return None
 
 
 def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool = True) -> Tensor:
-    '''Execute a plan on the operands' device and return the output tensor.'''
+    """Execute a plan on the operands' device and return the output tensor."""
     _check_device(tensors)
     data0 = tensors[0]._data
+    device = data0.device
     if out is None:
-        out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = data0.dtype, device = data0.device))
-    ws = _workspace(plan, tensors)
-    prepared = [(_prepared_arena(plan, i, t, ws) if reuse_prepared else None) for i, t in enumerate(tensors)]
+        out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = data0.dtype, device = device))
+    stream = torch.cuda.current_stream(device).cuda_stream
+    ws = _workspace(plan, device, data0.dtype, stream)
+    prepared = [(_prepared_arena(plan, i, t, ws, stream) if reuse_prepared else None) for i, t in enumerate(tensors)]
     inputs = pointers(t._data.data_ptr() for t in tensors)
     prep = pointers((p.data_ptr() if p is not None else None) for p in prepared)
-    stream = torch.cuda.current_stream(data0.device).cuda_stream
     check(lib.tt_plan_execute(plan.handle, _DTYPE[data0.dtype], _precision, inputs, prep, out._data.data_ptr(),
                               ws.data_ptr() if ws is not None else None, stream))
     return out
