@@ -600,9 +600,21 @@ extern "C"
     });
   }
 
-  int32_t tt_svd_shared_doubles(int64_t *doubles)
+  int32_t tt_svd_workspace(int32_t count, const int64_t *shapes, int64_t *offsets, int64_t *total)
   {
-    return guarded([&] { *doubles = ttg::svd_shared_doubles(); });
+    return guarded([&] {
+      if (count < 0) throw ttg::InvalidArgument("a negative block count");
+      int64_t at = 0;
+      for (int32_t i = 0; i < count; ++i)
+      {
+        if (shapes[2 * i] > 1024 && shapes[2 * i + 1] > 1024)
+          throw ttg::InvalidArgument("a block of the batched SVD has more than 1024 rows and columns");
+        const int64_t need = ttg::svd_workspace_doubles(shapes[2 * i], shapes[2 * i + 1]);
+        offsets[i] = need ? at : -1;
+        at += (need + 31) / 32 * 32;
+      }
+      *total = at;
+    });
   }
 
   int32_t tt_svd_blocks(int32_t count, const int64_t *table, const double *a, double *u, double *s, double *vh,

@@ -104,8 +104,9 @@ namespace ttg
   // i did not converge.  svd_keep writes the kept factors into the split's arenas (12 int64-sized
   // fields per block, see svd.cu).
   cudaError_t svd_blocks(int32_t count, const void *table, const double *a, double *u, double *s, double *vh,
-                         double *workspace, int32_t *info, cudaStream_t stream);
-  int64_t svd_shared_doubles();
+                         void *workspace, int32_t *info, cudaStream_t stream);
+  // doubles of global workspace one block needs (0 when its working set fits in shared memory)
+  int64_t svd_workspace_doubles(int64_t rows, int64_t cols);
   cudaError_t svd_keep(int32_t count, const void *table, const double *u, const double *s, const double *vh,
                        double *first, double *second, double *values, cudaStream_t stream);
 

@@ -3,19 +3,30 @@
 //
 // Method: one-sided Jacobi (Hestenes 1958; the rotation of Rutishauser as in Demmel & Veselic,
 // "Jacobi's method is more accurate than QR", SIAM J. Matrix Anal. Appl. 13 (1992)).  The columns
-// of W (the block, or its transpose when it is wider than tall, so that W has min(m, n) columns)
-// are rotated in pairs until every pair is orthogonal to working precision; then the column norms
-// are the singular values, the normalised columns one set of singular vectors and the accumulated
-// rotations V the other.  The method is accurate in the relative sense for every singular value,
-// and U and V come out orthonormal to round-off, which a truncating DMRG needs for the kept
-// vectors however small their values.
+// of W (the block, or its transpose when it is wider than tall, so that W has k = min(m, n)
+// columns) are rotated in pairs until every pair is orthogonal to working precision; then the
+// column norms are the singular values, the normalised columns one set of singular vectors and
+// the accumulated rotations V the other.  U and V come out orthonormal to round-off, which a
+// truncating DMRG needs for the kept vectors however small their values.
 //
-// One CTA of 1024 threads per block: each sweep runs the pairs in the round-robin (circle) order,
-// min(m, n) - 1 rounds of disjoint pairs, a warp per pair: three dot products over the column
-// length reduced with shuffles, the rotation, and the update of both columns of W and of V.  W and
-// V sit in shared memory when they fit (227 KB), else in a global workspace (L2 resident).  The
-// sweeps stop when a sweep rotates nothing, at most kMaxSweeps; a block that did not converge
-// reports -1 in `info` (the host raises).  The loops are all bounded: no waits.
+// FP64 on this GPU runs at about 1/64 of the FP32 rate, so the sweeps are mixed precision:
+//   1. FP32 sweeps on a scaled copy of the block until its columns are orthogonal to ~1e-5; they
+//      give a rotation V32 close to the right singular vectors.
+//   2. V = V32 in FP64, made orthonormal to FP64 precision by two Newton-Schulz steps
+//      V <- V (3 I - V^T V) / 2 (quadratic: 1e-7 -> 1e-14 -> round-off).
+//   3. W = A V in FP64 (columns already orthogonal to ~1e-6).
+//   4. FP64 sweeps on W with V accumulated: from a start that close, Jacobi's quadratic
+//      convergence needs two sweeps and a third that finds nothing to rotate.
+// In the FP64 sweeps only the dot product of the pair is taken (the squared column norms are
+// carried along with the exact update of a rotation and recomputed at each sweep's start), and the
+// angle is found in FP32 and then made exactly orthogonal in FP64 (c^2 + s^2 = 1 by two Newton
+// steps): an angle good to 1e-7 still shrinks the pair's cosine by that factor each rotation.
+//
+// One CTA of 1024 threads per block; each sweep runs the pairs in the round-robin (circle) order,
+// k - 1 rounds of disjoint pairs, a warp per pair.  Everything sits in shared memory when it fits
+// (227 KB), else in a global workspace (L2 resident).  At most kMaxSweeps sweeps per phase; a
+// block whose FP64 phase did not converge reports -1 in `info` (the host raises).  All loops are
+// bounded: no waits.
 //
 // A second kernel writes the kept part of each block's factors into the two output arenas, with
 // the singular values absorbed as the caller asks, so that a whole truncating split is two
@@ -36,6 +47,8 @@ namespace ttg
     constexpr int kSvdThreads = 1024;
     constexpr int kMaxSweeps = 40;
     constexpr int kSvdSmemBytes = 227 * 1024;
+    constexpr int kStaticBytes = 12 * 1024;  // the ranks and values below
+    constexpr int64_t kDynamicBytes = kSvdSmemBytes - kStaticBytes - 1024;
 
     // per block: a_off, rows, cols, u_off, s_off, vh_off, ws_off (doubles; ws_off -1: no workspace)
     struct SvdEntry
@@ -43,63 +56,70 @@ namespace ttg
       int64_t a_off, rows, cols, u_off, s_off, vh_off, ws_off;
     };
 
-    __device__ __forceinline__ double warp_sum(double v)
+    // bytes of one block's working set: W (len x k) FP64, V and the Newton-Schulz product (k x k)
+    // FP64, W and V in FP32, the squared norms in FP64 and FP32
+    __host__ __device__ inline int64_t svd_bytes(int64_t len, int64_t k)
+    {
+      return (len * k + 2 * k * k + k) * 8 + (len * k + k * k + k) * 4 + 256;
+    }
+
+    template <typename T>
+    __device__ __forceinline__ T warp_sum(T v)
     {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
       return v;
     }
 
-    __global__ void __launch_bounds__(kSvdThreads, 1)
-      jacobi_svd_kernel(const SvdEntry *__restrict__ table, const double *__restrict__ a, double *__restrict__ u,
-                        double *__restrict__ s, double *__restrict__ vh, double *__restrict__ workspace,
-                        int32_t *__restrict__ info, int64_t smem_doubles)
+    // The rotation that makes the pair (alpha = |w_p|^2, beta = |w_q|^2, gamma = w_p . w_q)
+    // orthogonal: w_p' = c w_p - s w_q, w_q' = s w_p + c w_q with t = s / c the smaller root of
+    // t^2 + 2 zeta t - 1 = 0, zeta = (beta - alpha) / (2 gamma).  Found in FP32 on values scaled
+    // by a power of two; false when gamma is negligible at that scale.
+    __device__ __forceinline__ bool angle_of(float a, float b, float g, float &c, float &s)
     {
-      extern __shared__ double shared[];
-      __shared__ int rotated;
-      __shared__ int rank_of[1024];
-      const SvdEntry e = table[blockIdx.x];
-      const int64_t m = e.rows, n = e.cols;
-      const bool wide = n > m;
-      const int64_t len = wide ? n : m, k = wide ? m : n;  // W is len x k, column-major
-      if (k == 0)
-      {
-        if (threadIdx.x == 0) info[blockIdx.x] = 0;
-        return;
-      }
-      double *w, *v;
-      if ((len * k + k * k) <= smem_doubles)
-      {
-        w = shared;
-        v = shared + len * k;
-      }
-      else if (len * k <= smem_doubles)
-      {
-        w = shared;
-        v = workspace + e.ws_off;
-      }
-      else
-      {
-        w = workspace + e.ws_off;
-        v = w + len * k;
-      }
-      const double *src = a + e.a_off;
-      // W: column j of the block (tall) or row j of the block (wide); V = identity
-      for (int64_t i = threadIdx.x; i < len * k; i += blockDim.x)
-      {
-        const int64_t col = i / len, row = i % len;
-        w[i] = wide ? src[col * n + row] : src[row * n + col];
-      }
-      for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x) v[i] = (i / k == i % k) ? 1.0 : 0.0;
-      __syncthreads();
+      if (g == 0.0f) return false;
+      const float zeta = (b - a) / (2.0f * g);
+      const float t = fabsf(zeta) > 1e15f ? 0.5f / zeta : copysignf(1.0f, zeta) / (fabsf(zeta) + sqrtf(1.0f + zeta * zeta));
+      c = rsqrtf(1.0f + t * t);
+      s = c * t;
+      return true;
+    }
 
+    // FP32 columns are scaled to |entries| <= 1, so their squared norms neither overflow nor lose
+    // the angle; FP64 ones are brought to that scale by a power of two first
+    __device__ __forceinline__ bool angle(float alpha, float beta, float gamma, float &c, float &s)
+    {
+      return angle_of(alpha, beta, gamma, c, s);
+    }
+    __device__ __forceinline__ bool angle(double alpha, double beta, double gamma, float &c, float &s)
+    {
+      int ex;
+      frexp(fmax(alpha, beta), &ex);
+      return angle_of(static_cast<float>(ldexp(alpha, -ex)), static_cast<float>(ldexp(beta, -ex)),
+                      static_cast<float>(ldexp(gamma, -ex)), c, s);
+    }
+
+    // One Jacobi phase over W (len x k, column-major) with the rotations accumulated into V (k x k).
+    // FP32: everything in FP32.  FP64: the dot products, updates and norms in FP64, the angle in
+    // FP32 made exactly orthogonal.  Returns the sweeps taken, -1 when kMaxSweeps did not do.
+    template <typename T>
+    __device__ int jacobi_phase(T *w, T *v, T *norms, int64_t len, int64_t k, double tol, int *rotated)
+    {
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-      const double tolerance = 2.220446049250313e-16 * sqrt(static_cast<double>(len));
       const int64_t players = k + (k & 1);  // a dummy column pairs with the odd one out
-      int sweeps = -1;
+      const T tol2 = static_cast<T>(tol * tol);
       for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
       {
-        if (threadIdx.x == 0) rotated = 0;
+        // exact squared norms at the start of every sweep
+        for (int64_t j = warp; j < k; j += warps)
+        {
+          const T *wj = w + j * len;
+          T sum = 0;
+          for (int64_t i = lane; i < len; i += 32) sum = fma(wj[i], wj[i], sum);
+          sum = warp_sum(sum);
+          if (lane == 0) norms[j] = sum;
+        }
+        if (threadIdx.x == 0) *rotated = 0;
         __syncthreads();
         for (int64_t round = 0; round + 1 < players; ++round)
         {
@@ -124,57 +144,157 @@ namespace ttg
               p = lower;
             }
             if (q >= k) continue;  // the dummy
-            double *wp = w + p * len, *wq = w + q * len;
-            double alpha = 0, beta = 0, gamma = 0;
-            for (int64_t i = lane; i < len; i += 32)
-            {
-              const double x = wp[i], y = wq[i];
-              alpha = fma(x, x, alpha);
-              beta = fma(y, y, beta);
-              gamma = fma(x, y, gamma);
-            }
-            alpha = warp_sum(alpha);
-            beta = warp_sum(beta);
+            T *wp = w + p * len, *wq = w + q * len;
+            T gamma = 0;
+            for (int64_t i = lane; i < len; i += 32) gamma = fma(wp[i], wq[i], gamma);
             gamma = warp_sum(gamma);
-            // orthogonal to working precision: the cosine of the pair's angle below sqrt(len) eps
-            if (gamma == 0.0 || fabs(gamma) <= tolerance * sqrt(alpha) * sqrt(beta)) continue;
-            const double zeta = (beta - alpha) / (2.0 * gamma);
-            const double tan = copysign(1.0, zeta) / (fabs(zeta) + hypot(1.0, zeta));
-            const double cs = 1.0 / hypot(1.0, tan), sn = cs * tan;
+            const T alpha = norms[p], beta = norms[q];
+            // orthogonal to working precision: cos^2 of the pair's angle below tol^2
+            if (gamma * gamma <= tol2 * alpha * beta) continue;
+            float cf, sf;
+            if (!angle(alpha, beta, gamma, cf, sf)) continue;
+            T c = cf, s = sf;
+            if (sizeof(T) == 8)
+            {
+              // c^2 + s^2 = 1 to FP64 precision: two Newton steps on 1 / sqrt(c^2 + s^2)
+#pragma unroll
+              for (int it = 0; it < 2; ++it)
+              {
+                const T f = static_cast<T>(1.5) - static_cast<T>(0.5) * fma(c, c, s * s);
+                c *= f;
+                s *= f;
+              }
+            }
             for (int64_t i = lane; i < len; i += 32)
             {
-              const double x = wp[i], y = wq[i];
-              wp[i] = cs * x - sn * y;
-              wq[i] = sn * x + cs * y;
+              const T x = wp[i], y = wq[i];
+              wp[i] = fma(c, x, -s * y);
+              wq[i] = fma(s, x, c * y);
             }
-            double *vp = v + p * k, *vq = v + q * k;
+            T *vp = v + p * k, *vq = v + q * k;
             for (int64_t i = lane; i < k; i += 32)
             {
-              const double x = vp[i], y = vq[i];
-              vp[i] = cs * x - sn * y;
-              vq[i] = sn * x + cs * y;
+              const T x = vp[i], y = vq[i];
+              vp[i] = fma(c, x, -s * y);
+              vq[i] = fma(s, x, c * y);
             }
-            if (lane == 0) rotated = 1;
+            if (lane == 0)
+            {
+              const T cc = c * c, ss = s * s, cs2 = 2 * c * s * gamma;
+              norms[p] = cc * alpha - cs2 + ss * beta;
+              norms[q] = ss * alpha + cs2 + cc * beta;
+              *rotated = 1;
+            }
           }
           __syncthreads();
         }
-        const int any = rotated;
+        const int any = *rotated;
         __syncthreads();
-        if (!any)
-        {
-          sweeps = sweep + 1;
-          break;
-        }
+        if (!any) return sweep + 1;
       }
-      // singular values (column norms) into the shared tail of the ranks, then the ranks
+      return -1;
+    }
+
+    __global__ void __launch_bounds__(kSvdThreads, 1)
+      jacobi_svd_kernel(const SvdEntry *__restrict__ table, const double *__restrict__ a, double *__restrict__ u,
+                        double *__restrict__ s, double *__restrict__ vh, unsigned char *__restrict__ workspace,
+                        int32_t *__restrict__ info)
+    {
+      extern __shared__ __align__(16) unsigned char dynamic[];
+      __shared__ int rotated;
+      __shared__ int rank_of[1024];
       __shared__ double sigma[1024];
+      __shared__ double big;
+      const SvdEntry e = table[blockIdx.x];
+      const int64_t m = e.rows, n = e.cols;
+      const bool wide = n > m;
+      const int64_t len = wide ? n : m, k = wide ? m : n;  // W is len x k, column-major
+      if (k == 0)
+      {
+        if (threadIdx.x == 0) info[blockIdx.x] = 0;
+        return;
+      }
+      unsigned char *base = svd_bytes(len, k) <= kDynamicBytes ? dynamic : workspace + e.ws_off * 8;
+      double *w = reinterpret_cast<double *>(base);
+      double *v = w + len * k;
+      double *g = v + k * k;
+      double *norms = g + k * k;
+      float *w32 = reinterpret_cast<float *>(norms + k);
+      float *v32 = w32 + len * k;
+      float *norms32 = v32 + k * k;
+      const double *src = a + e.a_off;
+      const auto entry = [&](int64_t row, int64_t col) -> double
+      { return wide ? src[col * n + row] : src[row * n + col]; };  // row < len, col < k
+
+      // 1. FP32 sweeps on the block scaled to |entries| <= 1
+      if (threadIdx.x == 0) big = 0.0;
+      __syncthreads();
+      {
+        double local = 0.0;
+        for (int64_t i = threadIdx.x; i < len * k; i += blockDim.x) local = fmax(local, fabs(entry(i % len, i / len)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long *>(&big), __double_as_longlong(local));
+      }
+      __syncthreads();
+      const double scale = big > 0.0 ? 1.0 / big : 1.0;
+      for (int64_t i = threadIdx.x; i < len * k; i += blockDim.x)
+        w32[i] = static_cast<float>(entry(i % len, i / len) * scale);
+      for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x) v32[i] = (i / k == i % k) ? 1.0f : 0.0f;
+      __syncthreads();
+      jacobi_phase<float>(w32, v32, norms32, len, k, 1e-5, &rotated);
+
+      // 2. V = V32 in FP64, orthonormal by two Newton-Schulz steps: G = V^T V, V <- V (3 I - G) / 2
+      for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x) v[i] = static_cast<double>(v32[i]);
+      __syncthreads();
+      for (int step = 0; step < 2; ++step)
+      {
+        for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x)
+        {
+          const int64_t r = i % k, c = i / k;  // G[r][c] = v_r . v_c (columns of V)
+          const double *vr = v + r * k, *vc = v + c * k;
+          double sum = 0.0;
+          for (int64_t x = 0; x < k; ++x) sum = fma(vr[x], vc[x], sum);
+          g[i] = sum;
+        }
+        __syncthreads();
+        // the new V into W's space (free until step 3): V'[:, c] = sum_r V[:, r] (1.5 d_rc - 0.5 G[r][c])
+        for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x)
+        {
+          const int64_t row = i % k, c = i / k;
+          double sum = 1.5 * v[c * k + row];
+          for (int64_t r = 0; r < k; ++r) sum = fma(-0.5 * g[c * k + r], v[r * k + row], sum);
+          w[i] = sum;
+        }
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x) v[i] = w[i];
+        __syncthreads();
+      }
+
+      // 3. W = A V in FP64
+      for (int64_t i = threadIdx.x; i < len * k; i += blockDim.x)
+      {
+        const int64_t row = i % len, j = i / len;
+        const double *vj = v + j * k;
+        double sum = 0.0;
+        for (int64_t c = 0; c < k; ++c) sum = fma(entry(row, c), vj[c], sum);
+        w[i] = sum;
+      }
+      __syncthreads();
+
+      // 4. FP64 sweeps
+      const int sweeps = jacobi_phase<double>(w, v, norms, len, k, 2.220446049250313e-16 * sqrt(static_cast<double>(len)),
+                                             &rotated);
+
+      // singular values (column norms), their ranks, and the factors in descending order
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
       for (int64_t j = warp; j < k; j += warps)
       {
         const double *wj = w + j * len;
-        double norm = 0;
-        for (int64_t i = lane; i < len; i += 32) norm = fma(wj[i], wj[i], norm);
-        norm = warp_sum(norm);
-        if (lane == 0) sigma[j] = sqrt(norm);
+        double sum = 0;
+        for (int64_t i = lane; i < len; i += 32) sum = fma(wj[i], wj[i], sum);
+        sum = warp_sum(sum);
+        if (lane == 0) sigma[j] = sqrt(sum);
       }
       __syncthreads();
       for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
@@ -248,23 +368,27 @@ namespace ttg
   } // namespace
 
   cudaError_t svd_blocks(int32_t count, const void *table, const double *a, double *u, double *s, double *vh,
-                         double *workspace, int32_t *info, cudaStream_t stream)
+                         void *workspace, int32_t *info, cudaStream_t stream)
   {
     if (count <= 0) return cudaSuccess;
     static std::once_flag once;
     static cudaError_t configured = cudaSuccess;
     std::call_once(once, [] {
       configured = cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        kSvdSmemBytes - 16 * 1024);
+                                        static_cast<int>(kDynamicBytes));
     });
     if (configured != cudaSuccess) return configured;
-    const int64_t smem = kSvdSmemBytes - 16 * 1024;  // the static arrays take 12 KB
-    jacobi_svd_kernel<<<count, kSvdThreads, smem, stream>>>(static_cast<const SvdEntry *>(table), a, u, s, vh,
-                                                            workspace, info, smem / 8);
+    jacobi_svd_kernel<<<count, kSvdThreads, kDynamicBytes, stream>>>(static_cast<const SvdEntry *>(table), a, u, s, vh,
+                                                                      static_cast<unsigned char *>(workspace), info);
     return cudaGetLastError();
   }
 
-  int64_t svd_shared_doubles() { return (kSvdSmemBytes - 16 * 1024) / 8; }
+  int64_t svd_workspace_doubles(int64_t rows, int64_t cols)
+  {
+    const int64_t len = std::max(rows, cols), k = std::min(rows, cols);
+    const int64_t bytes = svd_bytes(len, k);
+    return bytes <= kDynamicBytes ? 0 : (bytes + 7) / 8;
+  }
 
   cudaError_t svd_keep(int32_t count, const void *table, const double *u, const double *s, const double *vh,
                        double *first, double *second, double *values, cudaStream_t stream)

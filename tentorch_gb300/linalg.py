@@ -23,7 +23,7 @@ from typing import Optional
 
 import torch
 
-from tentorch_gb300._lib import check, f64, i32, i64, ints32, lib, pointers, vp
+from tentorch_gb300._lib import check, f64, i32, i64, ints32, ints64, lib, pointers, vp
 from tentorch_gb300.symmetry import Leg, _label
 from tentorch_gb300.tensor import BlockKey, Space, Tensor
 
@@ -294,18 +294,6 @@ def is_close(first: Tensor, second: Tensor, rtol: float = 1e-10, atol: float = 1
 # ---------------------------------------------------------------------------------------------
 
 
-_svd_shared = None
-
-
-def _shared_doubles() -> int:
-    global _svd_shared
-    if _svd_shared is None:
-        value = i64()
-        check(lib.tt_svd_shared_doubles(ctypes.byref(value)))
-        _svd_shared = value.value
-    return _svd_shared
-
-
 def _factor_blocks(arranged: Tensor):
     """The thin SVD of every non-empty block.  float64 blocks on the GPU go through one launch of
     the engine's Jacobi SVD (tt_svd_blocks), complex blocks, blocks beyond its size and the
@@ -323,16 +311,18 @@ def _factor_blocks(arranged: Tensor):
             factors.append([key, u, sv, vh, 0, 0])
         host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
         return factors, host, None
-    shared = _shared_doubles()
+    dims, count = ints64(x for i, _ in present for x in space.shapes[i])
+    places, total = (i64 * max(len(present), 1))(), i64()
+    check(lib.tt_svd_workspace(len(present), dims, places, ctypes.byref(total)))
+    ws_at = total.value
     table, shapes = [], []
-    u_at = s_at = vh_at = ws_at = 0
-    for i, key in present:
+    u_at = s_at = vh_at = 0
+    for at, (i, key) in enumerate(present):
         rows, cols = space.shapes[i]
-        k, length = min(rows, cols), max(rows, cols)
-        need = 0 if length * k + k * k <= shared else (k * k if length * k <= shared else length * k + k * k)
-        table += [space.offsets[i], rows, cols, u_at, s_at, vh_at, ws_at if need else -1]
+        k = min(rows, cols)
+        table += [space.offsets[i], rows, cols, u_at, s_at, vh_at, places[at]]
         shapes.append((key, rows, cols, k, u_at, s_at, vh_at))
-        u_at, s_at, vh_at, ws_at = u_at + rows * k, s_at + k, vh_at + k * cols, ws_at + (need + 31) // 32 * 32
+        u_at, s_at, vh_at = u_at + rows * k, s_at + k, vh_at + k * cols
     device = arranged.device
     dev_table = torch.tensor(table, dtype = torch.int64).to(device)
     u = torch.empty(max(u_at, 1), dtype = torch.float64, device = device)
