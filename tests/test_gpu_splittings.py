@@ -12,19 +12,22 @@ from tentorch_gb300 import linalg as la
 pytestmark = pytest.mark.gpu
 
 
-def _tensor(rows_by_charge, cols_by_charge, seed, scale = None):
+def _tensor(rows_by_charge, cols_by_charge, seed):
     '''A U(1) matrix-like tensor with one block per charge: codomain [a], domain [b].'''
     cat = tg.u1
     charges = sorted(rows_by_charge)
     a = tg.Leg(cat, [(q,) for q in charges], [rows_by_charge[q] for q in charges])
     b = tg.Leg(cat, [(q,) for q in charges], [cols_by_charge[q] for q in charges])
     t = tg.Tensor(cat, [a], [b], (0,), dtype = torch.float64, device = 'cuda')
-    gen = torch.Generator().manual_seed(seed)
-    data = torch.randn(t.data.shape, dtype = torch.float64, generator = gen)
-    if scale is not None:
-        data = data * scale
-    t.data.copy_(data)
+    _fill(t, seed)
     return t
+
+
+def _fill(t, seed):
+    """N(0, 1) blocks in key order; the arena's padding stays zero."""
+    gen = torch.Generator().manual_seed(seed)
+    for block in t.to_tuple()[3].values():
+        block.copy_(torch.randn(block.shape, dtype = torch.float64, generator = gen))
 
 
 SHAPES = {-3: (1, 1), -2: (1, 5), -1: (5, 1), 0: (60, 90), 1: (90, 60), 2: (117, 117), 3: (130, 140), 4: (300, 200)}
@@ -92,7 +95,7 @@ def test_split_of_the_two_site_tensor_pairs_the_bond():
     bond = tg.Leg(cat, [(-2,), (0,), (2,)], [6, 9, 6])
     phys = tg.Leg(cat, [(-1,), (1,)], [1, 1])
     t = tg.Tensor(cat, [bond, phys], [phys, bond], (0,), dtype = torch.float64, device = 'cuda')
-    t.data.copy_(torch.randn(t.data.shape, dtype = torch.float64, generator = torch.Generator().manual_seed(4)))
+    _fill(t, 4)
     first, values, second = tg.svd(t, 11, 1e-14, 2)
     leg = first.domain[0]
     mult = {leg.sector(b): leg.multiplicity(b) for b in range(leg.nblocks())}
