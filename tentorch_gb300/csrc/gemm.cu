@@ -288,13 +288,18 @@ namespace ttg
       asm volatile("bar.sync %0, %1;\n" ::"r"(worker + 1), "r"(kWorkerThreads) : "memory");
     }
 
-    // The next item for a worker: its first thread draws from the launch's counter (the word after
-    // the tile tickets, zeroed before the launch), so faster SMs simply take more items.
+    // A worker's first item is fixed, round robin over the SMs first (worker w of CTA b takes item
+    // w * grid + b): the workers of one SM share its FP64 pipe, so the opening items have to spread
+    // over every SM before any SM gets a second one.  After that each worker draws from the launch's
+    // counter (the word after the tile tickets, zeroed before the launch), so faster SMs simply take
+    // more items.
+    __device__ __forceinline__ int64_t first_item(int worker) { return static_cast<int64_t>(worker) * gridDim.x + blockIdx.x; }
+
     __device__ __forceinline__ int64_t claim(int worker, int lt, int *slot, int *counter)
     {
       if (lt == 0) *slot = atomicAdd(counter, 1);
       worker_sync(worker);
-      const int64_t idx = *slot;
+      const int64_t idx = *slot + static_cast<int64_t>(gridDim.x) * (blockDim.x / kWorkerThreads);
       worker_sync(worker);
       return idx;
     }
@@ -375,7 +380,7 @@ namespace ttg
       const int tx = lt % (BN / TN), ty = lt / (BN / TN);
       __shared__ int next[kF64Workers];
       int *counter = tickets + n_reduces;  // workers per CTA = blockDim.x / 128, chosen at launch
-      for (int64_t idx = claim(worker, lt, next + worker, counter); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      for (int64_t idx = first_item(worker); idx < n_items; idx = claim(worker, lt, next + worker, counter))
       {
         const GemmItem it = items[idx];
         const DevBlock blk = blocks[it.block];
@@ -483,7 +488,7 @@ namespace ttg
       const int fr = lane >> 2, fk = lane & 3;  // fragment row (or column) and k of this lane
       __shared__ int next[kF64Workers];
       int *counter = tickets + n_reduces;  // workers per CTA = blockDim.x / 128, chosen at launch
-      for (int64_t idx = claim(worker, lt, next + worker, counter); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      for (int64_t idx = first_item(worker); idx < n_items; idx = claim(worker, lt, next + worker, counter))
       {
         const GemmItem it = items[idx];
         const DevBlock blk = blocks[it.block];
@@ -684,7 +689,7 @@ namespace ttg
       const int wm = warp >> 1, wn = warp & 1;
       __shared__ int next[kSplitWorkers];
       int *counter = tickets + n_reduces;
-      for (int64_t idx = claim(worker, lt, next + worker, counter); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      for (int64_t idx = first_item(worker); idx < n_items; idx = claim(worker, lt, next + worker, counter))
       {
         const SplitItem it = items[idx];
         const DevBlock blk = blocks[it.block];
