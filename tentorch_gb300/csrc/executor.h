@@ -54,6 +54,9 @@ namespace ttg
     {
       GemmItem *items = nullptr;
       GemmReduce *reduces = nullptr;
+      int32_t *cta_begin = nullptr;  // per CTA, the start of its list of items (n_ctas + 1 entries)
+      int32_t n_ctas = 0;
+      int64_t longest = 0;           // the longest list
       int64_t n_items = 0, n_reduces = 0, slots = 0;
     };
     struct SplitTables

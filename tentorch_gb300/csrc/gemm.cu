@@ -45,9 +45,11 @@ namespace ttg
   {
     GemmSchedule s;
     // The workers of one SM share its FP64 pipe, so what has to balance is the work per SM: items
-    // of about 1/8 of an SM's share (a matvec's stage has only ~10^5 multiply-adds per SM), never
-    // smaller than a tile over 32 of K (below that the partial tiles cost more than they save).
-    const double target = std::max(op_work(p, op) / (152.0 * 8.0), static_cast<double>(bm) * bn * 32.0);
+    // of a few per SM (a matvec's stage has only ~10^5 multiply-adds per SM), each a tile over a
+    // K range of at least 16, dealt to the SMs largest first, each to the least loaded (LPT), with a
+    // fixed cost per item for its loads, its barriers and its partial tile.
+    const double target = std::max(op_work(p, op) / (kScheduleCtas * 6.0), static_cast<double>(bm) * bn * 16.0);
+    const double per_item = static_cast<double>(bm) * bn * 4.0;
     struct Sized
     {
       GemmItem item;
@@ -71,7 +73,7 @@ namespace ttg
           const int32_t bi = static_cast<int32_t>(b);
           if (chunks == 1)
           {
-            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work});
+            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work + per_item});
             continue;
           }
           const int32_t slot0 = static_cast<int32_t>(s.slots), reduce = static_cast<int32_t>(s.reduces.size());
@@ -80,14 +82,34 @@ namespace ttg
             const int64_t k0 = c * kc, k1 = std::min(ktotal, (c + 1) * kc);
             items.push_back({{bi, m0, n0, static_cast<int32_t>(k0), static_cast<int32_t>(k1), static_cast<int32_t>(s.slots++),
                               reduce, 0},
-                             rows * cols * static_cast<double>(k1 - k0)});
+                             rows * cols * static_cast<double>(k1 - k0) + per_item});
           }
           s.reduces.push_back({bi, m0, n0, slot0, static_cast<int32_t>(chunks), 0});
         }
     }
-    // the largest items first, so the round robin ends on small ones
     std::stable_sort(items.begin(), items.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
-    for (const Sized &it : items) s.items.push_back(it.item);
+    // LPT: each item to the CTA with the least work so far (ties to the lower index)
+    const int ctas = static_cast<int>(std::min<size_t>(kScheduleCtas, std::max<size_t>(items.size(), 1)));
+    std::vector<std::vector<GemmItem>> lists(static_cast<size_t>(ctas));
+    std::vector<std::pair<double, int>> heap;
+    for (int c = 0; c < ctas; ++c) heap.push_back({0.0, c});
+    const auto later = [](const std::pair<double, int> &a, const std::pair<double, int> &b)
+    { return a.first > b.first || (a.first == b.first && a.second > b.second); };
+    std::make_heap(heap.begin(), heap.end(), later);
+    for (const Sized &it : items)
+    {
+      std::pop_heap(heap.begin(), heap.end(), later);
+      auto &least = heap.back();
+      lists[static_cast<size_t>(least.second)].push_back(it.item);
+      least.first += it.work;
+      std::push_heap(heap.begin(), heap.end(), later);
+    }
+    s.cta_begin.push_back(0);
+    for (const auto &list : lists)
+    {
+      s.items.insert(s.items.end(), list.begin(), list.end());
+      s.cta_begin.push_back(static_cast<int32_t>(s.items.size()));
+    }
     return s;
   }
 
@@ -295,6 +317,16 @@ namespace ttg
     // more items.
     __device__ __forceinline__ int64_t first_item(int worker) { return static_cast<int64_t>(worker) * gridDim.x + blockIdx.x; }
 
+    // The next entry of the CTA's own list for a worker.
+    __device__ __forceinline__ int64_t local_claim(int worker, int lt, int *slot, int *taken)
+    {
+      if (lt == 0) *slot = atomicAdd(taken, 1);
+      worker_sync(worker);
+      const int64_t idx = *slot;
+      worker_sync(worker);
+      return idx;
+    }
+
     __device__ __forceinline__ int64_t claim(int worker, int lt, int *slot, int *counter)
     {
       if (lt == 0) *slot = atomicAdd(counter, 1);
@@ -368,7 +400,7 @@ namespace ttg
     __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1)
       gemm_f64_kernel(const T *__restrict__ A, const T *__restrict__ B, T *__restrict__ C,
                       const DevBlock *__restrict__ blocks, const DevPair *__restrict__ pairs,
-                      const GemmItem *__restrict__ items, int64_t n_items, const GemmReduce *__restrict__ reduces,
+                      const GemmItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                       int64_t n_reduces, T *__restrict__ partial, int *__restrict__ tickets)
     {
       constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16, TM = 2, TN = 4;
@@ -378,9 +410,15 @@ namespace ttg
       T(*bs)[BN + 1] = reinterpret_cast<T(*)[BN + 1]>(smem_raw + (worker * 2 + 1) * BK * (BM + 1) * sizeof(T));
       __shared__ int flags[kF64Workers];
       const int tx = lt % (BN / TN), ty = lt / (BN / TN);
+      // this CTA's list of items (dealt by the host, largest first, to balance the SMs); its
+      // workers take them in order through a shared counter
       __shared__ int next[kF64Workers];
-      int *counter = tickets + n_reduces;  // workers per CTA = blockDim.x / 128, chosen at launch
-      for (int64_t idx = first_item(worker); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      __shared__ int taken;
+      if (threadIdx.x == 0) taken = 0;
+      __syncthreads();
+      const int64_t list_begin = cta_begin[blockIdx.x], list_end = cta_begin[blockIdx.x + 1];
+      for (int64_t idx = list_begin + local_claim(worker, lt, next + worker, &taken); idx < list_end;
+           idx = list_begin + local_claim(worker, lt, next + worker, &taken))
       {
         const GemmItem it = items[idx];
         const DevBlock blk = blocks[it.block];
@@ -471,7 +509,7 @@ namespace ttg
     __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1)
       gemm_dmma_kernel(const double *__restrict__ A, const double *__restrict__ B, double *__restrict__ C,
                        const DevBlock *__restrict__ blocks, const DevPair *__restrict__ pairs,
-                       const GemmItem *__restrict__ items, int64_t n_items, const GemmReduce *__restrict__ reduces,
+                       const GemmItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                        int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
     {
       constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16;
@@ -486,9 +524,15 @@ namespace ttg
       const int warp = lt >> 5, lane = lt & 31;
       const int wm = warp >> 1, wn = warp & 1;
       const int fr = lane >> 2, fk = lane & 3;  // fragment row (or column) and k of this lane
+      // this CTA's list of items (dealt by the host, largest first, to balance the SMs); its
+      // workers take them in order through a shared counter
       __shared__ int next[kF64Workers];
-      int *counter = tickets + n_reduces;  // workers per CTA = blockDim.x / 128, chosen at launch
-      for (int64_t idx = first_item(worker); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      __shared__ int taken;
+      if (threadIdx.x == 0) taken = 0;
+      __syncthreads();
+      const int64_t list_begin = cta_begin[blockIdx.x], list_end = cta_begin[blockIdx.x + 1];
+      for (int64_t idx = list_begin + local_claim(worker, lt, next + worker, &taken); idx < list_end;
+           idx = list_begin + local_claim(worker, lt, next + worker, &taken))
       {
         const GemmItem it = items[idx];
         const DevBlock blk = blocks[it.block];
@@ -871,9 +915,9 @@ namespace ttg
     cudaError_t e = cudaSuccess;
     e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces + 1) * 4, stream);  // tickets and the item counter
     if (e != cudaSuccess) return e;
-    // spread the items over every SM first: workers per CTA = items / SMs, at most kF64Workers
-    const int grid = static_cast<int>(std::min<int64_t>(sm_count(), sched.n_items));
-    const int workers = static_cast<int>(std::clamp<int64_t>((sched.n_items + grid - 1) / grid, 1, kF64Workers));
+    // one CTA per list the schedule dealt, as many workers as its longest list needs (at most four)
+    const int grid = sched.n_ctas;
+    const int workers = static_cast<int>(std::clamp<int64_t>(sched.longest, 1, kF64Workers));
     if (complex)
     {
       const int bytes = std::max<int>(kF64Workers * 2 * 16 * (kF64TileM + 1) * 16, kPinBytes);
@@ -881,7 +925,7 @@ namespace ttg
       if ((e = configure(gemm_f64_kernel<double2>, bytes, once)) != cudaSuccess) return e;
       gemm_f64_kernel<double2><<<grid, workers * kWorkerThreads, bytes, stream>>>(
         static_cast<const double2 *>(A), static_cast<const double2 *>(B), static_cast<double2 *>(C), blocks, pairs,
-        sched.items, sched.n_items, sched.reduces, sched.n_reduces, static_cast<double2 *>(partial), tickets);
+        sched.items, sched.cta_begin, sched.reduces, sched.n_reduces, static_cast<double2 *>(partial), tickets);
     }
     else
     {
@@ -890,7 +934,7 @@ namespace ttg
       if ((e = configure(gemm_dmma_kernel, bytes, once)) != cudaSuccess) return e;
       gemm_dmma_kernel<<<grid, workers * kWorkerThreads, bytes, stream>>>(
         static_cast<const double *>(A), static_cast<const double *>(B), static_cast<double *>(C), blocks, pairs,
-        sched.items, sched.n_items, sched.reduces, sched.n_reduces, static_cast<double *>(partial), tickets);
+        sched.items, sched.cta_begin, sched.reduces, sched.n_reduces, static_cast<double *>(partial), tickets);
     }
     return cudaGetLastError();
   }
@@ -954,8 +998,13 @@ namespace ttg
         dst.n_items = static_cast<int64_t>(s.items.size());
         dst.n_reduces = static_cast<int64_t>(s.reduces.size());
         dst.slots = s.slots;
+        dst.n_ctas = static_cast<int32_t>(s.cta_begin.size()) - 1;
+        dst.longest = 0;
+        for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c)
+          dst.longest = std::max<int64_t>(dst.longest, s.cta_begin[c + 1] - s.cta_begin[c]);
         staging.add(s.items, reinterpret_cast<void **>(&dst.items));
         staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
+        staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
       }
       const SplitSchedule &s = p.gemm_plans->split[i];
       DeviceTables::SplitTables &dst = t.split[i];

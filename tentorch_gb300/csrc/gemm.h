@@ -34,10 +34,13 @@ namespace ttg
   };
   struct GemmSchedule
   {
-    std::vector<GemmItem> items;
+    std::vector<GemmItem> items;     // grouped by the CTA that runs them
     std::vector<GemmReduce> reduces;
-    int64_t slots = 0;  // partial tiles of bm x bn doubles
+    std::vector<int32_t> cta_begin;  // CTA b runs items [cta_begin[b], cta_begin[b + 1])
+    int64_t slots = 0;               // partial tiles of bm x bn doubles
   };
+  // The CTAs a schedule spreads its items over: one per SM of the GPU.
+  constexpr int kScheduleCtas = 152;
 
   // Split precision works pair by pair: an item is one pair's K range (a multiple of 32 long, but
   // for the pair's last one), so a tile with several pairs or chunks always goes through partials.

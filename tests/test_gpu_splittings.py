@@ -30,7 +30,11 @@ def _fill(t, seed):
         block.copy_(torch.randn(block.shape, dtype = torch.float64, generator = gen))
 
 
-SHAPES = {-3: (1, 1), -2: (1, 5), -1: (5, 1), 0: (60, 90), 1: (90, 60), 2: (117, 117), 3: (130, 140), 4: (300, 200)}
+# charge-symmetric (the split pairs q with -q, svd.cpp:97-120, so a bond sector without its dual
+# partner would be dropped): tall and wide blocks, small ones, ones whose working set fits in
+# shared memory and ones that need the global workspace
+SHAPES = {-5: (300, 200), -4: (130, 140), -3: (1, 1), -2: (1, 5), -1: (60, 90), 0: (117, 117), 1: (90, 60),
+          2: (5, 1), 3: (1, 1), 4: (140, 130), 5: (200, 300)}
 
 
 def _blocks(t):
