@@ -46,10 +46,26 @@ namespace ttg
     GemmSchedule s;
     // The workers of one SM share its FP64 pipe, so what has to balance is the work per SM: items
     // of a few per SM (a matvec's stage has only ~10^5 multiply-adds per SM), each a tile over a
-    // K range of at least 16, dealt to the SMs largest first, each to the least loaded (LPT), with a
-    // fixed cost per item for its loads, its barriers and its partial tile.
-    const double target = std::max(op_work(p, op) / (kScheduleCtas * 6.0), static_cast<double>(bm) * bn * 16.0);
-    const double per_item = static_cast<double>(bm) * bn * 4.0;
+    // K range of at least 16, dealt to the SMs largest first, each to the least loaded (LPT).
+    // Cost of an item: the 8 x 8 DMMA fragments it computes (fragments wholly outside the block are
+    // skipped) times its K range, plus per K step of 16 a quarter of a full tile's step (its loads
+    // and barriers) and per item the same again (claim, write or partial tile).
+    const auto cost = [bm, bn](double rows, double cols, double k)
+    {
+      const double frag = std::ceil(rows / 8.0) * 8.0 * std::ceil(cols / 8.0) * 8.0;
+      return frag * k + 0.25 * bm * bn * 16.0 * (std::ceil(k / 16.0) + 1.0);
+    };
+    double total = 0;
+    for (int64_t b = op.begin; b < op.begin + op.count; ++b)
+    {
+      const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(b)];
+      int64_t ktotal = 0;
+      for (int32_t k = 0; k < blk.pair_count; ++k) ktotal += p.gemm_pairs[static_cast<size_t>(blk.pair_begin + k)].k;
+      for (int32_t m0 = 0; m0 < blk.m; m0 += bm)
+        for (int32_t n0 = 0; n0 < blk.n; n0 += bn)
+          total += cost(std::min(bm, blk.m - m0), std::min(bn, blk.n - n0), static_cast<double>(ktotal));
+    }
+    const double target = std::max(total / (kScheduleCtas * 6.0), cost(bm, bn, 16.0));
     struct Sized
     {
       GemmItem item;
@@ -65,7 +81,7 @@ namespace ttg
         for (int32_t n0 = 0; n0 < blk.n; n0 += bn)
         {
           const double rows = std::min(bm, blk.m - m0), cols = std::min(bn, blk.n - n0);
-          const double work = rows * cols * static_cast<double>(ktotal);
+          const double work = cost(rows, cols, static_cast<double>(ktotal));
           int64_t chunks = std::max<int64_t>(1, static_cast<int64_t>(std::ceil(work / target)));
           int64_t kc = (ktotal + chunks - 1) / std::max<int64_t>(chunks, 1);
           kc = std::max<int64_t>(16, (kc + 15) / 16 * 16);
@@ -73,7 +89,7 @@ namespace ttg
           const int32_t bi = static_cast<int32_t>(b);
           if (chunks == 1)
           {
-            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work + per_item});
+            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work});
             continue;
           }
           const int32_t slot0 = static_cast<int32_t>(s.slots), reduce = static_cast<int32_t>(s.reduces.size());
@@ -82,7 +98,7 @@ namespace ttg
             const int64_t k0 = c * kc, k1 = std::min(ktotal, (c + 1) * kc);
             items.push_back({{bi, m0, n0, static_cast<int32_t>(k0), static_cast<int32_t>(k1), static_cast<int32_t>(s.slots++),
                               reduce, 0},
-                             rows * cols * static_cast<double>(k1 - k0) + per_item});
+                             cost(rows, cols, static_cast<double>(k1 - k0))});
           }
           s.reduces.push_back({bi, m0, n0, slot0, static_cast<int32_t>(chunks), 0});
         }
@@ -537,6 +553,8 @@ namespace ttg
         const GemmItem it = items[idx];
         const DevBlock blk = blocks[it.block];
         double acc[2][2][2] = {};
+        const bool live_i[2] = {it.m0 + wm * 16 < blk.m, it.m0 + wm * 16 + 8 < blk.m};
+        const bool live_j[2] = {it.n0 + wn * 16 < blk.n, it.n0 + wn * 16 + 8 < blk.n};
         int32_t kbase = 0;
         for (int32_t pi = 0; pi < blk.pair_count; ++pi)
         {
@@ -562,18 +580,24 @@ namespace ttg
               bs[kk][cc] = (gk < hi && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : 0.0;
             }
             worker_sync(worker);
-#pragma unroll
-            for (int kb = 0; kb < BK; kb += 4)
+            if (live_i[0] && live_j[0])  // the warp's 16 x 16 quarter touches the block
             {
-              double af[2], bf[2];
 #pragma unroll
-              for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
+              for (int kb = 0; kb < BK; kb += 4)
+              {
+                double af[2], bf[2];
 #pragma unroll
-              for (int j = 0; j < 2; ++j) bf[j] = bs[kb + fk][wn * 16 + j * 8 + fr];
+                for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
 #pragma unroll
-              for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j) bf[j] = bs[kb + fk][wn * 16 + j * 8 + fr];
+                // an 8 x 8 fragment wholly outside the block costs the FP64 pipe as much as a full
+                // one: skip it (warp-uniform)
 #pragma unroll
-                for (int j = 0; j < 2; ++j) dmma(acc[i][j], af[i], bf[j]);
+                for (int i = 0; i < 2; ++i)
+#pragma unroll
+                  for (int j = 0; j < 2; ++j)
+                    if (live_i[i] && live_j[j]) dmma(acc[i][j], af[i], bf[j]);
+              }
             }
             worker_sync(worker);
           }
