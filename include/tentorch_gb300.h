@@ -147,6 +147,21 @@ int32_t tt_step_plan(int32_t space, int32_t kind, int32_t arm, int64_t key_cod, 
 int32_t tt_chain(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
                  int32_t cap, int32_t *steps, int32_t *n);
 
+/* ---- the Lanczos eigensolver of a window (tentorch/linalg/lanczos.py:8-64) ------------------ */
+
+/* Doubles of scratch tt_lanczos needs for an arena of n entries and n_iter (1..60) steps. */
+int32_t tt_lanczos_scratch(int64_t n, int32_t n_iter, int32_t dtype, int64_t *doubles);
+/* The lowest eigenpair of the Hermitian action v -> plan(inputs with v as operand `vector_operand`)
+ * by n_iter Krylov steps from `start` with full reorthogonalisation, all on `stream` with one host
+ * synchronisation at the end: *energy is the lowest Ritz value, `result` the normalised Ritz vector
+ * and *size the Krylov dimension used (the steps before the first norm below `tol`, as the
+ * reference stops).  The plan's output space must be the vector operand's space.  `prepared` as
+ * for tt_plan_execute; `workspace` the plan's workspace; `scratch` tt_lanczos_scratch doubles. */
+int32_t tt_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                   const void *const *prepared, int32_t vector_operand, const void *start, int32_t n_iter,
+                   double tol, void *workspace, void *scratch, void *result, double *energy, int32_t *size,
+                   void *stream);
+
 /* ---- truncating splittings (tentorch/linalg/graded/svd.cpp:41-177) -------------------------- */
 
 /* Thin SVDs of `count` float64 blocks in one launch (one-sided Jacobi, mixed precision: FP32 sweeps,

@@ -113,6 +113,14 @@ namespace ttg
   cudaError_t svd_keep(int32_t count, const void *table, const double *u, const double *s, const double *vh,
                        double *first, double *second, double *values, cudaStream_t stream);
 
+  // The Lanczos loop of a window (lanczos.cu): `base` carries the plan's operands (the vector
+  // operand's pointer is replaced by each basis vector), prepared arenas and workspace; scratch holds
+  // lanczos_scratch_doubles() doubles; the normalised Ritz vector goes to `result`.
+  int64_t lanczos_scratch_doubles(int64_t n_doubles, int32_t n_iter);
+  cudaError_t lanczos(const Program &p, DeviceTables &t, const ExecArgs &base, int32_t vector_operand,
+                      const double *start, int64_t n_doubles, int32_t n_iter, double tol, double *scratch,
+                      double *result, double *energy, int32_t *size_out);
+
   constexpr int kDotParts = 120;
   // out[2j], out[2j+1] = re, im of <a_j, b> for j < count; partial holds 2*kDotParts*count doubles.
   cudaError_t arena_dots(const double *const *dev_as, int32_t count, const double *b, int64_t n_doubles, bool complex,

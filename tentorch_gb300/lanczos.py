@@ -10,6 +10,7 @@ steps computed after such a stop are discarded, so the result is the reference's
 '''
 from __future__ import annotations
 
+import ctypes
 from typing import Callable
 
 import numpy as np
@@ -80,3 +81,43 @@ def lanczos(action: Callable[[Tensor], Tensor], start: Tensor, n_iter: int = 5,
     result = torch.mv(basis[:size].transpose(0, 1), coefficients)
     result = result / torch.linalg.vector_norm(result)
     return float(values[0]), Tensor._wrap(space, result.contiguous())
+
+
+def lanczos_einsum(spec: str, tensors, vector: int, start: Tensor, n_iter: int = 5, tol: float = 1e-12,
+                   outcharge = None) -> tuple[float, Tensor]:
+    '''
+    `lanczos(lambda v: einsum(spec, *tensors with v as operand `vector`), start, n_iter, tol)` with
+    the whole Krylov loop on the device (tt_lanczos): the einsum's compiled plan runs on each basis
+    vector, the projections and norms stay on the GPU, and the host reads the tridiagonal once.  The
+    operands other than the vector are prepared once for every step (the head and tail of a DMRG
+    window).  Same result as `lanczos` up to round-off; block products in the current precision.
+    '''
+    if n_iter < 1:
+        raise ValueError(f'Lanczos needs at least one step, not {n_iter}.')
+    if norm(start) == 0.0:
+        raise ValueError('Lanczos needs a starting vector of non-zero norm.')
+    from tentorch_gb300 import linalg
+    from tentorch_gb300._lib import check, f64, i32, i64, lib, pointers
+    operands = list(tensors)
+    operands[vector] = start
+    linalg._check_device(operands)
+    plan = linalg.plan_of(spec, *operands, outcharge = outcharge)
+    if plan.out_space is not start._space:
+        raise ValueError('the action has to map the vector to a tensor with the same legs')
+    data = start._data
+    device = data.device
+    stream = torch.cuda.current_stream(device).cuda_stream
+    ws = linalg._workspace(plan, device, data.dtype, stream)
+    prepared = [None if i == vector else linalg._prepared_arena(plan, i, t, ws, stream, force = True)
+                for i, t in enumerate(operands)]
+    doubles = i64()
+    check(lib.tt_lanczos_scratch(start._space.size, n_iter, linalg._DTYPE[data.dtype], ctypes.byref(doubles)))
+    scratch = torch.empty(doubles.value, dtype = torch.float64, device = device)
+    result = torch.empty_like(data)
+    energy, size = f64(), i32()
+    check(lib.tt_lanczos(plan.handle, linalg._DTYPE[data.dtype], linalg.get_precision(),
+                         pointers(t._data.data_ptr() for t in operands),
+                         pointers((p.data_ptr() if p is not None else None) for p in prepared), vector, data.data_ptr(),
+                         n_iter, tol, ws.data_ptr() if ws is not None else None, scratch.data_ptr(), result.data_ptr(),
+                         ctypes.byref(energy), ctypes.byref(size), stream))
+    return float(energy.value), Tensor._wrap(start._space, result)

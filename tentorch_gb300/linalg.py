@@ -141,7 +141,7 @@ def _workspace(plan: Plan, device, dtype, stream) -> Optional[torch.Tensor]:
     return pool
 
 
-def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws, stream) -> Optional[torch.Tensor]:
+def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws, stream, force: bool = False) -> Optional[torch.Tensor]:
     """The operand's prepared arena when the same arena (same version) comes back to this plan: the
     first sighting runs the operand's phase inside the plan and only remembers the arena; the
     second prepares it once for every call after (the head and tail of a Lanczos window)."""
@@ -151,13 +151,13 @@ def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws, stream) -> Opt
     key = (plan.handle.value, operand)
     held = _prepared.get(key)
     data = tensor._data
-    if held is not None and held[0]() is data and held[1] == data._version:
-        if held[2] is not None:
+    if force or (held is not None and held[0]() is data and held[1] == data._version):
+        if held is not None and held[0]() is data and held[1] == data._version and held[2] is not None:
             return held[2]
         arena = torch.empty(size, dtype = data.dtype, device = data.device)
         check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
                                   ws.data_ptr() if ws is not None else None, stream))
-        _prepared[key] = (held[0], held[1], arena)
+        _prepared[key] = (weakref.ref(data), data._version, arena)
         return arena
     if len(_prepared) > 256:
         # operands that are gone

@@ -15,7 +15,7 @@ from typing import Callable, Literal, Optional, Sequence
 import numpy as np
 import torch
 
-from tentorch_gb300.lanczos import lanczos
+from tentorch_gb300.lanczos import lanczos, lanczos_einsum
 from tentorch_gb300.linalg import contract, einsum, inner, precision, qr, rq, svd
 from tentorch_gb300.symmetry import (AbelianGroup, FusionCategory, FusionTree, Leg, NoSymmetry, fusion_trees,
                                      reachable_charges, u1)
@@ -367,12 +367,11 @@ class DMRG:
         head = einsum('EIa,IPqj->EPaqj', self.left[at], site)
         tail = einsum('JRsk,Fkb->JRSFb', following, self.right[at + 2])
 
-        def action(vector: Tensor) -> Tensor:
-            self.matvecs += 1
-            with precision(self.precision):
-                return einsum('EPaqj,JRSFb,AQsb->EPrf', head, tail, vector)
-
-        energy, vector = lanczos(action, two, self.n_iter)
+        # the reference's action, einsum('EPaqj,JRSFb,AQsb->EPrf', head, tail, vector), with the
+        # Krylov loop on the device
+        with precision(self.precision):
+            energy, vector = lanczos_einsum('EPaqj,JRSFb,AQsb->EPrf', [head, tail, two], 2, two, self.n_iter)
+        self.matvecs += self.n_iter
         factor = 2 if direction == 'right' else 1
         left, values, right = svd(vector, self.max_bond_dim, self.svd_tol, factor)
         self.state.tensors[at], self.state.tensors[at + 1] = left, right.place([0, 1])
