@@ -94,6 +94,10 @@ int32_t tt_space_legs(int32_t space, int32_t cap, int32_t *legs, int32_t *ncod, 
 int32_t tt_plan_place(int32_t space, int32_t nabove, const int32_t *above, int32_t nbelow, const int32_t *below,
                       tt_plan **out);
 /* contract(left, right, left_legs, right_legs[, charge]) (linalg/graded/contract.cpp:117-175). */
+/* The conjugate-transpose (bra) of a tensor of `space`: block (r, s, c) becomes block (s, r, c) of the
+ * space with codomain and domain swapped and the dual charge, transposed and conjugated
+ * (tentorch/tensors/tensor.cpp:99-107); one tiles pass. */
+int32_t tt_plan_conj(int32_t space, tt_plan **out);
 int32_t tt_plan_contract(int32_t left, int32_t right, int32_t n, const int32_t *left_legs, const int32_t *right_legs,
                          int32_t has_charge, int64_t charge, tt_plan **out);
 /* einsum(spec, *operands, outcharge=) (linalg/graded/einsum.cpp:444-605, bindings.cpp:347-361). */

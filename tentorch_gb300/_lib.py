@@ -46,6 +46,7 @@ _declare('tt_space_size', i32, P(i64), P(i64))
 _declare('tt_space_blocks', i32, i64, P(i64), P(i64))
 _declare('tt_space_legs', i32, i32, P(i32), P(i32), P(i32), P(i64))
 _declare('tt_plan_place', i32, i32, P(i32), i32, P(i32), P(vp))
+_declare('tt_plan_conj', i32, P(vp))
 _declare('tt_plan_contract', i32, i32, i32, P(i32), P(i32), i32, i64, P(vp))
 _declare('tt_plan_einsum', ctypes.c_char_p, i32, P(i32), i32, i64, P(vp))
 _declare('tt_plan_info', vp, P(i32), P(i64), P(f64), P(i64), P(i32))
@@ -93,6 +94,6 @@ def pointers(values):
 
 EXPORTED = ['tt_last_error', 'tt_version', 'tt_category', 'tt_outcomes', 'tt_dual', 'tt_q_dim', 'tt_F_symbol',
             'tt_R_symbol', 'tt_leg', 'tt_leg_blocks', 'tt_reachable_charges', 'tt_fusion_trees', 'tt_space',
-            'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_contract', 'tt_plan_einsum',
+            'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_conj', 'tt_plan_contract', 'tt_plan_einsum',
             'tt_plan_info', 'tt_plan_describe', 'tt_plan_cache_clear', 'tt_plan_gather', 'tt_plan_prepared_size', 'tt_plan_execute', 'tt_plan_execute_timed', 'tt_plan_prepare', 'tt_step_plan', 'tt_chain', 'tt_svd_workspace', 'tt_lanczos_scratch', 'tt_lanczos', 'tt_svd_blocks', 'tt_svd_keep',
             'tt_dots', 'tt_dots_noalloc']

@@ -299,6 +299,14 @@ extern "C"
     });
   }
 
+  int32_t tt_plan_conj(int32_t space, tt_plan **out)
+  {
+    return guarded([&] {
+      const std::string name = "conj|" + std::to_string(space);
+      *out = keep(plan_cache(), name, [&] { return ttg::compile_conj(ttg::space_by_id(space)); });
+    });
+  }
+
   int32_t tt_plan_contract(int32_t left, int32_t right, int32_t n, const int32_t *left_legs, const int32_t *right_legs,
                            int32_t has_charge, int64_t charge, tt_plan **out)
   {

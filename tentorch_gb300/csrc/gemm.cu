@@ -48,12 +48,12 @@ namespace ttg
     // of a few per SM (a matvec's stage has only ~10^5 multiply-adds per SM), each a tile over a
     // K range of at least 16, dealt to the SMs largest first, each to the least loaded (LPT).
     // Cost of an item: the 8 x 8 DMMA fragments it computes (fragments wholly outside the block are
-    // skipped) times its K range, plus per K step of 16 a quarter of a full tile's step (its loads
-    // and barriers) and per item the same again (claim, write or partial tile).
+    // skipped) times its K range, plus per staged K step (its copies and barriers) and per item
+    // (claim, write or partial tile) a quarter of a full tile over 16 of K.
     const auto cost = [bm, bn](double rows, double cols, double k)
     {
       const double frag = std::ceil(rows / 8.0) * 8.0 * std::ceil(cols / 8.0) * 8.0;
-      return frag * k + 0.25 * bm * bn * 16.0 * (std::ceil(k / 16.0) + 1.0);
+      return frag * k + 0.25 * bm * bn * 16.0 * (std::ceil(k / kDmmaStepK) + 1.0);
     };
     double total = 0;
     for (int64_t b = op.begin; b < op.begin + op.count; ++b)
@@ -333,6 +333,16 @@ namespace ttg
     // more items.
     __device__ __forceinline__ int64_t first_item(int worker) { return static_cast<int64_t>(worker) * gridDim.x + blockIdx.x; }
 
+    // 8-byte asynchronous copy global -> shared; `in` false fills the destination with zeros and
+    // reads nothing
+    __device__ __forceinline__ void copy8(double *dst, const double *src, bool in)
+    {
+      const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(in ? 8 : 0) : "memory");
+    }
+    __device__ __forceinline__ void copy_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+    __device__ __forceinline__ void copy_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
     // The next entry of the CTA's own list for a worker.
     __device__ __forceinline__ int64_t local_claim(int worker, int lt, int *slot, int *taken)
     {
@@ -528,14 +538,13 @@ namespace ttg
                        const GemmItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                        int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
     {
-      constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16;
+      constexpr int BM = kF64TileM, BN = kF64TileN, BK = kDmmaStepK;
       extern __shared__ __align__(16) unsigned char smem_raw[];
       const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
       // rows of 36 doubles: a warp's m8n8k4 fragment loads (k = lane % 4, row = lane / 4) then fall on
-      // distinct bank pairs within each half warp
+      // distinct bank pairs within each half warp.  Two stages of A (k-major) and B per worker.
       constexpr int P = 36;
-      double(*as)[P] = reinterpret_cast<double(*)[P]>(smem_raw + worker * 2 * BK * P * sizeof(double));
-      double(*bs)[P] = reinterpret_cast<double(*)[P]>(smem_raw + (worker * 2 + 1) * BK * P * sizeof(double));
+      double *stage_base = reinterpret_cast<double *>(smem_raw) + static_cast<size_t>(worker) * 2 * 2 * BK * P;
       __shared__ int flags[kF64Workers];
       const int warp = lt >> 5, lane = lt & 31;
       const int wm = warp >> 1, wn = warp & 1;
@@ -565,26 +574,46 @@ namespace ttg
           if (lo >= hi) continue;
           const double *a = A + pr.a;
           const double *b = B + pr.b;
-          for (int k0 = lo; k0 < hi; k0 += BK)
+          // K in steps of BK through two shared stages: the copies of step s + 1 (cp.async, entries
+          // outside the block or past hi filled with zeros) are in flight while step s computes
+          const auto load = [&](int stage, int k0)
           {
+            double *as = stage_base + stage * 2 * BK * P, *bs = as + BK * P;
             for (int i = lt; i < BM * BK; i += kWorkerThreads)
             {
               const int r = i / BK, kk = i % BK;
               const int gm = it.m0 + r, gk = k0 + kk;
-              as[kk][r] = (gm < blk.m && gk < hi) ? a[static_cast<int64_t>(gm) * K + gk] : 0.0;
+              const bool in = gm < blk.m && gk < hi;
+              copy8(as + kk * P + r, in ? a + static_cast<int64_t>(gm) * K + gk : a, in);
             }
             for (int i = lt; i < BK * BN; i += kWorkerThreads)
             {
               const int kk = i / BN, cc = i % BN;
               const int gk = k0 + kk, gn = it.n0 + cc;
-              bs[kk][cc] = (gk < hi && gn < blk.n) ? b[static_cast<int64_t>(gk) * blk.n + gn] : 0.0;
+              const bool in = gk < hi && gn < blk.n;
+              copy8(bs + kk * P + cc, in ? b + static_cast<int64_t>(gk) * blk.n + gn : b, in);
             }
+            copy_commit();
+          };
+          load(0, lo);
+          int stage = 0;
+          for (int k0 = lo; k0 < hi; k0 += BK, stage ^= 1)
+          {
+            if (k0 + BK < hi)
+              load(stage ^ 1, k0 + BK);
+            else
+              copy_commit();  // an empty group keeps the count of the wait below
+            copy_wait_one();
             worker_sync(worker);
+            const double(*as)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P);
+            const double(*bs)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P + BK * P);
+            const int steps = min(BK, hi - k0);
             if (live_i[0] && live_j[0])  // the warp's 16 x 16 quarter touches the block
             {
 #pragma unroll
               for (int kb = 0; kb < BK; kb += 4)
               {
+                if (kb >= steps) break;
                 double af[2], bf[2];
 #pragma unroll
                 for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
@@ -953,7 +982,7 @@ namespace ttg
     }
     else
     {
-      const int bytes = std::max<int>(kF64Workers * 2 * 16 * 36 * 8, kPinBytes);
+      const int bytes = std::max<int>(kF64Workers * 2 * 2 * kDmmaStepK * 36 * 8, kPinBytes);
       static std::once_flag once;
       if ((e = configure(gemm_dmma_kernel, bytes, once)) != cudaSuccess) return e;
       gemm_dmma_kernel<<<grid, workers * kWorkerThreads, bytes, stream>>>(

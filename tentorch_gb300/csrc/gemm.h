@@ -75,6 +75,7 @@ namespace ttg
 
   // Tile sizes of the two kernels.
   constexpr int kF64TileM = 32, kF64TileN = 32;
+  constexpr int kDmmaStepK = 32;  // K staged per step (two stages in flight) in the DMMA kernel
   constexpr int kSplitTileM = 32, kSplitTileN = 32, kSplitStepK = 32;
   // Persistent launches: one CTA per SM (held there by its shared memory), several workers of 128
   // threads per CTA taking items round robin.

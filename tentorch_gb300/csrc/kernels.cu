@@ -106,7 +106,10 @@ namespace ttg
     // One chunk of a tile per CTA: a warp per output row, the row's part of the input offset
     // computed once by its warp and the columns' part per entry (mixed radix over the copies of
     // the output domain legs, the last fastest).  Writes are coalesced along the columns.
-    template <typename T>
+    __device__ __forceinline__ double conj_of(double x) { return x; }
+    __device__ __forceinline__ double2 conj_of(double2 x) { return make_double2(x.x, -x.y); }
+
+    template <typename T, bool Conj>
     __global__ void __launch_bounds__(256) tiles_kernel(const T *__restrict__ src, T *__restrict__ dst,
                                                         const Tile *__restrict__ tiles,
                                                         const TileChunk *__restrict__ chunks)
@@ -142,7 +145,7 @@ namespace ttg
             in += static_cast<int64_t>(rc % e) * t.stride[l];
             rc /= e;
           }
-          out[c] = src[in];
+          out[c] = Conj ? conj_of(src[in]) : src[in];
         }
       }
     }
@@ -265,11 +268,14 @@ namespace ttg
       case OpKind::tiles:
         if (op.count > 0)
         {
-          if (args.complex)
-            tiles_kernel<double2><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
+          if (args.complex && (op.flags & 1))
+            tiles_kernel<double2, true><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
+              reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst), t.tiles, t.tile_chunks + op.begin);
+          else if (args.complex)
+            tiles_kernel<double2, false><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
               reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst), t.tiles, t.tile_chunks + op.begin);
           else
-            tiles_kernel<double><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
+            tiles_kernel<double, false><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
               reinterpret_cast<const double *>(src), reinterpret_cast<double *>(dst), t.tiles, t.tile_chunks + op.begin);
           e = check_launch();
         }

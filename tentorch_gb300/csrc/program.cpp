@@ -23,6 +23,7 @@ namespace ttg
     {
       std::vector<Tile> tiles;
       int64_t covered = 0;
+      bool conj = false;  // conjugate the values on the way
     };
 
     struct Value
@@ -77,6 +78,7 @@ namespace ttg
           }
           p_.tiles.insert(p_.tiles.end(), v.tiled->tiles.begin(), v.tiled->tiles.end());
           op.count = static_cast<int64_t>(p_.tile_chunks.size()) - op.begin;
+          op.flags = v.tiled->conj ? 1 : 0;
           p_.moved_elements += v.tiled->covered;
           if (op.count > 0) emit(op);
           return Value{dst, v.space, nullptr, v.phase};
@@ -894,6 +896,55 @@ namespace ttg
 
     constexpr int64_t kMaxCharges = 4096;
   } // namespace
+
+  std::shared_ptr<Program> compile_conj(Space space)
+  {
+    const Category &cat = *space->cat;
+    Space out = make_space(space->cat, space->domain, space->codomain, cat.dual(space->qtotal));
+    auto p = std::make_shared<Program>();
+    p->n_inputs = 1;
+    p->input_spaces = {space};
+    Builder b(*p);
+    Value v = b.input(0, space);
+    v.phase = -1;
+    auto map = std::make_shared<TileMap>();
+    map->conj = true;
+    for (const Block &ob : out->blocks)
+      if ((ob.rows * ob.cols) & 1)
+      {
+        Tile t{};
+        t.in_base = -1;
+        t.out_base = ob.offset + ob.rows * ob.cols;
+        t.out_ld = 1;
+        t.rows = t.cols = 1;
+        map->tiles.push_back(t);
+        ++map->covered;
+      }
+    for (const Block &blk : space->blocks)
+    {
+      if (blk.rows == 0 || blk.cols == 0) continue;
+      const int32_t at = out->find(BlockKey{blk.key.domain, blk.key.codomain, blk.key.copy});
+      if (at < 0) throw LogicError("a conjugate block lands outside the conjugate space");
+      const Block &ob = out->blocks[static_cast<size_t>(at)];
+      // out[c][r] = conj(in[r][c]): rows of the tile run over the input's columns, columns over its rows
+      Tile t{};
+      t.in_base = blk.offset;
+      t.out_base = ob.offset;
+      t.out_ld = static_cast<int32_t>(ob.cols);
+      t.rows = static_cast<int32_t>(blk.cols);
+      t.cols = static_cast<int32_t>(blk.rows);
+      t.n_row = 1;
+      t.n_col = 1;
+      t.extent[0] = static_cast<int32_t>(blk.cols);
+      t.stride[0] = 1;
+      t.extent[1] = static_cast<int32_t>(blk.rows);
+      t.stride[1] = blk.cols;
+      map->tiles.push_back(t);
+      map->covered += blk.rows * blk.cols;
+    }
+    finish(*p, b, {Value{v.buffer, out, nullptr, -1, map}});
+    return p;
+  }
 
   std::shared_ptr<Program> compile_place(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
   {

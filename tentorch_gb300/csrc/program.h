@@ -49,6 +49,7 @@ namespace ttg
     int64_t begin = 0, count = 0;  // range in the op's descriptor table
     int64_t elements = 0;          // destination elements (zero/add/copy/gather)
     int32_t phase = -1;            // operand whose prepare phase this belongs to, -1 for the core
+    int32_t flags = 0;             // tiles: 1 = conjugate the values (complex arenas)
   };
 
   // One destination run of a RUNS pass, already cut to at most kChunk elements.
@@ -141,6 +142,11 @@ namespace ttg
     int64_t moved_elements = 0;
     bool complex_coefficients = false;  // some RUNS term has an imaginary part
   };
+
+  // Compile the conjugate-transpose of a tensor (its bra): every block (r, s, c) becomes block
+  // (s, r, c) of the space with codomain and domain swapped and the dual charge, transposed and,
+  // for complex arenas, conjugated (tentorch/tensors/tensor.cpp:99-107).
+  std::shared_ptr<Program> compile_conj(Space space);
 
   // Compile one leg move of an arena of `space` into `above` / `below`.
   std::shared_ptr<Program> compile_place(Space space, const std::vector<int32_t> &above,

@@ -201,6 +201,12 @@ def place(tensor: Tensor, above, below = None) -> Tensor:
     return run(plan, [tensor], reuse_prepared = False)
 
 
+def conj(tensor: Tensor) -> Tensor:
+    '''tentorch/tensors/tensor.cpp:99-107: the bra of a tensor, one compiled pass.'''
+    plan = _plan(('conj', tensor._space.id), lambda out: lib.tt_plan_conj(tensor._space.id, out), tensor.cat)
+    return run(plan, [tensor], reuse_prepared = False)
+
+
 def contract(left: Tensor, right: Tensor, left_legs, right_legs, charge = None) -> Tensor:
     '''tentorch/linalg/graded/contract.cpp:117-175'''
     if left.cat is not right.cat:

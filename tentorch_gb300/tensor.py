@@ -188,7 +188,11 @@ class Tensor:
         return Tensor._wrap(self._space, self._data.clone())
 
     def conj(self) -> 'Tensor':
-        '''tentorch/tensors/tensor.cpp:99-107: the bra, blocks conjugate-transposed.'''
+        '''tentorch/tensors/tensor.cpp:99-107: the bra, blocks conjugate-transposed (one compiled
+        pass on the GPU; block by block for a host container).'''
+        if self.device.type == 'cuda':
+            from tentorch_gb300.linalg import conj
+            return conj(self)
         cat = self.cat
         out = Tensor(cat, self.domain, self.codomain, cat.dual(self.qtotal), self.dtype, self.device)
         for i, (r, s, c) in enumerate(self._space.keys):

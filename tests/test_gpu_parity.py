@@ -170,3 +170,20 @@ def test_device_dot_products(dtype):
     got = torch.complex(out[0::2], out[1::2]).cpu()
     want = torch.stack([torch.vdot(a, b) for a in arenas]).to(torch.complex128).cpu()
     assert torch.allclose(got, want, rtol = 1e-12, atol = 1e-10)
+
+
+@pytest.mark.parametrize('catname', ['u1', 'su2', 'fibonacci'])
+def test_conjugate_transpose_is_the_blockwise_one(catname):
+    '''tentorch/tensors/tensor.cpp:99-107: the compiled bra (one tiles pass) against the block-by-block
+    conjugate transpose on the host container.'''
+    cases = load_json('cases.json')
+    entry = next(e for c in cases for e in c['inputs'] if case_category(e['name']) == catname)
+    cat = PRODUCT_CATS[catname]
+    dtype = torch.complex128 if catname == 'fibonacci' else torch.float64
+    t = fixture_tensor(entry, cat, dtype)
+    if dtype == torch.complex128:
+        t.data.mul_(torch.exp(1j * torch.arange(t.data.numel(), dtype = torch.float64, device = 'cuda')))
+    got = t.conj()
+    want = t.to(device = 'cpu').conj()
+    assert got._space is want._space
+    assert torch.equal(got.data.cpu(), want.data)
