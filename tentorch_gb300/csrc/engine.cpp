@@ -475,12 +475,22 @@ namespace ttg
     // partial fusions there are) and one backward (those that reach the root).
     std::vector<std::set<Sector>> alive(n + 1);
     {
-      std::vector<std::set<Sector>> reach(n + 1);
-      reach[1].insert(legs[0]->sectors.begin(), legs[0]->sectors.end());
-      for (size_t k = 1; k < n; ++k)
-        for (const Sector &x : reach[k])
-          for (const Sector &s : legs[k]->sectors)
-            for (const Outcome &o : cat.outcomes(x, s)) reach[k + 1].insert(o.sector);
+      // the partial fusions after each leg depend on the legs only: kept per list of legs
+      static std::map<std::pair<const Category *, std::vector<int32_t>>, std::vector<std::set<Sector>>> reaches;
+      std::vector<int32_t> ids;
+      for (Leg l : legs) ids.push_back(l->id);
+      auto found = reaches.find({&cat, ids});
+      if (found == reaches.end())
+      {
+        std::vector<std::set<Sector>> r(n + 1);
+        r[1].insert(legs[0]->sectors.begin(), legs[0]->sectors.end());
+        for (size_t k = 1; k < n; ++k)
+          for (const Sector &x : r[k])
+            for (const Sector &s : legs[k]->sectors)
+              for (const Outcome &o : cat.outcomes(x, s)) r[k + 1].insert(o.sector);
+        found = reaches.emplace(std::make_pair(&cat, std::move(ids)), std::move(r)).first;
+      }
+      const std::vector<std::set<Sector>> &reach = found->second;
       if (reach[n].count(coupled)) alive[n].insert(coupled);
       for (size_t k = n - 1; k >= 1; --k)
         for (const Sector &x : reach[k])

@@ -61,6 +61,11 @@ namespace ttg
     };
     struct SplitTables
     {
+      bool ready = false;      // built on the op's first split launch, in an allocation of its own
+      void *base = nullptr;
+      int32_t *cta_begin = nullptr;  // per CTA, the start of its list of items (n_ctas + 1 entries)
+      int32_t n_ctas = 0;
+      int64_t longest = 0;
       void *items = nullptr, *pairs = nullptr, *lines = nullptr;
       GemmReduce *reduces = nullptr;
       int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0, slice_a = 0, slice_b = 0, exps = 0, slots = 0;

@@ -146,10 +146,10 @@ namespace ttg
     }
   }
 
-  SplitSchedule schedule_split(const Program &p, const Op &op)
+  SplitSchedule schedule_split(const Program &p, const Op &op, bool full)
   {
     SplitSchedule s;
-    s.pairs.assign(p.gemm_pairs.size(), SplitPair{0, 0, 0, 0, 0, 0});
+    if (full) s.pairs.assign(p.gemm_pairs.size(), SplitPair{0, 0, 0, 0, 0, 0});
     // slices: every distinct left block as rows of K padded to 32, every distinct right block
     // transposed the same way; exponents: one per row of A, one per column of B
     std::map<int64_t, std::pair<int64_t, int32_t>> a_at, b_at;  // arena offset -> (slice offset, exponent base)
@@ -167,7 +167,7 @@ namespace ttg
         if (fa == a_at.end())
         {
           fa = a_at.emplace(pr.a, std::make_pair(s.slice_a, static_cast<int32_t>(s.exps))).first;
-          for (int32_t r = 0; r < blk.m; ++r)
+          for (int32_t r = 0; full && r < blk.m; ++r)
             s.lines.push_back({pr.a + static_cast<int64_t>(r) * pr.k, s.slice_a + r * kp, pr.k, 1, static_cast<int32_t>(kp),
                                static_cast<int32_t>(s.exps + r)});
           s.slice_a += (blk.m * kp + 63) / 64 * 64;
@@ -177,14 +177,15 @@ namespace ttg
         if (fb == b_at.end())
         {
           fb = b_at.emplace(pr.b, std::make_pair(s.slice_b, static_cast<int32_t>(s.exps))).first;
-          for (int32_t c = 0; c < blk.n; ++c)
+          for (int32_t c = 0; full && c < blk.n; ++c)
             b_lines.push_back({pr.b + c, s.slice_b + c * kp, pr.k, blk.n, static_cast<int32_t>(kp),
                                static_cast<int32_t>(s.exps + c)});
           s.slice_b += (blk.n * kp + 63) / 64 * 64;
           s.exps += blk.n;
         }
-        s.pairs[pi] = SplitPair{fa->second.first, fb->second.first, static_cast<int32_t>(kp), fa->second.second,
-                                fb->second.second, 0};
+        if (full)
+          s.pairs[pi] = SplitPair{fa->second.first, fb->second.first, static_cast<int32_t>(kp), fa->second.second,
+                                  fb->second.second, 0};
       }
     }
     s.lines_a = static_cast<int64_t>(s.lines.size());
@@ -206,6 +207,10 @@ namespace ttg
         for (int32_t n0 = 0; n0 < blk.n; n0 += kSplitTileN)
         {
           const double rows = std::min(kSplitTileM, blk.m - m0), cols = std::min(kSplitTileN, blk.n - n0);
+          // a warp's 16 x 16 quarter outside the block skips its products
+          const double quarters = std::ceil(rows / 16.0) * std::ceil(cols / 16.0);
+          const auto cost = [quarters](double k)
+          { return quarters * 256.0 * (std::ceil(k / kSplitStepK) * kSplitStepK + 2.0 * kSplitStepK * (std::ceil(k / kExactChunk) + 1.0)); };
           tile.clear();
           for (int32_t k = 0; k < blk.pair_count; ++k)
           {
@@ -219,16 +224,18 @@ namespace ttg
             {
               const int64_t k0 = c * kc, k1 = std::min<int64_t>(K, (c + 1) * kc);
               tile.push_back({{static_cast<int32_t>(bi), m0, n0, pi, static_cast<int32_t>(k0), static_cast<int32_t>(k1), 0, -1},
-                              rows * cols * static_cast<double>(k1 - k0)});
+                              cost(static_cast<double>(k1 - k0))});
             }
           }
           if (tile.size() == 1)
           {
             tile[0].item.slot = -1;
-            items.push_back(tile[0]);
+            if (full) items.push_back(tile[0]);
           }
           else if (tile.empty())
-            items.push_back({{static_cast<int32_t>(bi), m0, n0, -1, 0, 0, -1, -1}, 0.0});  // no pair: zeros
+          {
+            if (full) items.push_back({{static_cast<int32_t>(bi), m0, n0, -1, 0, 0, -1, -1}, cost(0.0)});  // no pair: zeros
+          }
           else
           {
             const int32_t slot0 = static_cast<int32_t>(s.slots), reduce = static_cast<int32_t>(s.reduces.size());
@@ -236,14 +243,36 @@ namespace ttg
             {
               t.item.slot = static_cast<int32_t>(s.slots++);
               t.item.reduce = reduce;
-              items.push_back(t);
+              if (full) items.push_back(t);
             }
             s.reduces.push_back({static_cast<int32_t>(bi), m0, n0, slot0, static_cast<int32_t>(tile.size()), 0});
           }
         }
     }
+    if (!full) return s;
     std::stable_sort(items.begin(), items.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
-    for (const Sized &it : items) s.items.push_back(it.item);
+    // dealt to the SMs like the FP64 items (largest first onto the least loaded)
+    const int ctas = static_cast<int>(std::min<size_t>(kScheduleCtas, std::max<size_t>(items.size(), 1)));
+    std::vector<std::vector<SplitItem>> lists(static_cast<size_t>(ctas));
+    std::vector<std::pair<double, int>> heap;
+    for (int c = 0; c < ctas; ++c) heap.push_back({0.0, c});
+    const auto later = [](const std::pair<double, int> &a, const std::pair<double, int> &b)
+    { return a.first > b.first || (a.first == b.first && a.second > b.second); };
+    std::make_heap(heap.begin(), heap.end(), later);
+    for (const Sized &it : items)
+    {
+      std::pop_heap(heap.begin(), heap.end(), later);
+      auto &least = heap.back();
+      lists[static_cast<size_t>(least.second)].push_back(it.item);
+      least.first += it.work;
+      std::push_heap(heap.begin(), heap.end(), later);
+    }
+    s.cta_begin.push_back(0);
+    for (const auto &list : lists)
+    {
+      s.items.insert(s.items.end(), list.begin(), list.end());
+      s.cta_begin.push_back(static_cast<int32_t>(s.items.size()));
+    }
     return s;
   }
 
@@ -273,9 +302,10 @@ namespace ttg
       const Op &op = p.ops[i];
       if (op.kind != OpKind::gemm) continue;
       plans->f64[i] = schedule_gemm(p, op, kF64TileM, kF64TileN);
-      plans->split[i] = schedule_split(p, op);
+      // the split schedule itself is built on the first split launch (most plans never run one);
+      // here only its scratch
       need = std::max(need, (f64_bytes(plans->f64[i]) + 7) / 8);
-      need = std::max(need, (split_bytes(plans->split[i], kMaxSlices) + 7) / 8);
+      need = std::max(need, (split_bytes(schedule_split(p, op, false), kMaxSlices) + 7) / 8);
     }
     p.gemm_plans = std::move(plans);
     return need;
@@ -326,13 +356,6 @@ namespace ttg
       asm volatile("bar.sync %0, %1;\n" ::"r"(worker + 1), "r"(kWorkerThreads) : "memory");
     }
 
-    // A worker's first item is fixed, round robin over the SMs first (worker w of CTA b takes item
-    // w * grid + b): the workers of one SM share its FP64 pipe, so the opening items have to spread
-    // over every SM before any SM gets a second one.  After that each worker draws from the launch's
-    // counter (the word after the tile tickets, zeroed before the launch), so faster SMs simply take
-    // more items.
-    __device__ __forceinline__ int64_t first_item(int worker) { return static_cast<int64_t>(worker) * gridDim.x + blockIdx.x; }
-
     // 8-byte asynchronous copy global -> shared; `in` false fills the destination with zeros and
     // reads nothing
     __device__ __forceinline__ void copy8(double *dst, const double *src, bool in)
@@ -349,15 +372,6 @@ namespace ttg
       if (lt == 0) *slot = atomicAdd(taken, 1);
       worker_sync(worker);
       const int64_t idx = *slot;
-      worker_sync(worker);
-      return idx;
-    }
-
-    __device__ __forceinline__ int64_t claim(int worker, int lt, int *slot, int *counter)
-    {
-      if (lt == 0) *slot = atomicAdd(counter, 1);
-      worker_sync(worker);
-      const int64_t idx = *slot + static_cast<int64_t>(gridDim.x) * (blockDim.x / kWorkerThreads);
       worker_sync(worker);
       return idx;
     }
@@ -773,7 +787,7 @@ namespace ttg
       gemm_split_kernel(const uint16_t *__restrict__ sa_all, const uint16_t *__restrict__ sb_all,
                         const int16_t *__restrict__ exps, int64_t stride_a, int64_t stride_b, double *__restrict__ C,
                         const DevBlock *__restrict__ blocks, const DevSplitPair *__restrict__ spairs,
-                        const SplitItem *__restrict__ items, int64_t n_items, const GemmReduce *__restrict__ reduces,
+                        const SplitItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                         int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
     {
       extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -785,13 +799,19 @@ namespace ttg
       const int g = lane >> 2, tig = lane & 3;
       const int wm = warp >> 1, wn = warp & 1;
       __shared__ int next[kSplitWorkers];
-      int *counter = tickets + n_reduces;
-      for (int64_t idx = first_item(worker); idx < n_items; idx = claim(worker, lt, next + worker, counter))
+      __shared__ int taken;
+      if (threadIdx.x == 0) taken = 0;
+      __syncthreads();
+      const int64_t list_begin = cta_begin[blockIdx.x], list_end = cta_begin[blockIdx.x + 1];
+      for (int64_t idx = list_begin + local_claim(worker, lt, next + worker, &taken); idx < list_end;
+           idx = list_begin + local_claim(worker, lt, next + worker, &taken))
       {
         const SplitItem it = items[idx];
         const DevBlock blk = blocks[it.block];
         double acc[2][4] = {};
         const int r0 = it.m0 + wm * 16 + g, c0 = it.n0 + wn * 16 + tig * 2;
+        // the warp's 16 x 16 quarter of the tile touches the block (warp-uniform)
+        const bool live = it.m0 + wm * 16 < blk.m && it.n0 + wn * 16 < blk.n;
         if (it.pair >= 0 && it.k1 > it.k0)
         {
           const DevSplitPair sp = spairs[it.pair];
@@ -844,6 +864,7 @@ namespace ttg
 #pragma unroll
             for (int kk = 0; kk < kSplitStepK; kk += 16)
             {
+              if (!live) break;
               uint32_t af[S][4], bf[S][4];
 #pragma unroll
               for (int t = 0; t < S; ++t)
@@ -935,17 +956,18 @@ namespace ttg
     template <int S>
     cudaError_t launch_split_s(const uint16_t *sa, const uint16_t *sb, const int16_t *exps, int64_t stride_a,
                                int64_t stride_b, double *C, const DevBlock *blocks, const DevSplitPair *spairs,
-                               const SplitItem *items, int64_t n_items, const GemmReduce *reduces, int64_t n_reduces,
-                               double *partial, int *tickets, cudaStream_t stream)
+                               const SplitItem *items, const int32_t *cta_begin, int32_t n_ctas, int64_t longest,
+                               const GemmReduce *reduces, int64_t n_reduces, double *partial, int *tickets,
+                               cudaStream_t stream)
     {
       const int bytes = std::max(kSplitWorkers * split_worker_bytes<S>(), kPinBytes);
       static std::once_flag once;
       cudaError_t e = configure(gemm_split_kernel<S>, bytes, once);
       if (e != cudaSuccess) return e;
-      const int grid = static_cast<int>(std::min<int64_t>(sm_count(), n_items));
-      const int workers = static_cast<int>(std::clamp<int64_t>((n_items + grid - 1) / grid, 1, kSplitWorkers));
-      gemm_split_kernel<S><<<grid, workers * kWorkerThreads, bytes, stream>>>(
-        sa, sb, exps, stride_a, stride_b, C, blocks, spairs, items, n_items, reduces, n_reduces, partial, tickets);
+      // one CTA per list the schedule dealt, as many workers as its longest list needs
+      const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kSplitWorkers));
+      gemm_split_kernel<S><<<n_ctas, workers * kWorkerThreads, bytes, stream>>>(
+        sa, sb, exps, stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets);
       return cudaGetLastError();
     }
   } // namespace
@@ -995,8 +1017,35 @@ namespace ttg
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream)
   {
-    (void)p;
-    (void)op;
+    {
+      std::lock_guard<std::mutex> lock(t.mutex);
+      DeviceTables::SplitTables &dst = t.split[op_index];
+      if (!dst.ready)
+      {
+        const SplitSchedule s = schedule_split(p, op, true);
+        dst.n_items = static_cast<int64_t>(s.items.size());
+        dst.n_reduces = static_cast<int64_t>(s.reduces.size());
+        dst.n_lines_a = s.lines_a;
+        dst.n_lines_b = static_cast<int64_t>(s.lines.size()) - s.lines_a;
+        dst.slice_a = s.slice_a;
+        dst.slice_b = s.slice_b;
+        dst.exps = s.exps;
+        dst.slots = s.slots;
+        dst.n_ctas = static_cast<int32_t>(s.cta_begin.size()) - 1;
+        dst.longest = 0;
+        for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c)
+          dst.longest = std::max<int64_t>(dst.longest, s.cta_begin[c + 1] - s.cta_begin[c]);
+        TableStaging staging;
+        staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
+        staging.add(s.items, &dst.items);
+        staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
+        staging.add(s.pairs, &dst.pairs);
+        staging.add(s.lines, &dst.lines);
+        const cudaError_t e = staging.commit(&dst.base);
+        if (e != cudaSuccess) return e;
+        dst.ready = true;
+      }
+    }
     const auto &sched = t.split[op_index];
     if (sched.n_items == 0) return cudaSuccess;
     char *base = static_cast<char *>(scratch);
@@ -1025,8 +1074,8 @@ namespace ttg
     {
 #define TTG_SPLIT(S)                                                                                                    \
   case S:                                                                                                               \
-    e = launch_split_s<S>(sa, sb, exps, sched.slice_a, sched.slice_b, C, blocks, spairs, items, sched.n_items,          \
-                          sched.reduces, sched.n_reduces, partial, tickets, stream);                                   \
+    e = launch_split_s<S>(sa, sb, exps, sched.slice_a, sched.slice_b, C, blocks, spairs, items, sched.cta_begin,       \
+                          sched.n_ctas, sched.longest, sched.reduces, sched.n_reduces, partial, tickets, stream);                                   \
     break;
       TTG_SPLIT(1) TTG_SPLIT(2) TTG_SPLIT(3) TTG_SPLIT(4) TTG_SPLIT(5) TTG_SPLIT(6) TTG_SPLIT(7) TTG_SPLIT(8)
 #undef TTG_SPLIT
@@ -1059,20 +1108,6 @@ namespace ttg
         staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
         staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
       }
-      const SplitSchedule &s = p.gemm_plans->split[i];
-      DeviceTables::SplitTables &dst = t.split[i];
-      dst.n_items = static_cast<int64_t>(s.items.size());
-      dst.n_reduces = static_cast<int64_t>(s.reduces.size());
-      dst.n_lines_a = s.lines_a;
-      dst.n_lines_b = static_cast<int64_t>(s.lines.size()) - s.lines_a;
-      dst.slice_a = s.slice_a;
-      dst.slice_b = s.slice_b;
-      dst.exps = s.exps;
-      dst.slots = s.slots;
-      staging.add(s.items, &dst.items);
-      staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
-      staging.add(s.pairs, &dst.pairs);
-      staging.add(s.lines, &dst.lines);
     }
   }
 

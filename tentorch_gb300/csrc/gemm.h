@@ -70,8 +70,11 @@ namespace ttg
     int64_t slice_a = 0, slice_b = 0;  // elements of one slice of all A (B) rows
     int64_t exps = 0;                  // int16 exponents
     int64_t slots = 0;
+    std::vector<int32_t> cta_begin;    // CTA b runs items [cta_begin[b], cta_begin[b + 1])
   };
-  SplitSchedule schedule_split(const Program &p, const Op &op);
+  // The split-precision schedule of a GEMM op; with full = false only its sizes (slices, exponents,
+  // partial slots, reductions), for sizing the scratch without building its tables.
+  SplitSchedule schedule_split(const Program &p, const Op &op, bool full = true);
 
   // Tile sizes of the two kernels.
   constexpr int kF64TileM = 32, kF64TileN = 32;

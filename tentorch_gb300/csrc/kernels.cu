@@ -167,6 +167,8 @@ namespace ttg
   DeviceTables::~DeviceTables()
   {
     if (base) cudaFree(base);
+    for (SplitTables &g : split)
+      if (g.base) cudaFree(g.base);
   }
 
   cudaError_t TableStaging::commit(void **base)
