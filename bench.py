@@ -8,9 +8,13 @@ physical d = 2, theta in the Sz = 0 sector), inputs N(0, 1) float64 from a seed.
 A step is one matvec through the public API, with the operator (head, tail) prepared once as a
 Lanczos window uses it and a different resident vector every step.  L2 (129 MB) is flushed between
 timed steps by writing a 256 MB buffer, and each step is timed alone with CUDA events on the
-launching stream.  Prints ONE JSON line (rank 0).
+launching stream.  The headline form is split precision (6 bf16 slices by default); the same loop
+times the grouped FP64 form and the per-block FP64 form (one cuBLAS call per block pair) on the same
+inputs.  The DMRG section times one sweep of the L = 64, chi = 256, n_iter = 10 Heisenberg chain in
+each form from one FP64 state, with the energy differences.  Prints ONE JSON line (rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P] [--impl reference]
+                    [--dmrg-length L] [--workload matvec|svd]
 
 --impl reference times the reference's CPU path for the same workload on the host cores: the
 oracle port of tentorch's einsum (oracle/engine.py), a bounded sample of matvecs.  With N > 1 (one
@@ -43,13 +47,16 @@ def parse():
     p.add_argument('--steps', type = int, default = 1000)
     p.add_argument('--warmup', type = int, default = 10)
     p.add_argument('--impl', default = 'gb300', choices = ['gb300', 'reference'])
-    p.add_argument('--precision', type = int, default = 8,
-                   help = 'the headline form: k bf16 slices (1..8) or 0 for FP64 block products')
+    p.add_argument('--precision', type = int, default = 6,
+                   help = 'the headline form: k bf16 slices (1..8) or 0 for FP64 block products; 6 slices give '
+                          '1.4e-12 relative on the matvec and |dE| ~ 7e-12 over a sweep')
     p.add_argument('--chi', type = int, default = CHI)
     p.add_argument('--cpu-sample', type = int, default = 20, help = 'matvecs in the CPU baseline sample')
     p.add_argument('--dmrg-length', type = int, default = 64, help = 'chain of the DMRG sweep timing (0: skip)')
     p.add_argument('--dmrg-iter', type = int, default = 10, help = 'Lanczos steps per window in the DMRG timing')
     p.add_argument('--dmrg-warm', type = int, default = 2, help = 'FP64 sweeps before the timed sweeps')
+    p.add_argument('--workload', default = 'matvec', choices = ['matvec', 'svd'],
+                   help = 'matvec: the headline line; svd: time the truncating split of a two-site tensor')
     return p.parse_args()
 
 
@@ -436,8 +443,42 @@ def run_gpu(args, rank, world):
         print(json.dumps(line), flush = True)
 
 
+def run_splittings(args):
+    """Time the truncating split of a chi-sized two-site tensor (the SVD of every window of a DMRG
+    sweep): [bond, phys] -> [phys, bond] with the bond of the matvec workload, seeded N(0, 1) blocks,
+    `tg.svd(t, chi, 1e-14, 2)` per step (all blocks in one launch, the kept factors in a second).
+    Prints one line of its own (not the headline); also a driver for profiling the SVD kernels."""
+    import torch
+    import tentorch_gb300 as tg
+    from oracle import engine as orc
+    device = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(device)
+    qs, deg = orc.degeneracies(args.chi)
+    cat = tg.u1
+    bond = tg.Leg(cat, [(2 * q,) for q in qs], deg)
+    phys = tg.Leg(cat, [(1,), (-1,)], [1, 1])
+    t = tg.Tensor(cat, [bond, phys], [phys, bond], (0,), dtype = torch.float64, device = device)
+    gen = torch.Generator().manual_seed(SEED)
+    for block in t.to_tuple()[3].values():
+        block.copy_(torch.randn(block.shape, dtype = torch.float64, generator = gen))
+    for _ in range(args.warmup):
+        tg.svd(t, args.chi, 1e-14, 2)
+    torch.cuda.synchronize(device)
+    start = time.perf_counter()
+    for _ in range(args.steps):
+        tg.svd(t, args.chi, 1e-14, 2)
+    torch.cuda.synchronize(device)
+    elapsed = time.perf_counter() - start
+    shapes = sorted((r, c) for r, c in t._space.shapes)
+    print(json.dumps({'workload': f'u1_two_site_svd_chi{args.chi}', 'ms_per_split': 1e3 * elapsed / args.steps,
+                      'blocks': len(shapes), 'largest': shapes[-1], 'steps': args.steps}), flush = True)
+
+
 def main():
     args = parse()
+    if args.workload == 'svd':
+        run_splittings(args)
+        return
     rank, world = int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1))
     if world > 1:
         import torch.distributed as dist
