@@ -15,6 +15,7 @@
 
 #include "engine.h"
 #include "executor.h"
+#include "gemm.h"
 #include "program.h"
 
 struct tt_plan
@@ -411,6 +412,16 @@ extern "C"
         out += "op " + std::to_string(i) + " " + kinds[static_cast<int>(op.kind)] + " src " + std::to_string(op.src) +
                " src2 " + std::to_string(op.src2) + " dst " + std::to_string(op.dst) + " phase " + std::to_string(op.phase) +
                " elements " + std::to_string(op.elements) + " count " + std::to_string(op.count) + "\n";
+        if (op.kind == ttg::OpKind::gemm && p.gemm_plans && i < p.gemm_plans->f64.size())
+        {
+          // the FP64 schedule: items dealt to the SMs, K-split tiles and the longest list
+          const ttg::GemmSchedule &s = p.gemm_plans->f64[i];
+          int64_t longest = 0;
+          for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c) longest = std::max<int64_t>(longest, s.cta_begin[c + 1] - s.cta_begin[c]);
+          out += "  fp64 schedule: items " + std::to_string(s.items.size()) + " split tiles " + std::to_string(s.reduces.size()) +
+                 " partial slots " + std::to_string(s.slots) + " ctas " +
+                 std::to_string(s.cta_begin.empty() ? 0 : s.cta_begin.size() - 1) + " longest list " + std::to_string(longest) + "\n";
+        }
         if (op.kind == ttg::OpKind::gemm)
           for (int64_t b = op.begin; b < op.begin + op.count; ++b)
           {

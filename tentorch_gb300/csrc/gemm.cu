@@ -622,25 +622,31 @@ namespace ttg
             const double(*as)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P);
             const double(*bs)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P + BK * P);
             const int steps = min(BK, hi - k0);
+            // an 8 x 8 fragment wholly outside the block costs the FP64 pipe as much as a full one:
+            // skip it (warp-uniform); a full step runs unrolled with no bound, so the fragment loads
+            // of the next k are issued ahead of the products of this one
+            const auto step_k = [&](int kb)
+            {
+              double af[2], bf[2];
+#pragma unroll
+              for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
+#pragma unroll
+              for (int j = 0; j < 2; ++j) bf[j] = bs[kb + fk][wn * 16 + j * 8 + fr];
+#pragma unroll
+              for (int i = 0; i < 2; ++i)
+#pragma unroll
+                for (int j = 0; j < 2; ++j)
+                  if (live_i[i] && live_j[j]) dmma(acc[i][j], af[i], bf[j]);
+            };
             if (live_i[0] && live_j[0])  // the warp's 16 x 16 quarter touches the block
             {
-#pragma unroll
-              for (int kb = 0; kb < BK; kb += 4)
+              if (steps == BK)
               {
-                if (kb >= steps) break;
-                double af[2], bf[2];
 #pragma unroll
-                for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
-#pragma unroll
-                for (int j = 0; j < 2; ++j) bf[j] = bs[kb + fk][wn * 16 + j * 8 + fr];
-                // an 8 x 8 fragment wholly outside the block costs the FP64 pipe as much as a full
-                // one: skip it (warp-uniform)
-#pragma unroll
-                for (int i = 0; i < 2; ++i)
-#pragma unroll
-                  for (int j = 0; j < 2; ++j)
-                    if (live_i[i] && live_j[j]) dmma(acc[i][j], af[i], bf[j]);
+                for (int kb = 0; kb < BK; kb += 4) step_k(kb);
               }
+              else
+                for (int kb = 0; kb < steps; kb += 4) step_k(kb);
             }
             worker_sync(worker);
           }
@@ -676,6 +682,53 @@ namespace ttg
     // split precision
     // ---------------------------------------------------------------------------------------
 
+    // FP64 runs at a sixty-fourth of the FP32 rate on this GPU, so the slicing works on the bits of
+    // the doubles with integer instructions.
+    //
+    // frexp's exponent of a non-negative double given by its bits: x = f 2^e with f in [0.5, 1)
+    // (0 for zero).
+    __device__ __forceinline__ int frexp_exponent(unsigned long long bits)
+    {
+      if (bits == 0) return 0;
+      const int field = static_cast<int>(bits >> 52);
+      if (field != 0) return field - 1022;
+      return (64 - __clzll(static_cast<long long>(bits))) - 1074;  // subnormal: bits * 2^-1074
+    }
+
+    // __double2ll_rn(ldexp(x, k)) for |x| < 2^(63 - k) on the bits of x: the significand shifted by
+    // the exponent, rounded to nearest with ties to even.
+    __device__ __forceinline__ long long scaled_integer(double x, int k)
+    {
+      const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
+      const int field = static_cast<int>((bits >> 52) & 0x7ff);
+      unsigned long long mant = bits & 0xfffffffffffffull;
+      if (field != 0) mant |= 1ull << 52;
+      const int shift = (field != 0 ? field : 1) - 1075 + k;  // x 2^k = mant 2^shift
+      unsigned long long q;
+      if (mant == 0)
+        q = 0;
+      else if (shift >= 0)
+        q = mant << shift;
+      else if (shift < -62)
+        q = 0;
+      else
+      {
+        const int down = -shift;
+        q = mant >> down;
+        const unsigned long long rem = mant & ((1ull << down) - 1), half = 1ull << (down - 1);
+        if (rem > half || (rem == half && (q & 1ull))) ++q;
+      }
+      const long long v = static_cast<long long>(q);
+      return (bits >> 63) ? -v : v;
+    }
+
+    // 2^k as a double built from its bits (k in the normal range), else through ldexp
+    __device__ __forceinline__ double pow2(int k)
+    {
+      if (k > -1023 && k < 1024) return __longlong_as_double(static_cast<long long>(k + 1023) << 52);
+      return ldexp(1.0, k);
+    }
+
     // One warp per line (a row of A or a column of B), lines of A from `a` and lines of B from `b`:
     // the power of two 2^e that bounds the line, then each entry as the integer round(x 2^(56-e))
     // cut into `slices` balanced 7-bit digits (|q_1| <= 128, |q_t| <= 64 after it), exact in bf16,
@@ -695,22 +748,29 @@ namespace ttg
         const double *src = (left ? a : b) + line.src;
         uint16_t *dst = (left ? slices_a : slices_b) + line.dst;
         const int64_t stride = left ? stride_a : stride_b;
-        double big = 0.0;
+        // the largest |entry| by its bits (positive doubles order as integers), then its frexp
+        // exponent e: every |entry| < 2^e
+        unsigned long long big = 0;
         for (int i0 = 0; i0 < line.len; i0 += 256)
         {
-          double v[8];
+          unsigned long long v[8];
 #pragma unroll
           for (int u = 0; u < 8; ++u)
           {
             const int i = i0 + u * 32 + lane;
-            v[u] = i < line.len ? fabs(src[static_cast<int64_t>(i) * line.src_stride]) : 0.0;
+            v[u] = i < line.len ? (static_cast<unsigned long long>(__double_as_longlong(src[static_cast<int64_t>(i) * line.src_stride])) &
+                                   0x7fffffffffffffffull)
+                                : 0ull;
           }
 #pragma unroll
-          for (int u = 0; u < 8; ++u) big = fmax(big, v[u]);
+          for (int u = 0; u < 8; ++u) big = v[u] > big ? v[u] : big;
         }
-        for (int off = 16; off > 0; off >>= 1) big = fmax(big, __shfl_xor_sync(0xffffffffu, big, off));
-        int e = 0;
-        if (big > 0.0) frexp(big, &e);  // big = f 2^e with f in [0.5, 1): every |entry| / 2^e < 1
+        for (int off = 16; off > 0; off >>= 1)
+        {
+          const unsigned long long o = __shfl_xor_sync(0xffffffffu, big, off);
+          big = o > big ? o : big;
+        }
+        const int e = frexp_exponent(big);
         if (lane == 0) exps[line.exp] = static_cast<int16_t>(e);
         for (int i0 = 0; i0 < line.padded; i0 += 128)
         {
@@ -719,7 +779,7 @@ namespace ttg
           for (int u = 0; u < 4; ++u)
           {
             const int i = i0 + u * 32 + lane;
-            x[u] = i < line.len ? __double2ll_rn(ldexp(src[static_cast<int64_t>(i) * line.src_stride], 56 - e)) : 0ll;
+            x[u] = i < line.len ? scaled_integer(src[static_cast<int64_t>(i) * line.src_stride], 56 - e) : 0ll;
           }
 #pragma unroll
           for (int u = 0; u < 4; ++u)
@@ -738,7 +798,8 @@ namespace ttg
               }
               else
                 q = r;
-              dst[t * stride + i] = __bfloat16_as_ushort(__float2bfloat16_rn(static_cast<float>(q)));
+              // |q| <= 128: exact in bf16, converted through int32 and fp32
+              dst[t * stride + i] = __bfloat16_as_ushort(__float2bfloat16_rn(__int2float_rn(static_cast<int>(q))));
             }
           }
         }
@@ -836,6 +897,8 @@ namespace ttg
             cp_async_commit();
           };
           const int steps = (it.k1 - it.k0 + kSplitStepK - 1) / kSplitStepK;
+          long long acc_int[2][4] = {};
+          float acc_tail[2][4] = {};
           float lev[S][2][4];
 #pragma unroll
           for (int l = 0; l < S; ++l)
@@ -885,6 +948,8 @@ namespace ttg
             worker_sync(worker);
             if ((step + 1) % (kExactChunk / kSplitStepK) == 0 || step + 1 == steps)
             {
+              // the four leading levels are exact integers (below 2^24 over a chunk of <= 256 of K):
+              // combined exactly in int64 as sum_l lev_l 2^(7 (3 - l)); the rest in fp32
 #pragma unroll
               for (int ns = 0; ns < 2; ++ns)
 #pragma unroll
@@ -893,16 +958,27 @@ namespace ttg
                   float tail = 0.0f;
 #pragma unroll
                   for (int l = S - 1; l >= 4; --l) tail = fmaf(lev[l][ns][q], ldexpf(1.0f, -7 * (l - 4)), tail);
-                  double v = static_cast<double>(tail) * ldexp(1.0, -42);
+                  long long head = 0;
 #pragma unroll
-                  for (int l = (S < 4 ? S : 4) - 1; l >= 0; --l)
-                    v = fma(static_cast<double>(lev[l][ns][q]), ldexp(1.0, -7 * (l + 2)), v);
+                  for (int l = 0; l < 4; ++l)
+                    head = head * 128 + (l < S ? static_cast<long long>(__float2int_rn(lev[l][ns][q])) : 0ll);
+                  acc_int[ns][q] += head;
+                  acc_tail[ns][q] += tail;
 #pragma unroll
                   for (int l = 0; l < S; ++l) lev[l][ns][q] = 0.0f;
-                  acc[ns][q] = fma(v, ldexp(1.0, (q < 2 ? er0 : er1) + ec[ns][q & 1]), acc[ns][q]);
                 }
             }
           }
+          // one FP64 step per entry: head 2^-35 + tail 2^-42, times the row and column scales
+#pragma unroll
+          for (int ns = 0; ns < 2; ++ns)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+            {
+              const int ex = (q < 2 ? er0 : er1) + ec[ns][q & 1];
+              acc[ns][q] = fma(static_cast<double>(acc_int[ns][q]), pow2(ex - 35),
+                               static_cast<double>(acc_tail[ns][q]) * pow2(ex - 42));
+            }
         }
         if (it.slot >= 0)
         {
