@@ -176,7 +176,7 @@ def measured_peaks():
 
 
 def ncu_traffic(kernel):
-    '''Per-launch DRAM bytes of a kernel from the committed ncu summary, or None.'''
+    '''DRAM bytes of a kernel per matvec (its two launches) from the committed ncu summary, or None.'''
     path = os.path.join(HERE, 'profiles', 'traffic.json')
     if not os.path.exists(path):
         return None
