@@ -102,10 +102,26 @@ namespace ttg
     // One Jacobi phase over W (len x k, column-major) with the rotations accumulated into V (k x k).
     // FP32: everything in FP32.  FP64: the dot products, updates and norms in FP64, the angle in
     // FP32 made exactly orthogonal.  Returns the sweeps taken, -1 when kMaxSweeps did not do.
-    template <typename T>
+    template <typename T, int G>
+    __device__ __forceinline__ T group_sum(T v)
+    {
+#pragma unroll
+      for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+      return v;
+    }
+
+    // One Jacobi phase over W (len x k, column-major) with the rotations accumulated into V (k x k).
+    // FP32: everything in FP32.  FP64: the dot products, updates and norms in FP64, the angle in
+    // FP32 made exactly orthogonal.  A group of G lanes takes a pair (G = 8 for columns of up to 128
+    // entries, so a warp rotates four pairs at once and a dot product needs three shuffle steps, not
+    // five: FP64 instructions cost the same however few lanes they serve).  Returns the sweeps taken,
+    // -1 when kMaxSweeps did not do.
+    template <typename T, int G>
     __device__ int jacobi_phase(T *w, T *v, T *norms, int64_t len, int64_t k, double tol, int *rotated)
     {
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+      const int group = lane / G, gl = lane % G;
+      constexpr int per_warp = 32 / G;
       const int64_t players = k + (k & 1);  // a dummy column pairs with the odd one out
       const T tol2 = static_cast<T>(tol * tol);
       for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
@@ -123,10 +139,12 @@ namespace ttg
         __syncthreads();
         for (int64_t round = 0; round + 1 < players; ++round)
         {
-          for (int64_t t = warp; t < players / 2; t += warps)
+          // every group of the warp walks the same number of turns, so the shuffles stay converged
+          for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < players / 2; t0 += static_cast<int64_t>(warps) * per_warp)
           {
+            const int64_t t = t0 + group;
             // circle method: player players-1 stays, the others turn
-            int64_t p, q;
+            int64_t p = 0, q = 0;
             if (t == 0)
             {
               p = round;
@@ -143,44 +161,46 @@ namespace ttg
               q = p;
               p = lower;
             }
-            if (q >= k) continue;  // the dummy
-            T *wp = w + p * len, *wq = w + q * len;
+            const bool pair = t < players / 2 && q < k;  // not past the round, not the dummy
+            T *wp = w + (pair ? p : 0) * len, *wq = w + (pair ? q : 0) * len;
             T gamma = 0;
-            for (int64_t i = lane; i < len; i += 32) gamma = fma(wp[i], wq[i], gamma);
-            gamma = warp_sum(gamma);
+            if (pair)
+              for (int64_t i = gl; i < len; i += G) gamma = fma(wp[i], wq[i], gamma);
+            gamma = group_sum<T, G>(gamma);
+            if (!pair) continue;
             const T alpha = norms[p], beta = norms[q];
             // orthogonal to working precision: cos^2 of the pair's angle below tol^2
             if (gamma * gamma <= tol2 * alpha * beta) continue;
             float cf, sf;
             if (!angle(alpha, beta, gamma, cf, sf)) continue;
-            T c = cf, s = sf;
+            T c = cf, sn = sf;
             if (sizeof(T) == 8)
             {
               // c^2 + s^2 = 1 to FP64 precision: two Newton steps on 1 / sqrt(c^2 + s^2)
 #pragma unroll
               for (int it = 0; it < 2; ++it)
               {
-                const T f = static_cast<T>(1.5) - static_cast<T>(0.5) * fma(c, c, s * s);
+                const T f = static_cast<T>(1.5) - static_cast<T>(0.5) * fma(c, c, sn * sn);
                 c *= f;
-                s *= f;
+                sn *= f;
               }
             }
-            for (int64_t i = lane; i < len; i += 32)
+            for (int64_t i = gl; i < len; i += G)
             {
               const T x = wp[i], y = wq[i];
-              wp[i] = fma(c, x, -s * y);
-              wq[i] = fma(s, x, c * y);
+              wp[i] = fma(c, x, -sn * y);
+              wq[i] = fma(sn, x, c * y);
             }
             T *vp = v + p * k, *vq = v + q * k;
-            for (int64_t i = lane; i < k; i += 32)
+            for (int64_t i = gl; i < k; i += G)
             {
               const T x = vp[i], y = vq[i];
-              vp[i] = fma(c, x, -s * y);
-              vq[i] = fma(s, x, c * y);
+              vp[i] = fma(c, x, -sn * y);
+              vq[i] = fma(sn, x, c * y);
             }
-            if (lane == 0)
+            if (gl == 0)
             {
-              const T cc = c * c, ss = s * s, cs2 = 2 * c * s * gamma;
+              const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
               norms[p] = cc * alpha - cs2 + ss * beta;
               norms[q] = ss * alpha + cs2 + cc * beta;
               *rotated = 1;
@@ -193,6 +213,13 @@ namespace ttg
         if (!any) return sweep + 1;
       }
       return -1;
+    }
+
+    template <typename T>
+    __device__ int jacobi_phase(T *w, T *v, T *norms, int64_t len, int64_t k, double tol, int *rotated)
+    {
+      if (len <= 128) return jacobi_phase<T, 8>(w, v, norms, len, k, tol, rotated);
+      return jacobi_phase<T, 32>(w, v, norms, len, k, tol, rotated);
     }
 
     __global__ void __launch_bounds__(kSvdThreads, 1)
