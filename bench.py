@@ -39,6 +39,7 @@ METRIC = 'DMRG s/sweep & matvecs/s (U(1) χ=256) vs plain FP64 on same GPU at Δ
 WORKLOAD = 'u1_heisenberg_twosite_matvec_chi256'
 CHI = 256
 SEED = 0
+MATVEC = 'EPaqj,JRSFb,AQsb->EPrf'  # the two-site matvec (tentorch/algorithms/dmrg.py:118)
 
 
 def parse():
@@ -55,8 +56,9 @@ def parse():
     p.add_argument('--dmrg-length', type = int, default = 64, help = 'chain of the DMRG sweep timing (0: skip)')
     p.add_argument('--dmrg-iter', type = int, default = 10, help = 'Lanczos steps per window in the DMRG timing')
     p.add_argument('--dmrg-warm', type = int, default = 2, help = 'FP64 sweeps before the timed sweeps')
-    p.add_argument('--workload', default = 'matvec', choices = ['matvec', 'svd'],
-                   help = 'matvec: the headline line; svd: time the truncating split of a two-site tensor')
+    p.add_argument('--workload', default = 'matvec', choices = ['matvec', 'svd', 'recoupling', 'windows'],
+                   help = 'matvec: the headline line; svd: the truncating split of a two-site tensor; recoupling: '
+                          'the SU(2) / Fibonacci einsum; windows: 64 batched matvecs in a CUDA graph')
     return p.parse_args()
 
 
@@ -65,6 +67,58 @@ def config(args, precision):
             'equation': 'EPaqj,JRSFb,AQsb->EPrf', 'block_products': 'fp64' if precision == 0 else f'bf16x{precision} split',
             'l2': 'flushed between timed steps (256 MB write)', 'inputs': f'N(0,1) float64, seed {SEED}',
             'parallelism': f'replicas x{args.gpus}'}
+
+
+def bond_multiplicities(chi, qmax = 8):
+    """The bond of the matvec workload: U(1) charges 2q for q = -qmax..qmax, one multiplet each and
+    the rest apportioned proportional to exp(-q^2/8): floors first, the leftover in +-q pairs by
+    descending fractional part (ties to the smaller |q|), an odd leftover to q = 0.  Symmetric in q."""
+    qs = list(range(-qmax, qmax + 1))
+    weight = {q: math.exp(-q * q / 8) for q in qs}
+    share = {q: (chi - len(qs)) * weight[q] / sum(weight.values()) for q in qs}
+    mult = {q: 1 + int(share[q]) for q in qs}
+    left = chi - sum(mult.values())
+    for q in sorted(range(1, qmax + 1), key = lambda q: (int(share[q]) - share[q], q)):
+        if left >= 2:
+            mult[q] += 1
+            mult[-q] += 1
+            left -= 2
+    mult[0] += left
+    return [(2 * q,) for q in qs], [mult[q] for q in qs]
+
+
+def matvec_operands(tg, torch, device, chi, seed):
+    """One two-site window of the matvec workload on the device: environments L, R = (bond, w | bond)
+    and theta = (bond, phys | phys, bond) at the trivial charge, entries N(0, 1) float64 drawn in
+    block-key order from `torch.Generator().manual_seed(seed)` (L, then R, then theta), the bulk
+    site W of the Heisenberg MPO, and head = einsum('EIa,IPqj->EPaqj', L, W), tail =
+    einsum('JRsk,Fkb->JRSFb', W, R) as tentorch/algorithms/dmrg.py:113-114 builds them."""
+    cat = tg.u1
+    site = tg.heisenberg(cat, 4, dtype = torch.float64, device = device).tensors[1]
+    w, phys = site.codomain[0], site.codomain[1]
+    bond = tg.Leg(cat, *bond_multiplicities(chi))
+    gen = torch.Generator().manual_seed(seed)
+
+    def filled(cod, dom):
+        t = tg.Tensor(cat, cod, dom, (0,), dtype = torch.float64, device = device)
+        for block in t.to_tuple()[3].values():
+            block.copy_(torch.randn(block.shape, dtype = torch.float64, generator = gen))
+        return t
+    left, right = filled([bond, w], [bond]), filled([bond, w], [bond])
+    theta = filled([bond, phys], [phys, bond])
+    head = tg.einsum('EIa,IPqj->EPaqj', left, site)
+    tail = tg.einsum('JRsk,Fkb->JRSFb', site, right)
+    return head, tail, theta
+
+
+def to_oracle(orc, t):
+    """The oracle's copy of a device tensor (same legs, same blocks), for checking a result."""
+    import numpy as np
+    legs = lambda ls: [orc.Leg(orc.u1, list(l.sectors), list(l.multiplicities)) for l in ls]
+    out = orc.Tensor(orc.u1, legs(t.codomain), legs(t.domain), tuple(t.qtotal), np.float64)
+    for key in out.blocks:
+        out.blocks[key][...] = t.block(*key).cpu().numpy()
+    return out
 
 
 # ---------------------------------------------------------------------------------------------
@@ -257,27 +311,20 @@ def run_gpu(args, rank, world):
     from oracle import engine as orc
     from tentorch_gb300 import _lib
     from tentorch_gb300.linalg import PER_BLOCK
+    from torch.autograd.graph import increment_version
 
     local = int(os.environ.get('LOCAL_RANK', 0))
     torch.cuda.set_device(local)
     device = torch.device('cuda', local)
 
-    def product(t):
-        legs = lambda ls: [tg.Leg(tg.u1, list(l.sectors), list(l.multiplicities)) for l in ls]
-        out = tg.Tensor(tg.u1, legs(t.codomain), legs(t.domain), t.qtotal, dtype = torch.float64, device = device)
-        for key, block in t.blocks.items():
-            out.block(*key).copy_(torch.from_numpy(block))
-        return out
-
-    head_o, tail_o, theta_o = orc.matvec_inputs(args.chi, seed = SEED + rank)
-    head, tail = product(head_o), product(tail_o)
+    head, tail, theta = matvec_operands(tg, torch, device, args.chi, SEED + rank)
     gen = torch.Generator(device = device).manual_seed(SEED + 17 + rank)
-    vectors = []
-    for _ in range(4):
-        v = product(theta_o)
+    vectors = [theta]
+    for _ in range(3):
+        v = theta.clone()
         v.data.copy_(torch.randn(v.data.shape, dtype = torch.float64, device = device, generator = gen))
         vectors.append(v)
-    plan = tg.linalg.plan_of(orc.MATVEC, head, tail, vectors[0])
+    plan = tg.linalg.plan_of(MATVEC, head, tail, vectors[0])
     flush = torch.empty(64 * 1024 * 1024, dtype = torch.float32, device = device)  # 256 MB > L2
     stream = torch.cuda.current_stream(device)
 
@@ -294,15 +341,18 @@ def run_gpu(args, rank, world):
         return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
     def matvec(i):
-        return tg.einsum(orc.MATVEC, head, tail, vectors[i % 4])
+        # a Lanczos vector is new at every step: mark it written (host-side version counter, no
+        # device work) so that the engine runs its phase rather than reusing a prepared copy
+        increment_version(vectors[i % 4].data)
+        return tg.einsum(MATVEC, head, tail, vectors[i % 4])
 
     # correctness of this very workload before timing it, in every form, against the oracle
-    want = orc.einsum(orc.MATVEC, head_o, tail_o, theta_o)
+    want = orc.einsum(orc.MATVEC, to_oracle(orc, head), to_oracle(orc, tail), to_oracle(orc, theta))
     scale = max(np.abs(b).max() for b in want.blocks.values())
     parity = {}
     for name, form in (('split', args.precision), ('fp64_grouped', 0), ('fp64_per_block', PER_BLOCK)):
         with tg.precision(form):
-            got = tg.einsum(orc.MATVEC, head, tail, product(theta_o))
+            got = tg.einsum(MATVEC, head, tail, theta)
         parity[name] = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.blocks.items()) / scale
 
     for form in (args.precision, 0, PER_BLOCK):
@@ -397,11 +447,11 @@ def run_gpu(args, rank, world):
     for h, v in zip(host_in, vectors):
         h.copy_(v.data.cpu())
     host_out = torch.empty(plan.out_space.size, dtype = torch.float64, pin_memory = True)
-    staging = product(theta_o)
+    staging = theta.clone()
 
     def e2e_step(i):
         staging.data.copy_(host_in[i % 4], non_blocking = True)
-        out = tg.einsum(orc.MATVEC, head, tail, staging)
+        out = tg.einsum(MATVEC, head, tail, staging)
         host_out.copy_(out.data, non_blocking = True)
 
     tg.set_precision(args.precision)
@@ -450,12 +500,10 @@ def run_splittings(args):
     Prints one line of its own (not the headline); also a driver for profiling the SVD kernels."""
     import torch
     import tentorch_gb300 as tg
-    from oracle import engine as orc
     device = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
     torch.cuda.set_device(device)
-    qs, deg = orc.degeneracies(args.chi)
     cat = tg.u1
-    bond = tg.Leg(cat, [(2 * q,) for q in qs], deg)
+    bond = tg.Leg(cat, *bond_multiplicities(args.chi))
     phys = tg.Leg(cat, [(1,), (-1,)], [1, 1])
     t = tg.Tensor(cat, [bond, phys], [phys, bond], (0,), dtype = torch.float64, device = device)
     gen = torch.Generator().manual_seed(SEED)
@@ -474,10 +522,116 @@ def run_splittings(args):
                       'blocks': len(shapes), 'largest': shapes[-1], 'steps': args.steps}), flush = True)
 
 
+def run_recoupling(args):
+    """The SU(2) and Fibonacci recoupling einsum 'ABcd,DCef->ABef' (B's codomain order forces an
+    exchange F.R.F-dagger before the block products): SU(2) legs of spins j = 0..4 with 8 multiplets
+    each, float64; Fibonacci legs (vacuum 16, tau 16), complex128; seeded N(0, 1) blocks.  Times each
+    form the engine has for it (grouped FP64, split (float64 only), per-block cuBLAS) and the
+    largest relative difference between the forms.  Prints one line of its own."""
+    import torch
+    import tentorch_gb300 as tg
+    from tentorch_gb300.linalg import PER_BLOCK
+    device = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(device)
+    out = {'workload': 'recoupling_einsum_ABcd_DCef', 'equation': 'ABcd,DCef->ABef'}
+    for name, cat, leg, dtype in (('su2', tg.su2, tg.Leg(tg.su2, [(j,) for j in range(9)], [8] * 9), torch.float64),
+                                  ('fibonacci', tg.fibonacci, tg.Leg(tg.fibonacci, [(0,), (1,)], [16, 16]),
+                                   torch.complex128)):
+        gen = torch.Generator().manual_seed(SEED)
+        tensors = []
+        for _ in range(2):
+            t = tg.Tensor(cat, [leg, leg], [leg, leg], (0,), dtype = dtype, device = device)
+            for block in t.to_tuple()[3].values():
+                block.copy_(torch.randn(block.shape, dtype = torch.float64, generator = gen).to(dtype))
+            tensors.append(t)
+        plan = tg.linalg.plan_of('ABcd,DCef->ABef', *tensors)
+        forms = {'fp64_grouped': 0, 'fp64_per_block': PER_BLOCK}
+        if dtype == torch.float64:
+            forms['split'] = args.precision
+        results, images = {}, {}
+        for form_name, form in forms.items():
+            with tg.precision(form):
+                for _ in range(max(1, args.warmup)):
+                    images[form_name] = tg.einsum('ABcd,DCef->ABef', *tensors)
+                torch.cuda.synchronize(device)
+                start = time.perf_counter()
+                steps = max(1, min(args.steps, 5))
+                for _ in range(steps):
+                    tg.einsum('ABcd,DCef->ABef', *tensors)
+                torch.cuda.synchronize(device)
+            ms = 1e3 * (time.perf_counter() - start) / steps
+            flops = plan.flops * (4 if dtype == torch.complex128 else 1)
+            results[form_name] = {'ms': ms, 'tflops': flops / (ms / 1e3) / 1e12}
+        ref = images['fp64_grouped'].data
+        scale = float(ref.abs().max())
+        for form_name in results:
+            results[form_name]['max_rel_diff_vs_fp64_grouped'] = float((images[form_name].data - ref).abs().max()) / scale
+        out[name] = {'dtype': str(dtype).replace('torch.', ''), 'blocks': tensors[0].nblocks(),
+                     'entries_per_tensor': tensors[0].data.numel(), 'gemm_flop': plan.flops, 'forms': results}
+    print(json.dumps(out), flush = True)
+
+
+def run_windows(args):
+    """Batched windows: 64 independent U(1) two-site matvecs whose bond is drawn from a seed over
+    {32, 64, 128, 256, 512} (the sector layout, MPO and dtype of the matvec workload), one matvec per
+    window per step.  Timed issued one after another (the environments of each window prepared
+    once, as a Lanczos loop reuses them) and as one captured CUDA graph of all 64 (plans compiled and
+    tables uploaded before the capture; the graph reads every operand from its own buffer), in the
+    split form and the grouped FP64 form.  Prints one line of its own."""
+    import numpy as np
+    import torch
+    import tentorch_gb300 as tg
+    from torch.autograd.graph import increment_version
+    device = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(device)
+    rng = np.random.default_rng(SEED)
+    chis = [int(c) for c in rng.choice([32, 64, 128, 256, 512], size = 64)]
+    windows = [matvec_operands(tg, torch, device, chi, SEED + i) for i, chi in enumerate(chis)]
+    flops = sum(tg.linalg.plan_of(MATVEC, *win).flops for win in windows)
+    out = {'workload': 'batched_windows_u1_matvec', 'windows': len(windows), 'chis': chis, 'gemm_flop_per_step': flops}
+    stream = torch.cuda.current_stream(device)
+    for name, form in (('split', args.precision), ('fp64_grouped', 0)):
+        with tg.precision(form):
+            def step():
+                # every window's vector is new at every step (see matvec in run_gpu)
+                for win in windows:
+                    increment_version(win[2].data)
+                return [tg.einsum(MATVEC, *win) for win in windows]
+            for _ in range(3):
+                step()
+            torch.cuda.synchronize(device)
+            steps = max(1, min(args.steps, 50))
+            start = time.perf_counter()
+            for _ in range(steps):
+                step()
+            torch.cuda.synchronize(device)
+            eager_ms = 1e3 * (time.perf_counter() - start) / steps
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                step()
+            graph.replay()
+            torch.cuda.synchronize(device)
+            start = time.perf_counter()
+            for _ in range(steps):
+                graph.replay()
+            torch.cuda.synchronize(device)
+            graph_ms = 1e3 * (time.perf_counter() - start) / steps
+        out[name] = {'eager_ms_per_step': eager_ms, 'graph_ms_per_step': graph_ms,
+                     'matvecs_per_s_graph': len(windows) / (graph_ms / 1e3),
+                     'gflops_graph': flops / (graph_ms / 1e3) / 1e9}
+    print(json.dumps(out), flush = True)
+
+
 def main():
     args = parse()
     if args.workload == 'svd':
         run_splittings(args)
+        return
+    if args.workload == 'recoupling':
+        run_recoupling(args)
+        return
+    if args.workload == 'windows':
+        run_windows(args)
         return
     rank, world = int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1))
     if world > 1:

@@ -33,23 +33,6 @@ namespace ttg
     return s;
   }
 
-  bool Sector::operator==(const Sector &o) const
-  {
-    if (size != o.size) return false;
-    for (int32_t i = 0; i < size; ++i)
-      if (q[static_cast<size_t>(i)] != o.q[static_cast<size_t>(i)]) return false;
-    return true;
-  }
-
-  // tentorch/symmetry/cat/cat.h:121-130: lexicographic, the shorter first when one is a prefix.
-  bool Sector::operator<(const Sector &o) const
-  {
-    const int32_t common = std::min(size, o.size);
-    for (int32_t i = 0; i < common; ++i)
-      if (q[static_cast<size_t>(i)] != o.q[static_cast<size_t>(i)]) return q[static_cast<size_t>(i)] < o.q[static_cast<size_t>(i)];
-    return size < o.size;
-  }
-
   std::string Sector::str() const
   {
     std::string out = "(";

@@ -56,9 +56,22 @@ namespace ttg
     Sector(std::initializer_list<int64_t> values);
     static Sector of(const int64_t *values, int32_t n);
     int64_t operator[](int32_t i) const { return q[static_cast<size_t>(i)]; }
-    bool operator==(const Sector &o) const;
+    bool operator==(const Sector &o) const
+    {
+      if (size != o.size) return false;
+      for (int32_t i = 0; i < size; ++i)
+        if (q[static_cast<size_t>(i)] != o.q[static_cast<size_t>(i)]) return false;
+      return true;
+    }
     bool operator!=(const Sector &o) const { return !(*this == o); }
-    bool operator<(const Sector &o) const;
+    // tentorch/symmetry/cat/cat.h:121-130: lexicographic, the shorter first when one is a prefix.
+    bool operator<(const Sector &o) const
+    {
+      const int32_t common = size < o.size ? size : o.size;
+      for (int32_t i = 0; i < common; ++i)
+        if (q[static_cast<size_t>(i)] != o.q[static_cast<size_t>(i)]) return q[static_cast<size_t>(i)] < o.q[static_cast<size_t>(i)];
+      return size < o.size;
+    }
     std::string str() const;
   };
 

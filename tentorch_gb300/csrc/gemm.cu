@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <numeric>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -103,29 +104,37 @@ namespace ttg
           s.reduces.push_back({bi, m0, n0, slot0, static_cast<int32_t>(chunks), 0});
         }
     }
-    std::stable_sort(items.begin(), items.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
+    // largest first, equal work in the order made
+    std::vector<int32_t> order(items.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&items](int32_t a, int32_t b)
+              { return items[static_cast<size_t>(a)].work > items[static_cast<size_t>(b)].work ||
+                       (items[static_cast<size_t>(a)].work == items[static_cast<size_t>(b)].work && a < b); });
     // LPT: each item to the CTA with the least work so far (ties to the lower index)
     const int ctas = static_cast<int>(std::min<size_t>(kScheduleCtas, std::max<size_t>(items.size(), 1)));
-    std::vector<std::vector<GemmItem>> lists(static_cast<size_t>(ctas));
     std::vector<std::pair<double, int>> heap;
+    heap.reserve(static_cast<size_t>(ctas));
     for (int c = 0; c < ctas; ++c) heap.push_back({0.0, c});
     const auto later = [](const std::pair<double, int> &a, const std::pair<double, int> &b)
     { return a.first > b.first || (a.first == b.first && a.second > b.second); };
     std::make_heap(heap.begin(), heap.end(), later);
-    for (const Sized &it : items)
+    std::vector<int32_t> cta_of(items.size());
+    s.cta_begin.assign(static_cast<size_t>(ctas) + 1, 0);
+    for (const int32_t i : order)
     {
       std::pop_heap(heap.begin(), heap.end(), later);
       auto &least = heap.back();
-      lists[static_cast<size_t>(least.second)].push_back(it.item);
-      least.first += it.work;
+      cta_of[static_cast<size_t>(i)] = least.second;
+      ++s.cta_begin[static_cast<size_t>(least.second) + 1];
+      least.first += items[static_cast<size_t>(i)].work;
       std::push_heap(heap.begin(), heap.end(), later);
     }
-    s.cta_begin.push_back(0);
-    for (const auto &list : lists)
-    {
-      s.items.insert(s.items.end(), list.begin(), list.end());
-      s.cta_begin.push_back(static_cast<int32_t>(s.items.size()));
-    }
+    // the lists back to back, each in the order its items were dealt
+    for (int c = 0; c < ctas; ++c) s.cta_begin[static_cast<size_t>(c) + 1] += s.cta_begin[static_cast<size_t>(c)];
+    std::vector<int32_t> fill(s.cta_begin.begin(), s.cta_begin.end() - 1);
+    s.items.resize(items.size());
+    for (const int32_t i : order)
+      s.items[static_cast<size_t>(fill[static_cast<size_t>(cta_of[static_cast<size_t>(i)])]++)] = items[static_cast<size_t>(i)].item;
     return s;
   }
 

@@ -283,15 +283,6 @@ namespace ttg
     private:
       void emit(const Op &op) { p_.ops.push_back(op); }
 
-      // The composed gather index of a whole chain of leg moves when every F and R symbol is 1:
-      // after[i] = before[index[i]], -1 for entries nothing writes.  Such a chain only relabels:
-      // the entry at sector s_l, copy c_l of every leg l lands at the same copies of the output
-      // legs, a leg that ends on the other side reading its sector as the dual (each bend reads
-      // the dual sector's rows, tentorch/tensors/regroup.cpp:260-417).  A bent leg that does not
-      // hold the dual of an entry's sector drops the entry, as the chain's bends do; the chain
-      // bends every leg of below[kept:] down and every domain leg past `kept` up.  The result is
-      // the composition of the per-step permutations, built in one pass over the entries instead
-      // of one pass per step.
       // One piece of a relabelling move: an (input row tree, input column tree) part of an input
       // block and the rectangle of an output block it lands in.  Strides and extents are per
       // input leg; out_stride is within the output block (rows times its columns, or columns).
@@ -300,6 +291,73 @@ namespace ttg
         int64_t in_base, out_base, out_ld;
         const std::vector<int64_t> *extent, *in_stride, *out_stride;
       };
+
+      // Tuples of sector indices over a list of legs, numbered mixed-radix: a dense table when the
+      // legs have few sector combinations, a hash map when they have many, and tuples as vectors
+      // when the numbering would not fit in 62 bits.
+      class TupleIndex
+      {
+      public:
+        explicit TupleIndex(const std::vector<Leg> &legs)
+        {
+          for (const Leg leg : legs)
+          {
+            const int64_t r = static_cast<int64_t>(leg->sectors.size());
+            radix_.push_back(r);
+            if (total_ > (int64_t{1} << 62) / std::max<int64_t>(r, 1)) wide_ = true;
+            else total_ *= r;
+          }
+          dense_ = !wide_ && total_ <= (int64_t{1} << 20);
+          if (dense_) table_.assign(static_cast<size_t>(total_), -1);
+        }
+        int32_t get(const int32_t *idx) const
+        {
+          if (wide_)
+          {
+            const auto it = wide_map_.find(std::vector<int32_t>(idx, idx + radix_.size()));
+            return it == wide_map_.end() ? -1 : it->second;
+          }
+          const int64_t c = code(idx);
+          if (dense_) return table_[static_cast<size_t>(c)];
+          const auto it = hashed_.find(c);
+          return it == hashed_.end() ? -1 : it->second;
+        }
+        // keeps the first value stored for a tuple
+        void put_first(const int32_t *idx, int32_t value)
+        {
+          if (wide_) wide_map_.emplace(std::vector<int32_t>(idx, idx + radix_.size()), value);
+          else if (dense_)
+          {
+            int32_t &slot = table_[static_cast<size_t>(code(idx))];
+            if (slot < 0) slot = value;
+          }
+          else hashed_.emplace(code(idx), value);
+        }
+
+      private:
+        int64_t code(const int32_t *idx) const
+        {
+          int64_t c = 0;
+          for (size_t i = 0; i < radix_.size(); ++i) c = c * radix_[i] + idx[i];
+          return c;
+        }
+        std::vector<int64_t> radix_;
+        int64_t total_ = 1;
+        bool wide_ = false, dense_ = false;
+        std::vector<int32_t> table_;
+        std::unordered_map<int64_t, int32_t> hashed_;
+        std::map<std::vector<int32_t>, int32_t> wide_map_;
+      };
+
+      // The sector index on `legs` of every leg of every tree of a layout (row t at t * legs).
+      static std::vector<int32_t> tree_indices(const Layout &lay, const std::vector<Leg> &legs)
+      {
+        std::vector<int32_t> out;
+        out.reserve(lay.trees.size() * legs.size());
+        for (const Tree &t : lay.trees)
+          for (size_t l = 0; l < legs.size(); ++l) out.push_back(static_cast<int32_t>(legs[l]->index_of(t.sectors[l])));
+        return out;
+      }
 
       template <typename Fn>
       int64_t walk_pieces(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below, Space out,
@@ -317,13 +375,28 @@ namespace ttg
         for (size_t j = static_cast<size_t>(kept); j < below.size(); ++j) bent[static_cast<size_t>(below[j])] = true;
         for (const int32_t l : above) switched[static_cast<size_t>(l)] = l >= h;
         for (const int32_t l : below) switched[static_cast<size_t>(l)] = l < h;
-        // per leg and block of that leg: whether an entry survives the bends, and the paired
-        // multiplets a bend needs (the check bend_plan makes)
+        const std::vector<Leg> out_cod = out->codomain, out_dom = out->domain;
+        // per leg and block of that leg: whether an entry survives the bends (the check bend_plan
+        // makes on the paired multiplets), and the index of its sector on the output leg it
+        // becomes (read as the dual when the leg changes side; -1 when that leg lacks it)
         std::vector<std::vector<bool>> survives(static_cast<size_t>(n));
+        std::vector<std::vector<int32_t>> lands(static_cast<size_t>(n));
+        std::vector<Leg> target(static_cast<size_t>(n));
+        for (size_t i = 0; i < above.size(); ++i) target[static_cast<size_t>(above[i])] = out_cod[i];
+        for (size_t j = 0; j < below.size(); ++j) target[static_cast<size_t>(below[j])] = out_dom[j];
         for (int32_t l = 0; l < n; ++l)
         {
           const Leg leg = legs[static_cast<size_t>(l)];
           survives[static_cast<size_t>(l)].assign(leg->sectors.size(), true);
+          lands[static_cast<size_t>(l)].assign(leg->sectors.size(), -1);
+          for (size_t b = 0; b < leg->sectors.size(); ++b)
+          {
+            const Sector label = switched[static_cast<size_t>(l)] ? cat.dual(leg->sectors[b]) : leg->sectors[b];
+            const Leg to = target[static_cast<size_t>(l)];
+            const auto it = std::lower_bound(to->sectors.begin(), to->sectors.end(), label);
+            if (it != to->sectors.end() && *it == label)
+              lands[static_cast<size_t>(l)][b] = static_cast<int32_t>(it - to->sectors.begin());
+          }
           if (!bent[static_cast<size_t>(l)]) continue;
           for (size_t b = 0; b < leg->sectors.size(); ++b)
           {
@@ -342,48 +415,67 @@ namespace ttg
                                     std::to_string(other));
           }
         }
-        // the output trees by their sector tuples: (root, first row) on each side
-        const std::vector<Leg> out_cod = out->codomain, out_dom = out->domain;
-        std::map<std::vector<Sector>, std::pair<Sector, int64_t>> rows_of, cols_of;
+        // the output trees by the sector indices of their legs: (root, first row) on each side,
+        // the first tree of a tuple kept; the output blocks (copy 0) by their pair of roots
+        TupleIndex rows_of(out_cod), cols_of(out_dom);
+        std::vector<std::pair<int32_t, int64_t>> row_at, col_at;  // (root number, first row)
+        std::map<Sector, int32_t> cod_root, dom_root;
         for (const Block &ob : out->blocks)
         {
-          for (const auto &[side, root, table] :
-               {std::make_tuple(&out_cod, ob.key.codomain, &rows_of), std::make_tuple(&out_dom, ob.key.domain, &cols_of)})
+          cod_root.emplace(ob.key.codomain, static_cast<int32_t>(cod_root.size()));
+          dom_root.emplace(ob.key.domain, static_cast<int32_t>(dom_root.size()));
+        }
+        std::vector<int32_t> block_of(cod_root.size() * dom_root.size(), -1);
+        for (size_t bi = 0; bi < out->blocks.size(); ++bi)
+        {
+          const Block &ob = out->blocks[bi];
+          const int32_t rr = cod_root.at(ob.key.codomain), cr = dom_root.at(ob.key.domain);
+          if (ob.key.copy == 0) block_of[static_cast<size_t>(rr) * dom_root.size() + static_cast<size_t>(cr)] = static_cast<int32_t>(bi);
+          for (const auto &[side, root, number, table, at] :
+               {std::make_tuple(&out_cod, ob.key.codomain, rr, &rows_of, &row_at),
+                std::make_tuple(&out_dom, ob.key.domain, cr, &cols_of, &col_at)})
           {
             const Layout &lay = layout_of(cat, *side, root);
-            for (size_t t = 0; t < lay.trees.size(); ++t) table->emplace(lay.trees[t].sectors, std::make_pair(root, lay.offsets[t]));
+            const std::vector<int32_t> idx = tree_indices(lay, *side);
+            for (size_t t = 0; t < lay.trees.size(); ++t)
+            {
+              table->put_first(idx.data() + t * side->size(), static_cast<int32_t>(at->size()));
+              at->push_back({number, lay.offsets[t]});
+            }
           }
         }
-        std::vector<Sector> sec(static_cast<size_t>(n)), cod_out(above.size()), dom_out(below.size());
+        std::vector<int32_t> idx_out(static_cast<size_t>(n));
         std::vector<int64_t> extent(static_cast<size_t>(n)), in_stride(static_cast<size_t>(n)),
           out_stride(static_cast<size_t>(n));
+        std::vector<int32_t> at_of(static_cast<size_t>(n));
         int64_t covered = 0;
         for (const Block &blk : in->blocks)
         {
           const Layout &rl = layout_of(cat, in->codomain, blk.key.codomain);
           const Layout &cl = layout_of(cat, in->domain, blk.key.domain);
+          const std::vector<int32_t> r_idx = tree_indices(rl, in->codomain), c_idx = tree_indices(cl, in->domain);
           for (size_t rt = 0; rt < rl.trees.size(); ++rt)
             for (size_t ct = 0; ct < cl.trees.size(); ++ct)
             {
               bool keep = true;
               for (int32_t l = 0; l < n && keep; ++l)
               {
-                const Sector &s = l < h ? rl.trees[rt].sectors[static_cast<size_t>(l)]
-                                        : cl.trees[ct].sectors[static_cast<size_t>(l - h)];
-                sec[static_cast<size_t>(l)] = s;
-                const int64_t at = legs[static_cast<size_t>(l)]->index_of(s);
-                keep = survives[static_cast<size_t>(l)][static_cast<size_t>(at)];
+                const int32_t at = l < h ? r_idx[rt * static_cast<size_t>(h) + static_cast<size_t>(l)]
+                                         : c_idx[ct * static_cast<size_t>(d) + static_cast<size_t>(l - h)];
+                at_of[static_cast<size_t>(l)] = at;
+                keep = survives[static_cast<size_t>(l)][static_cast<size_t>(at)] && lands[static_cast<size_t>(l)][static_cast<size_t>(at)] >= 0;
                 extent[static_cast<size_t>(l)] = legs[static_cast<size_t>(l)]->mult[static_cast<size_t>(at)];
               }
               if (!keep) continue;
-              const auto label = [&](int32_t l)
-              { return switched[static_cast<size_t>(l)] ? cat.dual(sec[static_cast<size_t>(l)]) : sec[static_cast<size_t>(l)]; };
-              for (size_t i = 0; i < above.size(); ++i) cod_out[i] = label(above[i]);
-              for (size_t j = 0; j < below.size(); ++j) dom_out[j] = label(below[j]);
-              const auto r = rows_of.find(cod_out);
-              const auto c = cols_of.find(dom_out);
-              if (r == rows_of.end() || c == cols_of.end()) continue;
-              const int32_t ob_at = out->find(BlockKey{r->second.first, c->second.first, 0});
+              for (size_t i = 0; i < above.size(); ++i)
+                idx_out[i] = lands[static_cast<size_t>(above[i])][static_cast<size_t>(at_of[static_cast<size_t>(above[i])])];
+              for (size_t j = 0; j < below.size(); ++j)
+                idx_out[above.size() + j] = lands[static_cast<size_t>(below[j])][static_cast<size_t>(at_of[static_cast<size_t>(below[j])])];
+              const int32_t r = rows_of.get(idx_out.data());
+              const int32_t c = cols_of.get(idx_out.data() + above.size());
+              if (r < 0 || c < 0) continue;
+              const int32_t ob_at = block_of[static_cast<size_t>(row_at[static_cast<size_t>(r)].first) * dom_root.size() +
+                                             static_cast<size_t>(col_at[static_cast<size_t>(c)].first)];
               if (ob_at < 0) continue;
               const Block &ob = out->blocks[static_cast<size_t>(ob_at)];
               // strides: input rows and columns with the last leg of each side fastest; the same
@@ -402,8 +494,8 @@ namespace ttg
               for (int32_t l = 0; l < n; ++l) entries *= extent[static_cast<size_t>(l)];
               covered += entries;
               fn(MovePiece{blk.offset + rl.offsets[rt] * blk.cols + cl.offsets[ct],
-                       ob.offset + r->second.second * ob.cols + c->second.second, ob.cols, &extent, &in_stride,
-                       &out_stride});
+                           ob.offset + row_at[static_cast<size_t>(r)].second * ob.cols + col_at[static_cast<size_t>(c)].second,
+                           ob.cols, &extent, &in_stride, &out_stride});
             }
         }
         return covered;

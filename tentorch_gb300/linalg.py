@@ -144,27 +144,32 @@ def _workspace(plan: Plan, device, dtype, stream) -> Optional[torch.Tensor]:
 def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws, stream, force: bool = False) -> Optional[torch.Tensor]:
     """The operand's prepared arena when the same arena (same version) comes back to this plan: the
     first sighting runs the operand's phase inside the plan and only remembers the arena; the
-    second prepares it once for every call after (the head and tail of a Lanczos window)."""
+    second prepares it once for every call after (the head and tail of a Lanczos window).  Entries
+    are per arena, so windows that share a plan each keep theirs; an entry goes with its arena."""
     size = plan.prepared_size(operand)
     if size <= 0:
         return None
-    key = (plan.handle.value, operand)
-    held = _prepared.get(key)
     data = tensor._data
-    if force or (held is not None and held[0]() is data and held[1] == data._version):
-        if held is not None and held[0]() is data and held[1] == data._version and held[2] is not None:
-            return held[2]
+    key = (plan.handle.value, operand, data.data_ptr())
+    held = _prepared.get(key)
+    seen = held is not None and held[0]() is data and held[1] == data._version
+    if seen and held[2] is not None:
+        return held[2]
+    arena = None
+    if force or seen:
         arena = torch.empty(size, dtype = data.dtype, device = data.device)
         check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
                                   ws.data_ptr() if ws is not None else None, stream))
-        _prepared[key] = (weakref.ref(data), data._version, arena)
-        return arena
-    if len(_prepared) > 256:
-        # operands that are gone
-        for stale in [k for k, entry in _prepared.items() if entry[0]() is None]:
-            del _prepared[stale]
-    _prepared[key] = (weakref.ref(data), data._version, None)
-    return None
+    if held is None or held[0]() is not data:
+        def forget(ref, key = key):
+            entry = _prepared.get(key)
+            if entry is not None and entry[0] is ref:
+                del _prepared[key]
+        ref = weakref.ref(data, forget)
+    else:
+        ref = held[0]
+    _prepared[key] = (ref, data._version, arena)
+    return arena
 
 
 def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool = True) -> Tensor:
@@ -176,6 +181,8 @@ def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool 
         out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = data0.dtype, device = device))
     stream = torch.cuda.current_stream(device).cuda_stream
     ws = _workspace(plan, device, data0.dtype, stream)
+    # a captured CUDA graph reads every operand from its own buffer at each replay, never a prepared copy
+    reuse_prepared = reuse_prepared and not torch.cuda.is_current_stream_capturing()
     prepared = [(_prepared_arena(plan, i, t, ws, stream) if reuse_prepared else None) for i, t in enumerate(tensors)]
     inputs = pointers(t._data.data_ptr() for t in tensors)
     prep = pointers((p.data_ptr() if p is not None else None) for p in prepared)

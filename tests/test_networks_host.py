@@ -74,3 +74,20 @@ def test_argument_errors():
         nw.MPS([], tg.Leg(tg.u1, [(1,)], [1]))
     with pytest.raises(ValueError):
         nw.MPO([], tg.Leg(tg.u1, [(1,)], [1]), tg.u1)
+
+
+def test_bench_bond_layout_is_the_matvec_workload_layout():
+    '''The benchmark builds its bond with the layout the oracle's matvec inputs use (17 charges,
+    multiplicities from exp(-q^2/8) summing to chi, symmetric in q).'''
+    import importlib.util
+    import pathlib
+    from oracle import engine as orc
+    path = pathlib.Path(__file__).resolve().parents[1] / 'bench.py'
+    spec = importlib.util.spec_from_file_location('bench_under_test', path)
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    for chi in (32, 64, 100, 256, 512, 1024):
+        sectors, mult = bench.bond_multiplicities(chi)
+        qs, deg = orc.degeneracies(chi)
+        assert sectors == [(2 * q,) for q in qs] and mult == deg and sum(mult) == chi
+        assert mult == mult[::-1]
