@@ -169,19 +169,18 @@ int32_t tt_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const 
 /* ---- truncating splittings (tentorch/linalg/graded/svd.cpp:41-177) -------------------------- */
 
 /* Thin SVDs of `count` float64 blocks in one launch (one-sided Jacobi, mixed precision: FP32 sweeps,
- * then FP64 re-orthonormalisation and FP64 sweeps to full accuracy; a CTA per block; replaces the
- * per-block at::linalg_svd of svd.cpp:57-62).  `table` is a DEVICE array of 7 int64 per block:
+ * then FP64 re-orthonormalisation and FP64 sweeps to full accuracy; a thread-block cluster per
+ * block; replaces the per-block at::linalg_svd of svd.cpp:57-62).  `table` is a DEVICE array of 7 int64 per block:
  * a_off, rows, cols, u_off, s_off, vh_off, ws_off (offsets in doubles).  Block i is rows x cols
  * row-major at a + a_off; with k = min(rows, cols) <= 1024 it writes U (rows x k, row-major) at
  * u + u_off, the k singular values in descending order at s + s_off and Vh (k x cols, row-major)
- * at vh + vh_off.  ws_off places the block's working set in `workspace` when tt_svd_workspace gave
- * it one (-1 otherwise).  info[i] (device int32) receives the FP64 sweeps block i took, -1 when
+ * at vh + vh_off.  ws_off places the block's working set in `workspace` (from tt_svd_workspace).  info[i] (device int32) receives the FP64 sweeps block i took, -1 when
  * they did not converge (then its factors are not to be used).  Asynchronous on `stream`. */
 int32_t tt_svd_blocks(int32_t count, const int64_t *table, const double *a, double *u, double *s, double *vh,
                       double *workspace, int32_t *info, void *stream);
 /* The workspace of tt_svd_blocks: for `count` blocks (host array of rows, cols per block) the
- * offset in doubles of each block's working set in the workspace (-1: it fits in shared memory)
- * and the doubles the workspace needs in all. */
+ * offset in doubles of each block's working set in the workspace (-1 for an empty block) and the
+ * doubles the workspace needs in all. */
 int32_t tt_svd_workspace(int32_t count, const int64_t *shapes, int64_t *offsets, int64_t *total);
 /* Write the kept part of the factors of tt_svd_blocks into the two tensors of a split, one CTA per
  * kept block.  `table` is a DEVICE array of 10 int64 per block: u_off, s_off, vh_off (packed

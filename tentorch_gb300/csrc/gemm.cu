@@ -48,12 +48,12 @@ namespace ttg
     // The workers of one SM share its FP64 pipe, so what has to balance is the work per SM: items
     // of a few per SM (a matvec's stage has only ~10^5 multiply-adds per SM), each a tile over a
     // K range of at least 16, dealt to the SMs largest first, each to the least loaded (LPT).
-    // Cost of an item: the 8 x 8 DMMA fragments it computes (fragments wholly outside the block are
+    // Cost of an item: the 16 x 8 DMMA fragments it computes (fragments wholly outside the block are
     // skipped) times its K range, plus per staged K step (its copies and barriers) and per item
     // (claim, write or partial tile) a quarter of a full tile over 16 of K.
     const auto cost = [bm, bn](double rows, double cols, double k)
     {
-      const double frag = std::ceil(rows / 8.0) * 8.0 * std::ceil(cols / 8.0) * 8.0;
+      const double frag = std::ceil(rows / 16.0) * 16.0 * std::ceil(cols / 8.0) * 8.0;
       return frag * k + 0.25 * bm * bn * 16.0 * (std::ceil(k / kDmmaStepK) + 1.0);
     };
     double total = 0;
@@ -545,16 +545,20 @@ namespace ttg
       }
     }
 
-    __device__ __forceinline__ void dmma(double (&c)[2], double a, double b)
+    // D = A B + D on a 16 x 8 x 8 FP64 fragment.  Lane l (g = l / 4, t = l % 4) holds A at rows
+    // g, g + 8 and columns t, t + 4 (a0: (g, t), a1: (g + 8, t), a2: (g, t + 4), a3: (g + 8, t + 4)),
+    // B at rows t, t + 4 of column g, and D at rows g (c0, c1) and g + 8 (c2, c3) of columns 2t, 2t + 1.
+    __device__ __forceinline__ void dmma16(double (&c)[4], const double (&a)[4], const double (&b)[2])
     {
-      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
-                   : "+d"(c[0]), "+d"(c[1])
-                   : "d"(a), "d"(b));
+      asm volatile("mma.sync.aligned.m16n8k8.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                   "{%0,%1,%2,%3};\n"
+                   : "+d"(c[0]), "+d"(c[1]), "+d"(c[2]), "+d"(c[3])
+                   : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(b[0]), "d"(b[1]));
     }
 
-    // The float64 form of gemm_f64_kernel on the FP64 tensor instruction (mma m8n8k4 f64): each of
-    // a worker's 4 warps owns a 16 x 16 quarter of the 32 x 32 tile as 2 x 2 m8n8 accumulators; per
-    // K step of 16 staged in shared memory a warp issues 16 DMMA.
+    // The float64 form of gemm_f64_kernel on the FP64 matrix instruction (mma m16n8k8 f64): each of
+    // a worker's 4 warps owns a 16 x 16 quarter of the 32 x 32 tile as two m16n8 accumulators; per
+    // 8 of K staged in shared memory a warp issues 2 DMMA.
     __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1)
       gemm_dmma_kernel(const double *__restrict__ A, const double *__restrict__ B, double *__restrict__ C,
                        const DevBlock *__restrict__ blocks, const DevPair *__restrict__ pairs,
@@ -564,8 +568,8 @@ namespace ttg
       constexpr int BM = kF64TileM, BN = kF64TileN, BK = kDmmaStepK;
       extern __shared__ __align__(16) unsigned char smem_raw[];
       const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
-      // rows of 36 doubles: a warp's m8n8k4 fragment loads (k = lane % 4, row = lane / 4) then fall on
-      // distinct bank pairs within each half warp.  Two stages of A (k-major) and B per worker.
+      // rows of 36 doubles: a warp's fragment loads (k = lane % 4 (+ 4), row = lane / 4 (+ 8)) then
+      // fall on distinct bank pairs within each half warp.  Two stages of A (k-major) and B per worker.
       constexpr int P = 36;
       double *stage_base = reinterpret_cast<double *>(smem_raw) + static_cast<size_t>(worker) * 2 * 2 * BK * P;
       __shared__ int flags[kF64Workers];
@@ -584,8 +588,8 @@ namespace ttg
       {
         const GemmItem it = items[idx];
         const DevBlock blk = blocks[it.block];
-        double acc[2][2][2] = {};
-        const bool live_i[2] = {it.m0 + wm * 16 < blk.m, it.m0 + wm * 16 + 8 < blk.m};
+        double acc[2][4] = {};
+        const bool live_i = it.m0 + wm * 16 < blk.m;
         const bool live_j[2] = {it.n0 + wn * 16 < blk.n, it.n0 + wn * 16 + 8 < blk.n};
         int32_t kbase = 0;
         for (int32_t pi = 0; pi < blk.pair_count; ++pi)
@@ -631,31 +635,32 @@ namespace ttg
             const double(*as)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P);
             const double(*bs)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P + BK * P);
             const int steps = min(BK, hi - k0);
-            // an 8 x 8 fragment wholly outside the block costs the FP64 pipe as much as a full one:
+            // a 16 x 8 fragment wholly outside the block costs the FP64 pipe as much as a full one:
             // skip it (warp-uniform); a full step runs unrolled with no bound, so the fragment loads
-            // of the next k are issued ahead of the products of this one
+            // of the next k are issued ahead of the products of this one.  Entries of the stage past
+            // `hi` are zeros, so a last step rounded up to 8 adds nothing.
             const auto step_k = [&](int kb)
             {
-              double af[2], bf[2];
+              double af[4], bf[2][2];
 #pragma unroll
-              for (int i = 0; i < 2; ++i) af[i] = as[kb + fk][wm * 16 + i * 8 + fr];
+              for (int h = 0; h < 4; ++h) af[h] = as[kb + fk + (h >> 1) * 4][wm * 16 + (h & 1) * 8 + fr];
 #pragma unroll
-              for (int j = 0; j < 2; ++j) bf[j] = bs[kb + fk][wn * 16 + j * 8 + fr];
+              for (int j = 0; j < 2; ++j)
 #pragma unroll
-              for (int i = 0; i < 2; ++i)
+                for (int h = 0; h < 2; ++h) bf[j][h] = bs[kb + fk + h * 4][wn * 16 + j * 8 + fr];
 #pragma unroll
-                for (int j = 0; j < 2; ++j)
-                  if (live_i[i] && live_j[j]) dmma(acc[i][j], af[i], bf[j]);
+              for (int j = 0; j < 2; ++j)
+                if (live_j[j]) dmma16(acc[j], af, bf[j]);
             };
-            if (live_i[0] && live_j[0])  // the warp's 16 x 16 quarter touches the block
+            if (live_i && live_j[0])  // the warp's 16 x 16 quarter touches the block
             {
               if (steps == BK)
               {
 #pragma unroll
-                for (int kb = 0; kb < BK; kb += 4) step_k(kb);
+                for (int kb = 0; kb < BK; kb += 8) step_k(kb);
               }
               else
-                for (int kb = 0; kb < steps; kb += 4) step_k(kb);
+                for (int kb = 0; kb < steps; kb += 8) step_k(kb);
             }
             worker_sync(worker);
           }
@@ -664,24 +669,20 @@ namespace ttg
         {
           double *out = partial + static_cast<int64_t>(it.slot) * BM * BN;
 #pragma unroll
-          for (int i = 0; i < 2; ++i)
+          for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int j = 0; j < 2; ++j)
-#pragma unroll
-              for (int h = 0; h < 2; ++h) out[(wm * 16 + i * 8 + fr) * BN + wn * 16 + j * 8 + fk * 2 + h] = acc[i][j][h];
+            for (int h = 0; h < 4; ++h) out[(wm * 16 + (h >> 1) * 8 + fr) * BN + wn * 16 + j * 8 + fk * 2 + (h & 1)] = acc[j][h];
           finish_partial<double, BM, BN>(worker, lt, flags + worker, tickets, reduces, it.reduce, blocks, partial, C);
           continue;
         }
 #pragma unroll
-        for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j)
 #pragma unroll
-          for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int h = 0; h < 2; ++h)
-            {
-              const int gm = it.m0 + wm * 16 + i * 8 + fr, gn = it.n0 + wn * 16 + j * 8 + fk * 2 + h;
-              if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[i][j][h];
-            }
+          for (int h = 0; h < 4; ++h)
+          {
+            const int gm = it.m0 + wm * 16 + (h >> 1) * 8 + fr, gn = it.n0 + wn * 16 + j * 8 + fk * 2 + (h & 1);
+            if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[j][h];
+          }
         const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
         if (lt == 0 && it.m0 + BM >= blk.m && it.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = 0.0;
       }

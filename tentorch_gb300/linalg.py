@@ -59,12 +59,14 @@ def precision(slices: int):
 
 class Plan:
     '''A compiled program: its output space, workspace and the size of each operand's prepared
-    arena.'''
-    __slots__ = ('handle', 'cat', 'out_space', 'workspace', 'flops', 'moved', 'n_ops', 'prepared', 'sizes',
-                 '__weakref__')
+    arena.  The engine owns the program; a wholesale clear of the plan caches frees it, and a Plan
+    held across that clear compiles its program again on its next use (same key, same result).'''
+    __slots__ = ('_handle', 'generation', 'key', 'build', 'cat', 'out_space', 'workspace', 'flops', 'moved', 'n_ops',
+                 'prepared', 'sizes', '__weakref__')
 
-    def __init__(self, handle, cat):
-        self.handle, self.cat = handle, cat
+    def __init__(self, handle, cat, key = None, build = None):
+        self._handle, self.cat, self.key, self.build = handle, cat, key, build
+        self.generation = _generation
         space, ws, flops, moved, ops = i32(), i64(), f64(), i64(), i32()
         check(lib.tt_plan_info(handle, ctypes.byref(space), ctypes.byref(ws), ctypes.byref(flops), ctypes.byref(moved),
                                ctypes.byref(ops)))
@@ -72,6 +74,15 @@ class Plan:
         self.workspace, self.flops, self.moved, self.n_ops = ws.value, flops.value, moved.value, ops.value
         self.prepared = []
         self.sizes = {}
+
+    @property
+    def handle(self):
+        if self.generation != _generation:
+            if self.build is None:
+                raise RuntimeError('this plan was freed by clear_plans()')
+            fresh = _plan(self.key, self.build, self.cat)
+            self._handle, self.generation = fresh._handle, fresh.generation
+        return self._handle
 
     def describe(self) -> str:
         '''The plan's operations and GEMM block shapes, as text.'''
@@ -91,6 +102,11 @@ class Plan:
 
 
 _plans = {}
+# compiled plans kept before a wholesale clear (the reference clears its plan caches wholesale at a
+# budget, tentorch/tensors/cache.cpp:203-217): DMRG compiles new shapes at every window, so without
+# a bound the caches would grow with the length of the run
+_PLAN_BUDGET = 4096
+_generation = 0
 # (plan handle, operand) -> (weakref to the operand arena, its version, the prepared arena or None
 # when the operand has been seen once and not prepared yet)
 _prepared = {}
@@ -101,8 +117,10 @@ _pools = {}
 
 def clear_plans() -> None:
     '''Forget every compiled plan, here and in the engine (their device tables are freed): the next
-    contraction of each shape compiles again.  For bounding memory over a long run whose shapes keep
-    changing, and for timing compilation.'''
+    contraction of each shape compiles again.  Runs by itself when the cache reaches its budget; by
+    hand, for timing compilation.'''
+    global _generation
+    _generation += 1
     _plans.clear()
     _prepared.clear()
     _pools.clear()
@@ -112,9 +130,11 @@ def clear_plans() -> None:
 def _plan(key, build, cat) -> Plan:
     plan = _plans.get(key)
     if plan is None:
+        if len(_plans) >= _PLAN_BUDGET:
+            clear_plans()
         handle = vp()
         check(build(ctypes.byref(handle)))
-        plan = Plan(handle, cat)
+        plan = Plan(handle, cat, key, build)
         _plans[key] = plan
     return plan
 

@@ -301,3 +301,25 @@ def test_compiled_leg_moves_are_the_composed_step_plans():
             assert np.array_equal(got, want), (cat.name, legs, height, above, below)
             checked += 1
     assert checked >= 20
+
+
+def test_plan_cache_clears_wholesale_at_its_budget_and_held_plans_recompile(monkeypatch):
+    '''Past the budget the whole plan cache goes (tentorch/tensors/cache.cpp:203-217); a Plan held
+    across the clear compiles its program again on its next use and describes the same program.'''
+    import torch
+    import tentorch_gb300 as tg
+    from tentorch_gb300 import linalg as la
+    monkeypatch.setattr(la, '_PLAN_BUDGET', 3)
+    la.clear_plans()
+    cat = tg.u1
+    plans = []
+    for m in range(1, 6):
+        leg = tg.Leg(cat, [(0,), (2,)], [m, m + 1])
+        t = tg.Tensor(cat, [leg], [leg], (0,), dtype = torch.float64, device = 'cpu')
+        plans.append(la.plan_of('ab,bc->ac', t, t))
+        assert len(la._plans) <= 3
+    first = plans[0]
+    text = first.describe()
+    assert first.generation == la._generation
+    assert first.describe() == text
+    la.clear_plans()
