@@ -170,14 +170,17 @@ int32_t tt_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const 
 
 /* Thin SVDs of `count` float64 blocks in one launch (one-sided Jacobi, mixed precision: FP32 sweeps,
  * then FP64 re-orthonormalisation and FP64 sweeps to full accuracy; a thread-block cluster per
- * block; replaces the per-block at::linalg_svd of svd.cpp:57-62).  `table` is a DEVICE array of 7 int64 per block:
- * a_off, rows, cols, u_off, s_off, vh_off, ws_off (offsets in doubles).  Block i is rows x cols
- * row-major at a + a_off; with k = min(rows, cols) <= 1024 it writes U (rows x k, row-major) at
- * u + u_off, the k singular values in descending order at s + s_off and Vh (k x cols, row-major)
- * at vh + vh_off.  ws_off places the block's working set in `workspace` (from tt_svd_workspace).  info[i] (device int32) receives the FP64 sweeps block i took, -1 when
- * they did not converge (then its factors are not to be used).  Asynchronous on `stream`. */
-int32_t tt_svd_blocks(int32_t count, const int64_t *table, const double *a, double *u, double *s, double *vh,
-                      double *workspace, int32_t *info, void *stream);
+ * block; replaces the per-block at::linalg_svd of svd.cpp:57-62).  `table` is a DEVICE array of 7
+ * int64 per block: a_off, rows, cols, u_off, s_off, vh_off, ws_off (offsets in doubles), best
+ * ordered largest block first; `largest` is the largest min(rows, cols) among them (it sets the
+ * cluster size).  Block i is rows x cols row-major at a + a_off; with k = min(rows, cols) <= 1024
+ * it writes U (rows x k, row-major) at u + u_off, the k singular values in descending order at
+ * s + s_off and Vh (k x cols, row-major) at vh + vh_off.  ws_off places the block's working set in
+ * `workspace` (from tt_svd_workspace).  info[i] (device int32) receives the FP64 sweeps block i
+ * took, -1 when they did not converge (then its factors are not to be used).  Asynchronous on
+ * `stream`. */
+int32_t tt_svd_blocks(int32_t count, int64_t largest, const int64_t *table, const double *a, double *u, double *s,
+                      double *vh, double *workspace, int32_t *info, void *stream);
 /* The workspace of tt_svd_blocks: for `count` blocks (host array of rows, cols per block) the
  * offset in doubles of each block's working set in the workspace (-1 for an empty block) and the
  * doubles the workspace needs in all. */

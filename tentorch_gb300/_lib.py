@@ -64,7 +64,7 @@ _declare('tt_dots_noalloc', i32, i32, vp, vp, i64, vp, vp)
 _declare('tt_svd_workspace', i32, P(i64), P(i64), P(i64))
 _declare('tt_lanczos_scratch', i64, i32, i32, P(i64))
 _declare('tt_lanczos', vp, i32, i32, P(vp), P(vp), i32, vp, i32, f64, vp, vp, vp, P(f64), P(i32), vp)
-_declare('tt_svd_blocks', i32, vp, vp, vp, vp, vp, vp, vp, vp)
+_declare('tt_svd_blocks', i32, i64, vp, vp, vp, vp, vp, vp, vp, vp)
 _declare('tt_svd_keep', i32, vp, vp, vp, vp, vp, vp, vp, vp)
 
 _ERRORS = {1: ValueError, 2: IndexError, 3: RuntimeError, 4: RuntimeError}

@@ -679,11 +679,13 @@ extern "C"
     });
   }
 
-  int32_t tt_svd_blocks(int32_t count, const int64_t *table, const double *a, double *u, double *s, double *vh,
-                        double *workspace, int32_t *info, void *stream)
+  int32_t tt_svd_blocks(int32_t count, int64_t largest, const int64_t *table, const double *a, double *u, double *s,
+                        double *vh, double *workspace, int32_t *info, void *stream)
   {
     if (count < 0) return fail(TT_EINVAL, "a negative block count");
-    const cudaError_t e = ttg::svd_blocks(count, table, a, u, s, vh, workspace, info, static_cast<cudaStream_t>(stream));
+    if (largest < 0 || largest > 1024) return fail(TT_EINVAL, "the largest block of the batched SVD needs 0 to 1024 columns");
+    const cudaError_t e =
+      ttg::svd_blocks(count, largest, table, a, u, s, vh, workspace, info, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
     return TT_OK;
   }

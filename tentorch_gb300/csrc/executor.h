@@ -111,7 +111,7 @@ namespace ttg
   // block (a_off, rows, cols, u_off, s_off, vh_off, ws_off); info[i] = Jacobi sweeps, -1 when block
   // i did not converge.  svd_keep writes the kept factors into the split's arenas (12 int64-sized
   // fields per block, see svd.cu).
-  cudaError_t svd_blocks(int32_t count, const void *table, const double *a, double *u, double *s, double *vh,
+  cudaError_t svd_blocks(int32_t count, int64_t largest, const void *table, const double *a, double *u, double *s, double *vh,
                          void *workspace, int32_t *info, cudaStream_t stream);
   // doubles of global workspace one block needs (0 when its working set fits in shared memory)
   int64_t svd_workspace_doubles(int64_t rows, int64_t cols);

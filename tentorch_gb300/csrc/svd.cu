@@ -20,8 +20,8 @@
 //      convergence needs two sweeps and a third that finds nothing to rotate.
 // In the FP64 sweeps only the dot product of the pair is taken (the squared column norms are
 // carried along with the exact update of a rotation and recomputed at each sweep's start), and the
-// angle is found in FP32 and then made exactly orthogonal in FP64 (c^2 + s^2 = 1 by two Newton
-// steps): an angle good to 1e-7 still shrinks the pair's cosine by that factor each rotation.
+// angle is found in FP32 and then made exactly orthogonal in FP64 (c^2 + s^2 = 1 by a second-order
+// correction): an angle good to 1e-7 still shrinks the pair's cosine by that factor each rotation.
 //
 // A thread-block cluster of up to 8 CTAs (1024 threads each) per block.  Rank 0 runs step 1 alone;
 // steps 2-4 run on the whole cluster, step 4 with the rows of W and V dealt to the ranks and the
@@ -52,14 +52,24 @@ namespace ttg
   {
     namespace cg = cooperative_groups;
 
-    constexpr int kSvdThreads = 1024;
+    constexpr int kSvdThreads = 512;
     constexpr int kMaxSweeps = 40;
     constexpr int kMaxCols = 1024;              // k = min(rows, cols) of a block
     constexpr int kMaxPairs = kMaxCols / 2;     // pairs of a round
     constexpr int kSvdSmemBytes = 227 * 1024;
-    constexpr int kStaticBytes = 29 * 1024;     // the shares, norms, ranks and flags of the kernel
+    constexpr int kStaticBytes = 21 * 1024;     // the norms, their shares, ranks and flags of the kernel
     constexpr int64_t kDynamicBytes = kSvdSmemBytes - kStaticBytes - 1024;
-    constexpr int kMaxCluster = 8;
+    constexpr int kTile = 32;                   // tiles of the Newton-Schulz and W = A V products
+    constexpr int64_t kStageBytes = 2 * kTile * (kTile + 1) * 8;
+    // the end of the dynamic shared memory holds the tile stages (Newton-Schulz, W = A V) or, during
+    // sweeps over a cluster, the dot-product shares every rank pushes to every rank
+    __host__ __device__ inline int64_t exchange_bytes(int64_t k, int64_t ranks, int64_t size)
+    {
+      const int64_t pairs = (k + (k & 1)) / 2;
+      return ranks > 1 ? (2 * ranks * pairs * size + 15) / 16 * 16 : 0;
+    }
+    constexpr int kMaxCluster = 16;
+    constexpr int kNper = 12;                   // entries of a column each lane of a pair holds
 
     // per block: a_off, rows, cols, u_off, s_off, vh_off, ws_off (doubles)
     struct SvdEntry
@@ -68,50 +78,48 @@ namespace ttg
     };
 
     // One block's global workspace, in doubles: V and its next iterate (k x k each) and G = V^T V
-    // for the Newton-Schulz steps; W (len x k) and V by rank for clusters whose rows do not fit in
-    // shared memory (up to kMaxCluster - 1 padding rows each); rank 0's FP32 working set (W, V,
-    // norms) when it does not fit in shared memory.
+    // for the Newton-Schulz steps; W (len x k) and V (k x k) by rank for working sets that do not
+    // fit in shared memory (up to kMaxCluster - 1 padding rows each), in FP64 and again in FP32.
     struct SvdLayout
     {
-      int64_t v0, v1, g, w_slices, v_slices, leader, total;
-      bool leader_in_smem;
+      int64_t v0, v1, g, w_slices, v_slices, w32_slices, v32_slices, total;
     };
     __host__ __device__ inline SvdLayout svd_layout(int64_t len, int64_t k)
     {
       SvdLayout l;
-      const int64_t leader_bytes = (len * k + k * k + k) * 4 + 256;
-      l.leader_in_smem = leader_bytes <= kDynamicBytes;
       l.v0 = 0;
       l.v1 = k * k;
       l.g = 2 * k * k;
       l.w_slices = 3 * k * k;
       l.v_slices = l.w_slices + (len + kMaxCluster) * k;
-      l.leader = l.v_slices + (k + kMaxCluster) * k;
-      l.total = l.leader + (l.leader_in_smem ? 0 : (leader_bytes + 7) / 8);
+      l.w32_slices = l.v_slices + (k + kMaxCluster) * k;
+      l.v32_slices = l.w32_slices + ((len + kMaxCluster) * k + 1) / 2;
+      l.total = l.v32_slices + ((k + kMaxCluster) * k + 1) / 2;
       l.total = (l.total + 31) / 32 * 32;
       return l;
     }
 
-    // The circle method's pair t of a round (players even): player players - 1 stays, the others
-    // turn; p < q.
+    // The circle method's pair t of a round (players even, round < players - 1, t < players / 2):
+    // player players - 1 stays, the others turn; p < q.  In 32-bit arithmetic with one conditional
+    // subtraction each instead of a 64-bit remainder, which costs a long instruction sequence.
     __device__ __forceinline__ void circle_pair(int64_t round, int64_t t, int64_t players, int64_t &p, int64_t &q)
     {
-      if (t == 0)
+      const int32_t n = static_cast<int32_t>(players - 1), r = static_cast<int32_t>(round), u = static_cast<int32_t>(t);
+      int32_t a, b;
+      if (u == 0)
       {
-        p = round;
-        q = players - 1;
+        a = r;
+        b = n;
       }
       else
       {
-        p = (round + t) % (players - 1);
-        q = (round - t + players - 1) % (players - 1);
+        a = r + u;
+        if (a >= n) a -= n;
+        b = r - u + n;
+        if (b >= n) b -= n;
       }
-      if (p > q)
-      {
-        const int64_t lower = q;
-        q = p;
-        p = lower;
-      }
+      p = a < b ? a : b;
+      q = a < b ? b : a;
     }
 
     template <typename T>
@@ -150,9 +158,6 @@ namespace ttg
                       static_cast<float>(ldexp(gamma, -ex)), c, s);
     }
 
-    // One Jacobi phase over W (len x k, column-major) with the rotations accumulated into V (k x k).
-    // FP32: everything in FP32.  FP64: the dot products, updates and norms in FP64, the angle in
-    // FP32 made exactly orthogonal.  Returns the sweeps taken, -1 when kMaxSweeps did not do.
     template <typename T, int G>
     __device__ __forceinline__ T group_sum(T v)
     {
@@ -161,228 +166,285 @@ namespace ttg
       return v;
     }
 
-    // One Jacobi phase over W (len x k, column-major) with the rotations accumulated into V (k x k).
-    // FP32: everything in FP32.  FP64: the dot products, updates and norms in FP64, the angle in
-    // FP32 made exactly orthogonal.  A group of G lanes takes a pair (G = 8 for columns of up to 128
-    // entries, so a warp rotates four pairs at once and a dot product needs three shuffle steps, not
-    // five: FP64 instructions cost the same however few lanes they serve).  Returns the sweeps taken,
-    // -1 when kMaxSweeps did not do.
+    // A pair's columns as a group of G lanes holds them: lane gl has entries gl, gl + G, ... of
+    // each, the first kNper in registers (loads issued together, one latency), any further ones
+    // read again where needed.  Register slots past the column's length are skipped whole (the
+    // count is the same for every lane), so no FP64 instruction is spent on padding.
     template <typename T, int G>
-    __device__ int jacobi_phase(T *w, T *v, T *norms, int64_t len, int64_t k, double tol, int *rotated)
+    __device__ __forceinline__ T pair_dot(const T *wp, const T *wq, int64_t n, int gl, T (&x)[kNper], T (&y)[kNper])
     {
+      const int64_t slots = (n + G - 1) / G;
+#pragma unroll
+      for (int u = 0; u < kNper; ++u)
+      {
+        const int64_t i = gl + static_cast<int64_t>(u) * G;
+        x[u] = u < slots && i < n ? wp[i] : T(0);
+        y[u] = u < slots && i < n ? wq[i] : T(0);
+      }
+      T sum = 0;
+#pragma unroll
+      for (int u = 0; u < kNper; ++u)
+        if (u < slots) sum = fma(x[u], y[u], sum);
+      for (int64_t i = static_cast<int64_t>(G) * kNper + gl; i < n; i += G) sum = fma(wp[i], wq[i], sum);
+      return sum;
+    }
+
+    template <typename T, int G>
+    __device__ __forceinline__ void pair_rotate(T *wp, T *wq, int64_t n, int gl, const T (&x)[kNper], const T (&y)[kNper],
+                                                T c, T sn)
+    {
+      const int64_t slots = (n + G - 1) / G;
+#pragma unroll
+      for (int u = 0; u < kNper; ++u)
+      {
+        const int64_t i = gl + static_cast<int64_t>(u) * G;
+        if (u < slots && i < n)
+        {
+          wp[i] = fma(c, x[u], -sn * y[u]);
+          wq[i] = fma(sn, x[u], c * y[u]);
+        }
+      }
+      for (int64_t i = static_cast<int64_t>(G) * kNper + gl; i < n; i += G)
+      {
+        const T a = wp[i], b = wq[i];
+        wp[i] = fma(c, a, -sn * b);
+        wq[i] = fma(sn, a, c * b);
+      }
+    }
+
+    // rotate two columns in chunks of kNper entries per lane (each chunk's loads issued together)
+    template <typename T, int G>
+    __device__ __forceinline__ void cols_rotate(T *vp, T *vq, int64_t n, int gl, T c, T sn)
+    {
+      for (int64_t base = 0; base < n; base += static_cast<int64_t>(G) * kNper)
+      {
+        const int64_t slots = (n - base + G - 1) / G;
+        T x[kNper], y[kNper];
+#pragma unroll
+        for (int u = 0; u < kNper; ++u)
+        {
+          const int64_t i = base + gl + static_cast<int64_t>(u) * G;
+          x[u] = u < slots && i < n ? vp[i] : T(0);
+          y[u] = u < slots && i < n ? vq[i] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kNper; ++u)
+        {
+          const int64_t i = base + gl + static_cast<int64_t>(u) * G;
+          if (u < slots && i < n)
+          {
+            vp[i] = fma(c, x[u], -sn * y[u]);
+            vq[i] = fma(sn, x[u], c * y[u]);
+          }
+        }
+      }
+    }
+
+    // The rotation of a pair as FP64 values with c^2 + s^2 = 1 to FP64 precision, from the FP32
+    // angle: with c, s exact in FP64, d = c^2 + s^2 - 1 (~1e-7) is exact to FP64 rounding and
+    // 1 / sqrt(1 + d) = 1 - d/2 + 3 d^2/8 to below 1e-20.
+    __device__ __forceinline__ void exact_rotation(float cf, float sf, double &c, double &sn)
+    {
+      c = cf;
+      sn = sf;
+      const double d = fma(sn, sn, fma(c, c, -1.0));
+      const double f = fma(d, fma(0.375, d, -0.5), 1.0);
+      c *= f;
+      sn *= f;
+    }
+    __device__ __forceinline__ void exact_rotation(float cf, float sf, float &c, float &sn)
+    {
+      c = cf;
+      sn = sf;
+    }
+
+    // Jacobi sweeps over W (column-major, `rows` rows) with the rotations accumulated into V
+    // (`vrows` rows), until a sweep rotates nothing (or kMaxSweeps).  Alone, one CTA holds every
+    // row; otherwise the rows are dealt to the CTAs of the cluster: per round each CTA takes its
+    // rows' share of every pair's dot product, the shares cross the cluster through distributed
+    // shared memory and every CTA adds them in the same order, so that all hold the same dot
+    // products, angles and norms, and rotates its own rows.  One cluster barrier per round (shares
+    // double-buffered) and two per sweep; whether a sweep rotated anything is read from rank 0, so
+    // every CTA leaves the loop together.  FP32: everything in FP32; FP64: the angle in FP32 made
+    // exactly orthogonal in FP64 (exact_rotation; an angle good to 1e-7 still shrinks the pair's
+    // cosine by that factor each rotation).  Only the pair's dot product is taken: the squared norms are
+    // recomputed at each sweep's start and carried with each rotation's exact update.
+    template <typename T, int G>
+    __device__ int sweeps(const cg::cluster_group &cluster, bool alone, T *w, int64_t rows, T *v, int64_t vrows, int64_t k,
+                          double tol, T *norms, T *exchange, T *partial, int *flags)
+    {
+      const unsigned ranks = alone ? 1u : cluster.num_blocks(), me = alone ? 0u : cluster.block_rank();
+      const auto sync = [&] {
+        if (alone) __syncthreads();
+        else cluster.sync();
+      };
+      const auto at_rank = [&](T *local, unsigned r) -> const T * { return alone ? local : cluster.map_shared_rank(local, r); };
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
       const int group = lane / G, gl = lane % G;
       constexpr int per_warp = 32 / G;
-      const int64_t players = k + (k & 1);  // a dummy column pairs with the odd one out
+      const int64_t players = k + (k & 1), pairs = players / 2;
       const T tol2 = static_cast<T>(tol * tol);
       for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
       {
-        // exact squared norms at the start of every sweep
         for (int64_t j = warp; j < k; j += warps)
         {
-          const T *wj = w + j * len;
+          const T *wj = w + j * rows;
           T sum = 0;
-          for (int64_t i = lane; i < len; i += 32) sum = fma(wj[i], wj[i], sum);
+          for (int64_t i = lane; i < rows; i += 32) sum = fma(wj[i], wj[i], sum);
           sum = warp_sum(sum);
-          if (lane == 0) norms[j] = sum;
+          if (lane == 0) partial[j] = sum;
         }
-        if (threadIdx.x == 0) *rotated = 0;
+        if (threadIdx.x == 0) flags[sweep & 1] = 0;
+        sync();
+        for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
+        {
+          T sum = 0;
+          for (unsigned r = 0; r < ranks; ++r) sum += at_rank(partial, r)[j];
+          norms[j] = sum;
+        }
         __syncthreads();
         for (int64_t round = 0; round + 1 < players; ++round)
         {
-          // every group of the warp walks the same number of turns, so the shuffles stay converged
-          for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < players / 2; t0 += static_cast<int64_t>(warps) * per_warp)
+          // this round's shares: [rank][pair], double-buffered by rounds
+          T *share = exchange + (round & 1) * static_cast<int64_t>(ranks) * pairs;
+          // every group of a warp walks the same number of turns, so the shuffles stay converged
+          for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
           {
             const int64_t t = t0 + group;
             int64_t p, q;
             circle_pair(round, t, players, p, q);
-            const bool pair = t < players / 2 && q < k;  // not past the round, not the dummy
-            T *wp = w + (pair ? p : 0) * len, *wq = w + (pair ? q : 0) * len;
-            T gamma = 0;
-            if (pair)
-              for (int64_t i = gl; i < len; i += G) gamma = fma(wp[i], wq[i], gamma);
+            const bool pair = t < pairs && q < k;
+            T x[kNper], y[kNper];
+            T *wp = w + (pair ? p : 0) * rows, *wq = w + (pair ? q : 0) * rows;
+            T gamma = pair_dot<T, G>(wp, wq, pair ? rows : 0, gl, x, y);
             gamma = group_sum<T, G>(gamma);
-            if (!pair) continue;
-            const T alpha = norms[p], beta = norms[q];
-            // orthogonal to working precision: cos^2 of the pair's angle below tol^2
-            if (gamma * gamma <= tol2 * alpha * beta) continue;
-            float cf, sf;
-            if (!angle(alpha, beta, gamma, cf, sf)) continue;
-            T c = cf, sn = sf;
-            if (sizeof(T) == 8)
+            if (!alone && t < pairs)
             {
-              // c^2 + s^2 = 1 to FP64 precision: two Newton steps on 1 / sqrt(c^2 + s^2)
-#pragma unroll
-              for (int it = 0; it < 2; ++it)
+              // this CTA's share goes to every rank (remote stores do not wait); after the barrier
+              // each rank holds every share in its own memory
+              for (unsigned r = gl; r < ranks; r += G) cluster.map_shared_rank(share + static_cast<int64_t>(me) * pairs + t, r)[0] = gamma;
+            }
+            if (alone)
+            {
+              if (!pair) continue;
+              const T alpha = norms[p], beta = norms[q];
+              if (gamma * gamma <= tol2 * alpha * beta) continue;
+              float cf, sf;
+              if (!angle(alpha, beta, gamma, cf, sf)) continue;
+              T c, sn;
+              exact_rotation(cf, sf, c, sn);
+              pair_rotate<T, G>(wp, wq, rows, gl, x, y, c, sn);
+              cols_rotate<T, G>(v + p * vrows, v + q * vrows, vrows, gl, c, sn);
+              if (gl == 0)
               {
-                const T f = static_cast<T>(1.5) - static_cast<T>(0.5) * fma(c, c, sn * sn);
-                c *= f;
-                sn *= f;
+                const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
+                norms[p] = cc * alpha - cs2 + ss * beta;
+                norms[q] = ss * alpha + cs2 + cc * beta;
+                flags[sweep & 1] = 1;
               }
             }
-            for (int64_t i = gl; i < len; i += G)
+          }
+          if (!alone)
+          {
+            cluster.sync();
+            for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
             {
-              const T x = wp[i], y = wq[i];
-              wp[i] = fma(c, x, -sn * y);
-              wq[i] = fma(sn, x, c * y);
-            }
-            T *vp = v + p * k, *vq = v + q * k;
-            for (int64_t i = gl; i < k; i += G)
-            {
-              const T x = vp[i], y = vq[i];
-              vp[i] = fma(c, x, -sn * y);
-              vq[i] = fma(sn, x, c * y);
-            }
-            if (gl == 0)
-            {
-              const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
-              norms[p] = cc * alpha - cs2 + ss * beta;
-              norms[q] = ss * alpha + cs2 + cc * beta;
-              *rotated = 1;
+              const int64_t t = t0 + group;
+              int64_t p, q;
+              circle_pair(round, t, players, p, q);
+              const bool pair = t < pairs && q < k;
+              // lane gl adds ranks gl, gl + G, ...; the group's butterfly sum then gives every lane
+              // of every CTA the same value
+              T gamma = 0;
+              if (pair)
+                for (unsigned r = gl; r < ranks; r += G) gamma += share[static_cast<int64_t>(r) * pairs + t];
+              gamma = group_sum<T, G>(gamma);
+              if (!pair) continue;
+              const T alpha = norms[p], beta = norms[q];
+              if (gamma * gamma <= tol2 * alpha * beta) continue;
+              float cf, sf;
+              if (!angle(alpha, beta, gamma, cf, sf)) continue;
+              T c, sn;
+              exact_rotation(cf, sf, c, sn);
+              cols_rotate<T, G>(w + p * rows, w + q * rows, rows, gl, c, sn);
+              cols_rotate<T, G>(v + p * vrows, v + q * vrows, vrows, gl, c, sn);
+              if (gl == 0)
+              {
+                const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
+                norms[p] = cc * alpha - cs2 + ss * beta;
+                norms[q] = ss * alpha + cs2 + cc * beta;
+                flags[sweep & 1] = 1;
+              }
             }
           }
           __syncthreads();
         }
-        const int any = *rotated;
-        __syncthreads();
+        sync();
+        const int any = alone ? flags[sweep & 1] : cluster.map_shared_rank(flags, 0)[sweep & 1];
         if (!any) return sweep + 1;
       }
       return -1;
     }
 
     template <typename T>
-    __device__ int jacobi_phase(T *w, T *v, T *norms, int64_t len, int64_t k, double tol, int *rotated)
+    __device__ int sweeps(const cg::cluster_group &cluster, bool alone, T *w, int64_t rows, T *v, int64_t vrows, int64_t k,
+                          double tol, T *norms, T *exchange, T *partial, int *flags)
     {
-      if (len <= 128) return jacobi_phase<T, 8>(w, v, norms, len, k, tol, rotated);
-      return jacobi_phase<T, 32>(w, v, norms, len, k, tol, rotated);
+      const int64_t most = rows > vrows ? rows : vrows;
+      if (most <= 4 * kNper) return sweeps<T, 4>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
+      if (most <= 8 * kNper) return sweeps<T, 8>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
+      if (most <= 16 * kNper) return sweeps<T, 16>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
+      return sweeps<T, 32>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
     }
 
-    // The sweeps of a phase distributed over the CTAs of a cluster by rows: rank r holds `rows`
-    // rows of W (column-major, leading dimension `rows`) and `vrows` rows of V (leading dimension
-    // `vrows`).  Per round every CTA takes its rows' share of each pair's dot product, the shares
-    // cross the cluster through distributed shared memory, and every CTA adds them in the same
-    // order, so that all hold the same dot products, angles and norms; each then rotates its own
-    // rows.  One cluster barrier per round (shares double-buffered) and two per sweep.  Whether a
-    // sweep rotated anything is read from rank 0 so that every CTA leaves the loop together.
-    template <int G>
-    __device__ int cluster_sweeps(const cg::cluster_group &cluster, double *w, int64_t rows, double *v, int64_t vrows,
-                                  int64_t k, double tol, double *norms, double *shares, double *partial, int *flags)
+    // out(i, j) = sum_x a(x, i) b(x, j) + c(i, j) over a kTile x kTile tile, x < depth, staged
+    // kTile at a time in shared memory (a(x, i) from fa(x, i), b from fb; zero outside), with Acc
+    // accumulation; each of the 512 threads takes two entries (i, j) and (i, j + 16).  The loaders
+    // are called with x fastest across the threads when `x_fast`, else i (or j) fastest, to follow
+    // the memory order of the operand.
+    template <typename Acc, typename FA, typename FB, typename Out>
+    __device__ void tile_product(int64_t depth, FA fa, bool a_x_fast, FB fb, bool b_x_fast, Acc *sa, Acc *sb, Out out)
     {
-      const unsigned ranks = cluster.num_blocks();
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-      const int group = lane / G, gl = lane % G;
-      constexpr int per_warp = 32 / G;
-      const int64_t players = k + (k & 1), pairs = players / 2;
-      const double tol2 = tol * tol;
-      for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
+      constexpr int P = kTile + 1;
+      const int t = threadIdx.x, i = t % kTile, j = t / kTile;
+      Acc acc0 = 0, acc1 = 0;
+      for (int64_t x0 = 0; x0 < depth; x0 += kTile)
       {
-        // exact squared norms: this CTA's share of each, summed over the cluster in rank order
-        for (int64_t j = warp; j < k; j += warps)
+        for (int e = t; e < kTile * kTile; e += blockDim.x)
         {
-          const double *wj = w + j * rows;
-          double sum = 0;
-          for (int64_t i = lane; i < rows; i += 32) sum = fma(wj[i], wj[i], sum);
-          sum = warp_sum(sum);
-          if (lane == 0) partial[j] = sum;
-        }
-        if (threadIdx.x == 0) flags[sweep & 1] = 0;
-        cluster.sync();
-        for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
-        {
-          double sum = 0;
-          for (unsigned r = 0; r < ranks; ++r) sum += cluster.map_shared_rank(partial, r)[j];
-          norms[j] = sum;
+          const int fast = e % kTile, slow = e / kTile;
+          const int xa = a_x_fast ? fast : slow, ia = a_x_fast ? slow : fast;
+          sa[xa * P + ia] = x0 + xa < depth ? static_cast<Acc>(fa(x0 + xa, ia)) : Acc(0);
+          const int xb = b_x_fast ? fast : slow, jb = b_x_fast ? slow : fast;
+          sb[xb * P + jb] = x0 + xb < depth ? static_cast<Acc>(fb(x0 + xb, jb)) : Acc(0);
         }
         __syncthreads();
-        for (int64_t round = 0; round + 1 < players; ++round)
+#pragma unroll 8
+        for (int x = 0; x < kTile; ++x)
         {
-          double *share = shares + (round & 1) * kMaxPairs;
-          // this CTA's share of the dot product of every pair of the round
-          for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
-          {
-            const int64_t t = t0 + group;
-            int64_t p, q;
-            circle_pair(round, t, players, p, q);
-            const bool pair = t < pairs && q < k;
-            const double *wp = w + (pair ? p : 0) * rows, *wq = w + (pair ? q : 0) * rows;
-            double gamma = 0;
-            if (pair)
-              for (int64_t i = gl; i < rows; i += G) gamma = fma(wp[i], wq[i], gamma);
-            gamma = group_sum<double, G>(gamma);
-            if (t < pairs && gl == 0) share[t] = gamma;
-          }
-          cluster.sync();
-          for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
-          {
-            const int64_t t = t0 + group;
-            int64_t p, q;
-            circle_pair(round, t, players, p, q);
-            const bool pair = t < pairs && q < k;
-            // the shares of the cluster: lane gl adds ranks gl, gl + G, ...; the group's butterfly
-            // sum then gives every lane of every CTA the same value
-            double gamma = 0;
-            if (pair)
-              for (unsigned r = gl; r < ranks; r += G) gamma += cluster.map_shared_rank(share, r)[t];
-            gamma = group_sum<double, G>(gamma);
-            if (!pair) continue;
-            const double alpha = norms[p], beta = norms[q];
-            if (gamma * gamma <= tol2 * alpha * beta) continue;
-            float cf, sf;
-            if (!angle(alpha, beta, gamma, cf, sf)) continue;
-            double c = cf, sn = sf;
-#pragma unroll
-            for (int it = 0; it < 2; ++it)
-            {
-              const double f = 1.5 - 0.5 * fma(c, c, sn * sn);
-              c *= f;
-              sn *= f;
-            }
-            double *wp = w + p * rows, *wq = w + q * rows;
-            for (int64_t i = gl; i < rows; i += G)
-            {
-              const double x = wp[i], y = wq[i];
-              wp[i] = fma(c, x, -sn * y);
-              wq[i] = fma(sn, x, c * y);
-            }
-            double *vp = v + p * vrows, *vq = v + q * vrows;
-            for (int64_t i = gl; i < vrows; i += G)
-            {
-              const double x = vp[i], y = vq[i];
-              vp[i] = fma(c, x, -sn * y);
-              vq[i] = fma(sn, x, c * y);
-            }
-            if (gl == 0)
-            {
-              const double cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
-              norms[p] = cc * alpha - cs2 + ss * beta;
-              norms[q] = ss * alpha + cs2 + cc * beta;
-              flags[sweep & 1] = 1;
-            }
-          }
-          __syncthreads();
+          const Acc ax = sa[x * P + i];
+          acc0 = fma(ax, sb[x * P + j], acc0);
+          acc1 = fma(ax, sb[x * P + j + 16], acc1);
         }
-        cluster.sync();
-        const int any = cluster.map_shared_rank(flags, 0)[sweep & 1];
-        if (!any) return sweep + 1;
+        __syncthreads();
       }
-      return -1;
+      out(i, j, acc0);
+      out(i, j + 16, acc1);
     }
 
-    // A cluster of CTAs per block (grid = blocks x cluster size).  Rank 0 runs the FP32 sweeps alone
-    // (they are cheap and latency-bound: a cluster barrier per round would cost more than it
-    // saves); the cluster then shares the Newton-Schulz steps, forms its rows of W = A V, and runs
-    // the FP64 sweeps on rows dealt to the ranks.  Per block, the global workspace holds V twice
-    // and G = V^T V for the exchange, W and V by rank when a rank's rows do not fit in shared
-    // memory, and rank 0's FP32 working set when that does not fit.
+    // A thread-block cluster of up to 16 CTAs per block (grid = blocks x cluster size, the largest
+    // blocks first).  The FP32 sweeps run on rank 0 alone when its working set fits in shared
+    // memory (a cluster barrier per round would cost more than it saves), else over the cluster;
+    // the cluster shares the Newton-Schulz steps and W = A V as 32 x 32 tiles; the FP64 sweeps run
+    // over the cluster for blocks of 32 columns or more, on rank 0 alone for smaller ones.
     __global__ void __launch_bounds__(kSvdThreads, 1)
       jacobi_svd_kernel(const SvdEntry *__restrict__ table, const double *__restrict__ a, double *__restrict__ u,
                         double *__restrict__ s, double *__restrict__ vh, double *__restrict__ workspace,
                         int32_t *__restrict__ info)
     {
       extern __shared__ __align__(16) unsigned char dynamic[];
-      __shared__ double shares[2 * kMaxPairs];
-      __shared__ double norms[kMaxCols];
-      __shared__ double partial[kMaxCols];
+      __shared__ double norms_raw[kMaxCols];
+      __shared__ double partial_raw[kMaxCols];
       __shared__ int rank_of[kMaxCols];
       __shared__ int flags[2];
       __shared__ double big;
@@ -401,65 +463,119 @@ namespace ttg
       const SvdLayout lay = svd_layout(len, k);
       double *ws = workspace + e.ws_off;
       double *v_cur = ws + lay.v0, *v_next = ws + lay.v1, *g = ws + lay.g;
+      double *stage = reinterpret_cast<double *>(dynamic + kDynamicBytes - kStageBytes);
       const double *src = a + e.a_off;
       const auto entry = [&](int64_t row, int64_t col) -> double
       { return wide ? src[col * n + row] : src[row * n + col]; };  // row < len, col < k
 
-      // 1. rank 0: FP32 sweeps on the block scaled to |entries| <= 1; V32 goes out as V in FP64
-      if (rank == 0)
+      // 1. FP32 sweeps on the block scaled to |entries| <= 1, from V = I; V goes out in FP64.
+      // Rank 0 alone when W and V fit in its shared memory, else rows dealt over the cluster.
       {
-        unsigned char *base = lay.leader_in_smem ? dynamic : reinterpret_cast<unsigned char *>(ws + lay.leader);
-        float *w32 = reinterpret_cast<float *>(base);
-        float *v32 = w32 + len * k;
-        float *norms32 = v32 + k * k;
-        if (threadIdx.x == 0) big = 0.0;
-        __syncthreads();
+        const bool alone = (len * k + k * k) * 4 <= kDynamicBytes;
+        const int64_t rows = alone ? len : (len + ranks - 1) / ranks, vrows = alone ? k : (k + ranks - 1) / ranks;
+        const int64_t r0 = alone ? 0 : min(len, static_cast<int64_t>(rank) * rows), r1 = alone ? len : min(len, r0 + rows);
+        const int64_t c0 = alone ? 0 : min(k, static_cast<int64_t>(rank) * vrows), c1 = alone ? k : min(k, c0 + vrows);
+        const int64_t swap32 = exchange_bytes(k, alone ? 1 : ranks, 4);
+        const bool in_smem = (rows + vrows) * k * 4 + swap32 <= kDynamicBytes;
+        float *w32 = in_smem ? reinterpret_cast<float *>(dynamic)
+                             : reinterpret_cast<float *>(ws + lay.w32_slices) + static_cast<int64_t>(rank) * rows * k;
+        float *v32 = in_smem ? w32 + rows * k : reinterpret_cast<float *>(ws + lay.v32_slices) + static_cast<int64_t>(rank) * vrows * k;
+        if (alone ? rank == 0 : true)
         {
+          // the largest |entry| of the block (of this rank's rows, then over the cluster)
+          if (threadIdx.x == 0) big = 0.0;
+          __syncthreads();
           double local = 0.0;
-          for (int64_t i = threadIdx.x; i < len * k; i += blockDim.x) local = fmax(local, fabs(entry(i % len, i / len)));
+          for (int64_t i = threadIdx.x; i < (r1 - r0) * k; i += blockDim.x)
+            local = fmax(local, fabs(entry(r0 + i % (r1 - r0), i / (r1 - r0))));
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, o));
           if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long *>(&big), __double_as_longlong(local));
+          __syncthreads();
         }
-        __syncthreads();
-        const double scale = big > 0.0 ? 1.0 / big : 1.0;
-        for (int64_t i = threadIdx.x; i < len * k; i += blockDim.x)
-          w32[i] = static_cast<float>(entry(i % len, i / len) * scale);
-        for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x) v32[i] = (i / k == i % k) ? 1.0f : 0.0f;
-        __syncthreads();
-        jacobi_phase<float>(w32, v32, norms32, len, k, 1e-5, flags);
-        for (int64_t i = threadIdx.x; i < k * k; i += blockDim.x) v_cur[i] = static_cast<double>(v32[i]);
+        if (!alone)
+        {
+          if (threadIdx.x == 0) partial_raw[0] = big;
+          cluster.sync();
+          if (threadIdx.x == 0)
+          {
+            double most = 0.0;
+            for (unsigned r = 0; r < ranks; ++r) most = fmax(most, cluster.map_shared_rank(partial_raw, r)[0]);
+            big = most;
+          }
+          __syncthreads();
+        }
+        if (alone ? rank == 0 : true)
+        {
+          const double scale = big > 0.0 ? 1.0 / big : 1.0;
+          for (int64_t i = threadIdx.x; i < rows * k; i += blockDim.x)
+          {
+            const int64_t row = r0 + i % rows;
+            w32[i] = row < r1 ? static_cast<float>(entry(row, i / rows) * scale) : 0.0f;
+          }
+          for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
+            v32[i] = (c0 + i % vrows == i / vrows && c0 + i % vrows < c1) ? 1.0f : 0.0f;
+          __syncthreads();
+        }
+        if (!alone) cluster.sync();  // every rank's partial_raw read before it holds norms
+        if (alone ? rank == 0 : true)
+        {
+          sweeps<float>(cluster, alone, w32, rows, v32, vrows, k, 1e-5, reinterpret_cast<float *>(norms_raw),
+                        reinterpret_cast<float *>(dynamic + kDynamicBytes - swap32), reinterpret_cast<float *>(partial_raw),
+                        flags);
+          for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
+          {
+            const int64_t row = c0 + i % vrows;
+            if (row < c1) v_cur[(i / vrows) * k + row] = static_cast<double>(v32[i]);
+          }
+        }
       }
       cluster.sync();
 
-      // 2. V orthonormal to FP64 precision by two Newton-Schulz steps V <- V + V (I - V^T V) / 2.
-      // G = V^T V in FP64 (the symmetric half, by the whole cluster); the correction V E, E = I - G
-      // of size ~1e-6 and then ~1e-12, in FP32 accumulation: its rounding (~1e-7 of E) is below
-      // FP64 precision of V after the second step.  V and G pass between the CTAs through the
-      // workspace, read past L1 (__ldcg) so that no CTA sees an earlier iterate.
-      const int64_t lane_all = static_cast<int64_t>(rank) * blockDim.x + threadIdx.x;
-      const int64_t lanes_all = static_cast<int64_t>(ranks) * blockDim.x;
+      // 2. V orthonormal to FP64 precision by two Newton-Schulz steps V <- V + V (I - V^T V) / 2:
+      // G = V^T V in FP64 (the tiles on and above the diagonal), the correction V E, E = I - G of
+      // size ~1e-6 and then ~1e-12, in FP32 accumulation (its rounding, ~1e-7 of E, is below FP64
+      // precision of V after the second step).  Tiles are dealt to the ranks; V and G pass between
+      // the CTAs through the workspace, read past L1 (__ldcg) so that no CTA sees an earlier value.
+      const int64_t nt = (k + kTile - 1) / kTile;
       for (int step = 0; step < 2; ++step)
       {
-        for (int64_t i = lane_all; i < k * k; i += lanes_all)
+        for (int64_t tile = rank; tile < nt * nt; tile += ranks)
         {
-          const int64_t r = i % k, c = i / k;  // G[r][c] = v_r . v_c (columns of V)
-          if (r > c) continue;
-          const double *vr = v_cur + r * k, *vc = v_cur + c * k;
-          double sum = 0.0;
-          for (int64_t x = 0; x < k; ++x) sum = fma(__ldcg(vr + x), __ldcg(vc + x), sum);
-          g[c * k + r] = sum;
-          g[r * k + c] = sum;
+          const int64_t tr = tile % nt, tc = tile / nt;
+          if (tr > tc) continue;
+          const double *vc = v_cur;
+          tile_product<double>(
+            k, [&](int64_t x, int i) { return tr * kTile + i < k ? __ldcg(vc + (tr * kTile + i) * k + x) : 0.0; }, true,
+            [&](int64_t x, int j) { return tc * kTile + j < k ? __ldcg(vc + (tc * kTile + j) * k + x) : 0.0; }, true,
+            stage, stage + kTile * (kTile + 1),
+            [&](int i, int j, double sum) {
+              const int64_t r = tr * kTile + i, c = tc * kTile + j;
+              if (r < k && c < k)
+              {
+                g[c * k + r] = sum;
+                g[r * k + c] = sum;
+              }
+            });
         }
         cluster.sync();
-        for (int64_t i = lane_all; i < k * k; i += lanes_all)
+        for (int64_t tile = rank; tile < nt * nt; tile += ranks)
         {
-          const int64_t row = i % k, c = i / k;
-          const double *gc = g + c * k;
-          float sum = 0.0f;
-          for (int64_t r = 0; r < k; ++r)
-            sum = fmaf(static_cast<float>(__ldcg(v_cur + r * k + row)), static_cast<float>((r == c ? 1.0 : 0.0) - __ldcg(gc + r)), sum);
-          v_next[i] = fma(0.5, static_cast<double>(sum), __ldcg(v_cur + i));
+          const int64_t tr = tile % nt, tc = tile / nt;  // rows tr, columns tc of V'
+          const double *vc = v_cur, *gc = g;
+          float *sa = reinterpret_cast<float *>(stage), *sb = sa + kTile * (kTile + 1);
+          tile_product<float>(
+            k, [&](int64_t x, int i) { return tr * kTile + i < k ? static_cast<float>(__ldcg(vc + x * k + tr * kTile + i)) : 0.0f; },
+            false,
+            [&](int64_t x, int j) {
+              const int64_t c = tc * kTile + j;
+              return c < k ? static_cast<float>((x == c ? 1.0 : 0.0) - __ldcg(gc + c * k + x)) : 0.0f;
+            },
+            true, sa, sb,
+            [&](int i, int j, float sum) {
+              const int64_t row = tr * kTile + i, c = tc * kTile + j;
+              if (row < k && c < k) v_next[c * k + row] = fma(0.5, static_cast<double>(sum), __ldcg(vc + c * k + row));
+            });
         }
         cluster.sync();
         double *t = v_cur;
@@ -467,39 +583,50 @@ namespace ttg
         v_next = t;
       }
 
-      // 3. this rank's rows of W = A V (FP64) and of V
-      const int64_t rows = (len + ranks - 1) / ranks, vrows = (k + ranks - 1) / ranks;
-      const int64_t r0 = min(len, static_cast<int64_t>(rank) * rows), r1 = min(len, r0 + rows);
-      const int64_t c0 = min(k, static_cast<int64_t>(rank) * vrows), c1 = min(k, c0 + vrows);
-      const bool slices_in_smem = (rows + vrows) * k * 8 <= kDynamicBytes;
-      double *w = slices_in_smem ? reinterpret_cast<double *>(dynamic) : ws + lay.w_slices + rank * rows * k;
-      double *v = slices_in_smem ? w + rows * k : ws + lay.v_slices + rank * vrows * k;
-      for (int64_t i = threadIdx.x; i < rows * k; i += blockDim.x)
+      // 3. this rank's rows of W = A V (FP64) and of V.  FP64 sweeps over the cluster for 32
+      // columns or more, on rank 0 alone below that.
+      const bool alone = k < 32;
+      const int64_t rows = alone ? (rank == 0 ? len : 0) : (len + ranks - 1) / ranks;
+      const int64_t vrows = alone ? (rank == 0 ? k : 0) : (k + ranks - 1) / ranks;
+      const int64_t r0 = alone ? 0 : min(len, static_cast<int64_t>(rank) * rows), r1 = min(len, r0 + rows);
+      const int64_t c0 = alone ? 0 : min(k, static_cast<int64_t>(rank) * vrows), c1 = min(k, c0 + vrows);
+      const int64_t swap64 = exchange_bytes(k, alone ? 1 : ranks, 8);
+      const bool slices_in_smem = (rows + vrows) * k * 8 + (swap64 > kStageBytes ? swap64 : kStageBytes) <= kDynamicBytes;
+      double *w = slices_in_smem ? reinterpret_cast<double *>(dynamic) : ws + lay.w_slices + static_cast<int64_t>(rank) * rows * k;
+      double *v = slices_in_smem ? w + rows * k : ws + lay.v_slices + static_cast<int64_t>(rank) * vrows * k;
       {
-        const int64_t row = r0 + i % rows, j = i / rows;
-        double sum = 0.0;
-        if (row < r1)
+        const double *vc = v_cur;
+        const int64_t nr = (rows + kTile - 1) / kTile;
+        for (int64_t tile = 0; tile < nr * nt; ++tile)
         {
-          const double *vj = v_cur + j * k;
-          for (int64_t c = 0; c < k; ++c) sum = fma(entry(row, c), __ldcg(vj + c), sum);
+          const int64_t tr = tile % nr, tc = tile / nr;
+          tile_product<double>(
+            k, [&](int64_t x, int i) { const int64_t row = r0 + tr * kTile + i; return row < r1 ? entry(row, x) : 0.0; }, !wide,
+            [&](int64_t x, int j) { return tc * kTile + j < k ? __ldcg(vc + (tc * kTile + j) * k + x) : 0.0; }, true,
+            stage, stage + kTile * (kTile + 1),
+            [&](int i, int j, double sum) {
+              const int64_t row = tr * kTile + i, c = tc * kTile + j;
+              if (row < rows && c < k) w[c * rows + row] = r0 + row < r1 ? sum : 0.0;
+            });
         }
-        w[i] = sum;
+        for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
+        {
+          const int64_t row = c0 + i % vrows, j = i / vrows;
+          v[i] = row < c1 ? __ldcg(vc + j * k + row) : 0.0;
+        }
+        __syncthreads();
       }
-      for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
-      {
-        const int64_t row = c0 + i % vrows, j = i / vrows;
-        v[i] = row < c1 ? __ldcg(v_cur + j * k + row) : 0.0;
-      }
-      __syncthreads();
 
-      // 4. FP64 sweeps over the cluster
+      // 4. FP64 sweeps
       const double tol = 2.220446049250313e-16 * sqrt(static_cast<double>(len));
-      const int sweeps = rows <= 32 ? cluster_sweeps<4>(cluster, w, rows, v, vrows, k, tol, norms, shares, partial, flags)
-                                    : rows <= 128 ? cluster_sweeps<8>(cluster, w, rows, v, vrows, k, tol, norms, shares, partial, flags)
-                                                  : cluster_sweeps<32>(cluster, w, rows, v, vrows, k, tol, norms, shares, partial, flags);
+      int sweeps_taken = 0;
+      if (!alone || rank == 0)
+        sweeps_taken = sweeps<double>(cluster, alone, w, rows, v, vrows, k, tol, norms_raw,
+                                      reinterpret_cast<double *>(dynamic + kDynamicBytes - swap64), partial_raw, flags);
 
       // singular values (column norms over the cluster), their ranks, and this rank's rows of the
       // factors in descending order
+      double *norms = norms_raw, *partial = partial_raw;
       const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
       for (int64_t j = warp; j < k; j += warps)
       {
@@ -548,7 +675,7 @@ namespace ttg
         else
           vo[static_cast<int64_t>(rank_of[j]) * n + row] = v[i];
       }
-      if (threadIdx.x == 0 && rank == 0) info[block] = sweeps;
+      if (threadIdx.x == 0 && rank == 0) info[block] = sweeps_taken;
       // no CTA leaves while another may still read its shared memory
       cluster.sync();
     }
@@ -591,8 +718,8 @@ namespace ttg
     }
   } // namespace
 
-  cudaError_t svd_blocks(int32_t count, const void *table, const double *a, double *u, double *s, double *vh,
-                         void *workspace, int32_t *info, cudaStream_t stream)
+  cudaError_t svd_blocks(int32_t count, int64_t largest, const void *table, const double *a, double *u, double *s,
+                         double *vh, void *workspace, int32_t *info, cudaStream_t stream)
   {
     if (count <= 0) return cudaSuccess;
     static std::once_flag once;
@@ -601,6 +728,8 @@ namespace ttg
     std::call_once(once, [] {
       configured = cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(kDynamicBytes));
+      if (configured == cudaSuccess)
+        configured = cudaFuncSetAttribute(jacobi_svd_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
       for (int size = 1; size <= kMaxCluster && configured == cudaSuccess; size *= 2)
       {
         cudaLaunchConfig_t config = {};
@@ -624,11 +753,13 @@ namespace ttg
       }
     });
     if (configured != cudaSuccess) return configured;
-    // the largest cluster with which every block's cluster is resident at once (one CTA per block
-    // when even that does not hold)
+    // the cluster the largest block wants (16 CTAs from 128 columns, 8 from 32, below that the
+    // sweeps run on one CTA), or the largest the GPU can hold; blocks come largest first, so a
+    // second wave of clusters only holds small blocks
+    const int want = largest >= 128 ? 16 : largest >= 32 ? 8 : 1;
     int size = 1;
-    for (int c = kMaxCluster; c > 1; c /= 2)
-      if (cluster_for[c] >= count)
+    for (int c = want; c > 1; c /= 2)
+      if (cluster_for[c] >= 1)
       {
         size = c;
         break;

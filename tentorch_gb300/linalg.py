@@ -348,14 +348,18 @@ def _factor_blocks(arranged: Tensor):
     places, total = (i64 * max(len(present), 1))(), i64()
     check(lib.tt_svd_workspace(len(present), dims, places, ctypes.byref(total)))
     ws_at = total.value
-    table, shapes = [], []
+    entries, shapes = [], []
     u_at = s_at = vh_at = 0
     for at, (i, key) in enumerate(present):
         rows, cols = space.shapes[i]
         k = min(rows, cols)
-        table += [space.offsets[i], rows, cols, u_at, s_at, vh_at, places[at]]
+        entries.append([space.offsets[i], rows, cols, u_at, s_at, vh_at, places[at]])
         shapes.append((key, rows, cols, k, u_at, s_at, vh_at))
         u_at, s_at, vh_at = u_at + rows * k, s_at + k, vh_at + k * cols
+    # the largest blocks first: the launch's clusters then finish together, small blocks last
+    entries.sort(key = lambda e: -min(e[1], e[2]) ** 2 * max(e[1], e[2]))
+    table = [x for e in entries for x in e]
+    largest = max((min(e[1], e[2]) for e in entries), default = 0)
     device = arranged.device
     dev_table = torch.tensor(table, dtype = torch.int64).to(device)
     u = torch.empty(max(u_at, 1), dtype = torch.float64, device = device)
@@ -364,8 +368,8 @@ def _factor_blocks(arranged: Tensor):
     ws = torch.empty(max(ws_at, 1), dtype = torch.float64, device = device)
     info = torch.empty(max(len(present), 1), dtype = torch.int32, device = device)
     stream = torch.cuda.current_stream(device).cuda_stream
-    check(lib.tt_svd_blocks(len(present), dev_table.data_ptr(), arranged._data.data_ptr(), u.data_ptr(), sv.data_ptr(),
-                            vh.data_ptr(), ws.data_ptr(), info.data_ptr(), stream))
+    check(lib.tt_svd_blocks(len(present), largest, dev_table.data_ptr(), arranged._data.data_ptr(), u.data_ptr(),
+                            sv.data_ptr(), vh.data_ptr(), ws.data_ptr(), info.data_ptr(), stream))
     host = sv[:s_at].cpu().tolist()
     if present and int(info[:len(present)].min()) < 0:
         raise RuntimeError('the Jacobi SVD of a block did not converge')
