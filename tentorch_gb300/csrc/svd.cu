@@ -161,8 +161,11 @@ namespace ttg
     template <typename T, int G>
     __device__ __forceinline__ T group_sum(T v)
     {
+      if constexpr (G > 1)
+      {
 #pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+        for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, G);
+      }
       return v;
     }
 
@@ -391,6 +394,10 @@ namespace ttg
                           double tol, T *norms, T *exchange, T *partial, int *flags)
     {
       const int64_t most = rows > vrows ? rows : vrows;
+      // the fewest lanes per pair that hold its rows in registers: per-pair scalar work (the angle,
+      // the norms) runs once per lane of the group
+      if (most <= kNper) return sweeps<T, 1>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
+      if (most <= 2 * kNper) return sweeps<T, 2>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
       if (most <= 4 * kNper) return sweeps<T, 4>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
       if (most <= 8 * kNper) return sweeps<T, 8>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
       if (most <= 16 * kNper) return sweeps<T, 16>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
