@@ -478,7 +478,7 @@ namespace ttg
       // 1. FP32 sweeps on the block scaled to |entries| <= 1, from V = I; V goes out in FP64.
       // Rank 0 alone when W and V fit in its shared memory, else rows dealt over the cluster.
       {
-        const bool alone = (len * k + k * k) * 4 <= kDynamicBytes;
+        const bool alone = ranks == 1 || (k < 32 && (len * k + k * k) * 4 <= kDynamicBytes);
         const int64_t rows = alone ? len : (len + ranks - 1) / ranks, vrows = alone ? k : (k + ranks - 1) / ranks;
         const int64_t r0 = alone ? 0 : min(len, static_cast<int64_t>(rank) * rows), r1 = alone ? len : min(len, r0 + rows);
         const int64_t c0 = alone ? 0 : min(k, static_cast<int64_t>(rank) * vrows), c1 = alone ? k : min(k, c0 + vrows);
@@ -592,7 +592,7 @@ namespace ttg
 
       // 3. this rank's rows of W = A V (FP64) and of V.  FP64 sweeps over the cluster for 32
       // columns or more, on rank 0 alone below that.
-      const bool alone = k < 32;
+      const bool alone = ranks == 1 || k < 32;
       const int64_t rows = alone ? (rank == 0 ? len : 0) : (len + ranks - 1) / ranks;
       const int64_t vrows = alone ? (rank == 0 ? k : 0) : (k + ranks - 1) / ranks;
       const int64_t r0 = alone ? 0 : min(len, static_cast<int64_t>(rank) * rows), r1 = min(len, r0 + rows);
