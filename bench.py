@@ -392,7 +392,7 @@ def run_gpu(args, rank, world):
         op_ms = np.zeros(n_ops)
         kinds = None
         samples = min(args.steps, 200)
-        ws = torch.empty(max(plan.workspace, 1), dtype = torch.float64, device = device)
+        ws = torch.zeros(max(plan.workspace, 1), dtype = torch.float64, device = device)  # a fresh workspace is zero
         prepared = [tg.linalg._prepared_arena(plan, i, t, ws, stream.cuda_stream) for i, t in enumerate([head, tail, vectors[0]])]
         for i in range(samples):
             flush.zero_()

@@ -126,7 +126,11 @@ int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *ele
  * bf16 slices per operand; TT_PRECISION_PER_BLOCK (-1): the plain per-block FP64 form, one cuBLAS
  * call per block pair as the reference issues them on a CUDA device
  * (tentorch/linalg/graded/contract.cpp:148-163), the comparison arm of the grouped kernels.
- * `prepared` (may be NULL, or hold NULLs) gives operands' prepared arenas from tt_plan_prepare. */
+ * `prepared` (may be NULL, or hold NULLs) gives operands' prepared arenas from tt_plan_prepare.
+ * `workspace` (tt_plan_info's elements of the dtype) must start zeroed: a plan with block products
+ * keeps the counters of its split output tiles in the first 64 KiB, and every execution leaves
+ * them zero again, so one zeroed workspace serves any number of executions of any plans on one
+ * stream (they must not run concurrently on it). */
 int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                         const void *const *prepared, void *output, void *workspace, void *stream);
 /* The same, synchronously, recording a CUDA event pair around every operation on `stream`: per op

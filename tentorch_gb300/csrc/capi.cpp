@@ -449,6 +449,9 @@ extern "C"
       if (operand < 0 || operand >= p.n_inputs) throw ttg::InvalidArgument("no operand " + std::to_string(operand));
       const int32_t b = p.prepared[static_cast<size_t>(operand)];
       *elements = b < 0 ? 0 : p.buffers[static_cast<size_t>(b)].size;
+      // with the slices of its value that split-precision products read (float64 elements)
+      if (b >= 0 && p.gemm_plans && !p.gemm_plans->prepared_bytes.empty())
+        *elements = std::max<int64_t>(*elements, (p.gemm_plans->prepared_bytes[static_cast<size_t>(operand)] + 7) / 8);
     });
   }
 
@@ -542,7 +545,8 @@ extern "C"
     args.stream = static_cast<cudaStream_t>(stream);
     args.only_phase = operand;
     args.prepared_out = prepared;
-    const cudaError_t e = ttg::execute(p, *plan->tables, args);
+    cudaError_t e = ttg::execute(p, *plan->tables, args);
+    if (e == cudaSuccess && !args.complex) e = ttg::fill_slice_caches(p, *plan->tables, operand, prepared, args.stream);
     if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
     return TT_OK;
   }

@@ -68,7 +68,8 @@ namespace ttg
       int64_t longest = 0;
       void *items = nullptr, *pairs = nullptr, *lines = nullptr;
       GemmReduce *reduces = nullptr;
-      int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0, slice_a = 0, slice_b = 0, exps = 0, slots = 0;
+      int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0, slice_a = 0, slice_b = 0, exps_a = 0, exps = 0,
+              slots = 0;
     };
     std::vector<GemmTables> gemm;
     std::vector<SplitTables> split;
@@ -95,10 +96,17 @@ namespace ttg
   cudaError_t execute(const Program &p, DeviceTables &t, const ExecArgs &args);
 
   // The grouped GEMM of one op (gemm.cu): FP64 / complex128, or split precision with `slices`.
+  // `tickets` is the workspace's ticket region (kTicketInts ints, zero, left zero).
   cudaError_t launch_gemm_f64(const Program &p, DeviceTables &t, size_t op_index, const void *A, const void *B, void *C,
-                              bool complex, void *scratch, cudaStream_t stream);
+                              bool complex, void *scratch, int *tickets, cudaStream_t stream);
+  // `prepared`: the caller's prepared arenas (or null); a side read from one uses the slices cut
+  // into it by fill_slice_caches.
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
-                                const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream);
+                                const double *B, double *C, int32_t slices, void *scratch, int *tickets,
+                                const void *const *prepared, cudaStream_t stream);
+  // Cut the slices of the GEMM operands that are operand `operand`'s prepared value into its arena.
+  cudaError_t fill_slice_caches(const Program &p, DeviceTables &t, int32_t operand, const void *arena,
+                                cudaStream_t stream);
   void stage_gemm(const Program &p, DeviceTables &t, TableStaging &staging);
   // The plain per-block form (per_block.cu): one cuBLAS call per block pair.
   cudaError_t launch_gemm_per_block(const Program &p, const Op &op, const void *A, const void *B, void *C, bool complex,

@@ -175,28 +175,29 @@ namespace ttg
         auto fa = a_at.find(pr.a);
         if (fa == a_at.end())
         {
-          fa = a_at.emplace(pr.a, std::make_pair(s.slice_a, static_cast<int32_t>(s.exps))).first;
+          fa = a_at.emplace(pr.a, std::make_pair(s.slice_a, static_cast<int32_t>(s.exps_a))).first;
           for (int32_t r = 0; full && r < blk.m; ++r)
             s.lines.push_back({pr.a + static_cast<int64_t>(r) * pr.k, s.slice_a + r * kp, pr.k, 1, static_cast<int32_t>(kp),
-                               static_cast<int32_t>(s.exps + r)});
+                               static_cast<int32_t>(s.exps_a + r)});
           s.slice_a += (blk.m * kp + 63) / 64 * 64;
-          s.exps += blk.m;
+          s.exps_a += blk.m;
         }
         auto fb = b_at.find(pr.b);
         if (fb == b_at.end())
         {
-          fb = b_at.emplace(pr.b, std::make_pair(s.slice_b, static_cast<int32_t>(s.exps))).first;
+          fb = b_at.emplace(pr.b, std::make_pair(s.slice_b, static_cast<int32_t>(s.exps_b))).first;
           for (int32_t c = 0; full && c < blk.n; ++c)
             b_lines.push_back({pr.b + c, s.slice_b + c * kp, pr.k, blk.n, static_cast<int32_t>(kp),
-                               static_cast<int32_t>(s.exps + c)});
+                               static_cast<int32_t>(s.exps_b + c)});
           s.slice_b += (blk.n * kp + 63) / 64 * 64;
-          s.exps += blk.n;
+          s.exps_b += blk.n;
         }
         if (full)
           s.pairs[pi] = SplitPair{fa->second.first, fb->second.first, static_cast<int32_t>(kp), fa->second.second,
                                   fb->second.second, 0};
       }
     }
+    s.exps = s.exps_a + s.exps_b;
     s.lines_a = static_cast<int64_t>(s.lines.size());
     s.lines.insert(s.lines.end(), b_lines.begin(), b_lines.end());
     // items: one pair's K range each (a multiple of 32), about two per worker, never below a tile
@@ -305,6 +306,8 @@ namespace ttg
     auto plans = std::make_shared<GemmPlans>();
     plans->f64.resize(p.ops.size());
     plans->split.resize(p.ops.size());
+    plans->cache_a.assign(p.ops.size(), -1);
+    plans->cache_b.assign(p.ops.size(), -1);
     int64_t need = 0;
     for (size_t i = 0; i < p.ops.size(); ++i)
     {
@@ -314,7 +317,34 @@ namespace ttg
       // the split schedule itself is built on the first split launch (most plans never run one);
       // here only its scratch
       need = std::max(need, (f64_bytes(plans->f64[i]) + 7) / 8);
-      need = std::max(need, (split_bytes(schedule_split(p, op, false), kMaxSlices) + 7) / 8);
+      const SplitSchedule sizes = schedule_split(p, op, false);
+      need = std::max(need, (split_bytes(sizes, kMaxSlices) + 7) / 8);
+      // the slices of a prepared operand's value go into its arena
+      for (int side = 0; side < 2; ++side)
+      {
+        const int32_t buffer = side == 0 ? op.src : op.src2;
+        if (buffer < 0) continue;
+        const int32_t operand = p.buffers[static_cast<size_t>(buffer)].prepared_of;
+        if (operand < 0) continue;
+        if (plans->prepared_bytes.empty())
+        {
+          plans->prepared_bytes.assign(static_cast<size_t>(p.n_inputs), 0);
+          for (int32_t j = 0; j < p.n_inputs; ++j)
+            if (p.prepared[static_cast<size_t>(j)] >= 0)
+              plans->prepared_bytes[static_cast<size_t>(j)] = up256(p.buffers[static_cast<size_t>(p.prepared[static_cast<size_t>(j)])].size * 8);
+        }
+        SliceCache c;
+        c.op = static_cast<int32_t>(i);
+        c.side = side;
+        c.operand = operand;
+        c.offset = plans->prepared_bytes[static_cast<size_t>(operand)];
+        const int64_t slice = side == 0 ? sizes.slice_a : sizes.slice_b, exps = side == 0 ? sizes.exps_a : sizes.exps_b;
+        c.exps_offset = c.offset + up256(2 * kMaxSlices * slice);
+        c.bytes = up256(2 * kMaxSlices * slice) + up256(2 * exps);
+        plans->prepared_bytes[static_cast<size_t>(operand)] += c.bytes;
+        (side == 0 ? plans->cache_a : plans->cache_b)[i] = static_cast<int32_t>(plans->caches.size());
+        plans->caches.push_back(c);
+      }
     }
     p.gemm_plans = std::move(plans);
     return need;
@@ -400,6 +430,8 @@ namespace ttg
       const bool last = *flag;
       worker_sync(worker);
       if (!last) return;
+      // every other partial of the tile has taken its ticket: leave the counter zero for the next launch
+      if (lt == 0) tickets[reduce] = 0;
       __threadfence();
       const DevBlock blk = blocks[r.block];
       // every entry of the tile sums its slots in slot order; the loads of four slots for all of the
@@ -745,18 +777,20 @@ namespace ttg
     // written to a row padded with zeros to a multiple of 32.  Loads are issued eight at a time.
     __global__ void split_lines_kernel(const double *__restrict__ a, const double *__restrict__ b,
                                        uint16_t *__restrict__ slices_a, uint16_t *__restrict__ slices_b,
-                                       int16_t *__restrict__ exps, int64_t stride_a, int64_t stride_b,
-                                       const SplitLine *__restrict__ lines, int64_t lines_a, int64_t n_lines, int slices_n)
+                                       int16_t *__restrict__ exps_a, int16_t *__restrict__ exps_b, int64_t stride_a,
+                                       int64_t stride_b, const SplitLine *__restrict__ lines, int64_t lines_a,
+                                       int64_t line_begin, int64_t line_end, int slices_n)
     {
       const int lane = threadIdx.x & 31;
       const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
       const int64_t warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-      for (int64_t l = warp; l < n_lines; l += warps)
+      for (int64_t l = line_begin + warp; l < line_end; l += warps)
       {
         const SplitLine line = lines[l];
         const bool left = l < lines_a;
         const double *src = (left ? a : b) + line.src;
         uint16_t *dst = (left ? slices_a : slices_b) + line.dst;
+        int16_t *exps = left ? exps_a : exps_b;
         const int64_t stride = left ? stride_a : stride_b;
         // the largest |entry| by its bits (positive doubles order as integers), then its frexp
         // exponent e: every |entry| < 2^e
@@ -856,7 +890,8 @@ namespace ttg
     template <int S>
     __global__ void __launch_bounds__(kSplitWorkers * kWorkerThreads, 1)
       gemm_split_kernel(const uint16_t *__restrict__ sa_all, const uint16_t *__restrict__ sb_all,
-                        const int16_t *__restrict__ exps, int64_t stride_a, int64_t stride_b, double *__restrict__ C,
+                        const int16_t *__restrict__ exps_a, const int16_t *__restrict__ exps_b, int64_t stride_a,
+                        int64_t stride_b, double *__restrict__ C,
                         const DevBlock *__restrict__ blocks, const DevSplitPair *__restrict__ spairs,
                         const SplitItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                         int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
@@ -916,12 +951,12 @@ namespace ttg
             for (int ns = 0; ns < 2; ++ns)
 #pragma unroll
               for (int q = 0; q < 4; ++q) lev[l][ns][q] = 0.0f;
-          const int er0 = r0 < blk.m ? exps[sp.ea + r0] : 0, er1 = r0 + 8 < blk.m ? exps[sp.ea + r0 + 8] : 0;
+          const int er0 = r0 < blk.m ? exps_a[sp.ea + r0] : 0, er1 = r0 + 8 < blk.m ? exps_a[sp.ea + r0 + 8] : 0;
           int ec[2][2];
 #pragma unroll
           for (int ns = 0; ns < 2; ++ns)
 #pragma unroll
-            for (int h = 0; h < 2; ++h) ec[ns][h] = c0 + ns * 8 + h < blk.n ? exps[sp.eb + c0 + ns * 8 + h] : 0;
+            for (int h = 0; h < 2; ++h) ec[ns][h] = c0 + ns * 8 + h < blk.n ? exps_b[sp.eb + c0 + ns * 8 + h] : 0;
           load(0, it.k0);
           for (int step = 0; step < steps; ++step)
           {
@@ -1040,8 +1075,8 @@ namespace ttg
     }
 
     template <int S>
-    cudaError_t launch_split_s(const uint16_t *sa, const uint16_t *sb, const int16_t *exps, int64_t stride_a,
-                               int64_t stride_b, double *C, const DevBlock *blocks, const DevSplitPair *spairs,
+    cudaError_t launch_split_s(const uint16_t *sa, const uint16_t *sb, const int16_t *exps_a, const int16_t *exps_b,
+                               int64_t stride_a, int64_t stride_b, double *C, const DevBlock *blocks, const DevSplitPair *spairs,
                                const SplitItem *items, const int32_t *cta_begin, int32_t n_ctas, int64_t longest,
                                const GemmReduce *reduces, int64_t n_reduces, double *partial, int *tickets,
                                cudaStream_t stream)
@@ -1053,7 +1088,7 @@ namespace ttg
       // one CTA per list the schedule dealt, as many workers as its longest list needs
       const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kSplitWorkers));
       gemm_split_kernel<S><<<n_ctas, workers * kWorkerThreads, bytes, stream>>>(
-        sa, sb, exps, stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets);
+        sa, sb, exps_a, exps_b, stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets);
       return cudaGetLastError();
     }
   } // namespace
@@ -1063,7 +1098,7 @@ namespace ttg
   // ------------------------------------------------------------------------------------------
 
   cudaError_t launch_gemm_f64(const Program &p, DeviceTables &t, size_t op_index, const void *A, const void *B, void *C,
-                              bool complex, void *scratch, cudaStream_t stream)
+                              bool complex, void *scratch, int *ticket_region, cudaStream_t stream)
   {
     (void)p;
     const auto &sched = t.gemm[op_index];
@@ -1072,10 +1107,15 @@ namespace ttg
     const auto *pairs = reinterpret_cast<const DevPair *>(t.pairs);
     char *base = static_cast<char *>(scratch);
     void *partial = base;
-    int *tickets = reinterpret_cast<int *>(base + up256(sched.slots * kF64TileM * kF64TileN * 16));
+    // the workspace's ticket region (zero, and left zero by the kernel) when it holds them all,
+    // else tickets of our own in the scratch, cleared first
+    int *tickets = ticket_region;
     cudaError_t e = cudaSuccess;
-    e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces + 1) * 4, stream);  // tickets and the item counter
-    if (e != cudaSuccess) return e;
+    if (sched.n_reduces > kTicketInts)
+    {
+      tickets = reinterpret_cast<int *>(base + up256(sched.slots * kF64TileM * kF64TileN * 16));
+      if ((e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces) * 4, stream)) != cudaSuccess) return e;
+    }
     // one CTA per list the schedule dealt, as many workers as its longest list needs (at most four)
     const int grid = sched.n_ctas;
     const int workers = static_cast<int>(std::clamp<int64_t>(sched.longest, 1, kF64Workers));
@@ -1100,38 +1140,82 @@ namespace ttg
     return cudaGetLastError();
   }
 
-  cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
-                                const double *B, double *C, int32_t slices, void *scratch, cudaStream_t stream)
+  namespace
   {
+    // The split tables of a GEMM op, built on its first split use.
+    cudaError_t ensure_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index)
     {
       std::lock_guard<std::mutex> lock(t.mutex);
       DeviceTables::SplitTables &dst = t.split[op_index];
-      if (!dst.ready)
-      {
-        const SplitSchedule s = schedule_split(p, op, true);
-        dst.n_items = static_cast<int64_t>(s.items.size());
-        dst.n_reduces = static_cast<int64_t>(s.reduces.size());
-        dst.n_lines_a = s.lines_a;
-        dst.n_lines_b = static_cast<int64_t>(s.lines.size()) - s.lines_a;
-        dst.slice_a = s.slice_a;
-        dst.slice_b = s.slice_b;
-        dst.exps = s.exps;
-        dst.slots = s.slots;
-        dst.n_ctas = static_cast<int32_t>(s.cta_begin.size()) - 1;
-        dst.longest = 0;
-        for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c)
-          dst.longest = std::max<int64_t>(dst.longest, s.cta_begin[c + 1] - s.cta_begin[c]);
-        TableStaging staging;
-        staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
-        staging.add(s.items, &dst.items);
-        staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
-        staging.add(s.pairs, &dst.pairs);
-        staging.add(s.lines, &dst.lines);
-        const cudaError_t e = staging.commit(&dst.base);
-        if (e != cudaSuccess) return e;
-        dst.ready = true;
-      }
+      if (dst.ready) return cudaSuccess;
+      const SplitSchedule s = schedule_split(p, op, true);
+      dst.n_items = static_cast<int64_t>(s.items.size());
+      dst.n_reduces = static_cast<int64_t>(s.reduces.size());
+      dst.n_lines_a = s.lines_a;
+      dst.n_lines_b = static_cast<int64_t>(s.lines.size()) - s.lines_a;
+      dst.slice_a = s.slice_a;
+      dst.slice_b = s.slice_b;
+      dst.exps_a = s.exps_a;
+      dst.exps = s.exps;
+      dst.slots = s.slots;
+      dst.n_ctas = static_cast<int32_t>(s.cta_begin.size()) - 1;
+      dst.longest = 0;
+      for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c)
+        dst.longest = std::max<int64_t>(dst.longest, s.cta_begin[c + 1] - s.cta_begin[c]);
+      TableStaging staging;
+      staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
+      staging.add(s.items, &dst.items);
+      staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
+      staging.add(s.pairs, &dst.pairs);
+      staging.add(s.lines, &dst.lines);
+      const cudaError_t e = staging.commit(&dst.base);
+      if (e != cudaSuccess) return e;
+      dst.ready = true;
+      return cudaSuccess;
     }
+
+    cudaError_t launch_lines(const DeviceTables::SplitTables &sched, const double *A, const double *B, uint16_t *sa,
+                             uint16_t *sb, int16_t *exps_a, int16_t *exps_b, int64_t begin, int64_t end, int slices,
+                             cudaStream_t stream)
+    {
+      if (begin >= end) return cudaSuccess;
+      const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
+      split_lines_kernel<<<static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 7) / 8, 152 * 16))),
+                           256, 0, stream>>>(A, B, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, lines, sched.n_lines_a,
+                                             begin, end, slices);
+      return cudaGetLastError();
+    }
+  } // namespace
+
+  cudaError_t fill_slice_caches(const Program &p, DeviceTables &t, int32_t operand, const void *arena, cudaStream_t stream)
+  {
+    if (!p.gemm_plans) return cudaSuccess;
+    for (const SliceCache &c : p.gemm_plans->caches)
+    {
+      if (c.operand != operand) continue;
+      const Op &op = p.ops[static_cast<size_t>(c.op)];
+      cudaError_t e = ensure_split(p, op, t, static_cast<size_t>(c.op));
+      if (e != cudaSuccess) return e;
+      const auto &sched = t.split[static_cast<size_t>(c.op)];
+      if (sched.n_items == 0) continue;
+      char *base = static_cast<char *>(const_cast<void *>(arena));
+      auto *slices = reinterpret_cast<uint16_t *>(base + c.offset);
+      auto *exps = reinterpret_cast<int16_t *>(base + c.exps_offset);
+      const auto *value = static_cast<const double *>(arena);
+      e = c.side == 0 ? launch_lines(sched, value, nullptr, slices, nullptr, exps, nullptr, 0, sched.n_lines_a, kMaxSlices, stream)
+                      : launch_lines(sched, nullptr, value, nullptr, slices, nullptr, exps, sched.n_lines_a,
+                                     sched.n_lines_a + sched.n_lines_b, kMaxSlices, stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+
+  cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
+                                const double *B, double *C, int32_t slices, void *scratch, int *ticket_region,
+                                const void *const *prepared, cudaStream_t stream)
+  {
+    cudaError_t e = ensure_split(p, op, t, op_index);
+    if (e != cudaSuccess) return e;
     const auto &sched = t.split[op_index];
     if (sched.n_items == 0) return cudaSuccess;
     char *base = static_cast<char *>(scratch);
@@ -1139,20 +1223,40 @@ namespace ttg
     base += up256(2 * kMaxSlices * sched.slice_a);
     auto *sb = reinterpret_cast<uint16_t *>(base);
     base += up256(2 * kMaxSlices * sched.slice_b);
-    auto *exps = reinterpret_cast<int16_t *>(base);
+    auto *exps_a = reinterpret_cast<int16_t *>(base);
+    auto *exps_b = exps_a + sched.exps_a;
     base += up256(2 * sched.exps);
     auto *partial = reinterpret_cast<double *>(base);
     base += up256(sched.slots * kSplitTileM * kSplitTileN * 8);
-    auto *tickets = reinterpret_cast<int *>(base);
-    cudaError_t e = cudaSuccess;
-    e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces + 1) * 4, stream);  // tickets and the item counter
-    if (e != cudaSuccess) return e;
-    const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
-    const int64_t n_lines = sched.n_lines_a + sched.n_lines_b;
-    if (n_lines)
-      split_lines_kernel<<<static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((n_lines + 7) / 8, 152 * 16))), 256, 0,
-                           stream>>>(A, B, sa, sb, exps, sched.slice_a, sched.slice_b, lines, sched.n_lines_a, n_lines, slices);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int *tickets = ticket_region;
+    if (sched.n_reduces > kTicketInts)
+    {
+      tickets = reinterpret_cast<int *>(base);
+      if ((e = cudaMemsetAsync(tickets, 0, static_cast<size_t>(sched.n_reduces) * 4, stream)) != cudaSuccess) return e;
+    }
+    // a side whose operand's prepared arena the caller holds was cut when the arena was prepared
+    int64_t begin = 0, end = sched.n_lines_a + sched.n_lines_b;
+    if (p.gemm_plans && prepared)
+    {
+      const int32_t ca = p.gemm_plans->cache_a[op_index], cb = p.gemm_plans->cache_b[op_index];
+      if (ca >= 0 && prepared[p.gemm_plans->caches[static_cast<size_t>(ca)].operand])
+      {
+        const SliceCache &c = p.gemm_plans->caches[static_cast<size_t>(ca)];
+        char *arena = static_cast<char *>(const_cast<void *>(prepared[c.operand]));
+        sa = reinterpret_cast<uint16_t *>(arena + c.offset);
+        exps_a = reinterpret_cast<int16_t *>(arena + c.exps_offset);
+        begin = sched.n_lines_a;
+      }
+      if (cb >= 0 && prepared[p.gemm_plans->caches[static_cast<size_t>(cb)].operand])
+      {
+        const SliceCache &c = p.gemm_plans->caches[static_cast<size_t>(cb)];
+        char *arena = static_cast<char *>(const_cast<void *>(prepared[c.operand]));
+        sb = reinterpret_cast<uint16_t *>(arena + c.offset);
+        exps_b = reinterpret_cast<int16_t *>(arena + c.exps_offset);
+        end = sched.n_lines_a;
+      }
+    }
+    if ((e = launch_lines(sched, A, B, sa, sb, exps_a, exps_b, begin, end, slices, stream)) != cudaSuccess) return e;
     const auto *blocks = reinterpret_cast<const DevBlock *>(t.blocks);
     const auto *spairs = reinterpret_cast<const DevSplitPair *>(sched.pairs);
     const auto *items = reinterpret_cast<const SplitItem *>(sched.items);
@@ -1160,8 +1264,9 @@ namespace ttg
     {
 #define TTG_SPLIT(S)                                                                                                    \
   case S:                                                                                                               \
-    e = launch_split_s<S>(sa, sb, exps, sched.slice_a, sched.slice_b, C, blocks, spairs, items, sched.cta_begin,       \
-                          sched.n_ctas, sched.longest, sched.reduces, sched.n_reduces, partial, tickets, stream);                                   \
+    e = launch_split_s<S>(sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, C, blocks, spairs, items,              \
+                          sched.cta_begin, sched.n_ctas, sched.longest, sched.reduces, sched.n_reduces, partial, tickets,  \
+                          stream);                                                                                      \
     break;
       TTG_SPLIT(1) TTG_SPLIT(2) TTG_SPLIT(3) TTG_SPLIT(4) TTG_SPLIT(5) TTG_SPLIT(6) TTG_SPLIT(7) TTG_SPLIT(8)
 #undef TTG_SPLIT

@@ -68,7 +68,8 @@ namespace ttg
     std::vector<SplitLine> lines;  // rows of A then columns of B
     int64_t lines_a = 0;
     int64_t slice_a = 0, slice_b = 0;  // elements of one slice of all A (B) rows
-    int64_t exps = 0;                  // int16 exponents
+    int64_t exps_a = 0, exps_b = 0;    // int16 exponents of the rows of A, of the columns of B
+    int64_t exps = 0;                  // both
     int64_t slots = 0;
     std::vector<int32_t> cta_begin;    // CTA b runs items [cta_begin[b], cta_begin[b + 1])
   };
@@ -91,10 +92,26 @@ namespace ttg
   // Scratch doubles a program's GEMM ops need at most (FP64 partials, or slices + exponents +
   // partials for split precision), laid out per op from offset 0.
   // Per op of a program (empty for the ops that are not GEMMs): the FP64 and the split schedules.
+  // The slices of a GEMM operand that is an operand's prepared value (fixed while the arena is
+  // unchanged: the head and tail of a Lanczos window) are cut once, when the arena is prepared,
+  // into the arena after the prepared value: kMaxSlices slices (any fewer are a prefix of them)
+  // and the exponents, laid out as the launch's scratch lays them out.
+  struct SliceCache
+  {
+    int32_t op;       // the GEMM op
+    int32_t side;     // 0: its A (rows), 1: its B (columns)
+    int32_t operand;  // whose prepared arena holds it
+    int64_t offset;   // bytes into that arena: the slices, then the exponents at exps_offset
+    int64_t exps_offset;
+    int64_t bytes;
+  };
   struct GemmPlans
   {
     std::vector<GemmSchedule> f64;
     std::vector<SplitSchedule> split;
+    std::vector<SliceCache> caches;
+    std::vector<int32_t> cache_a, cache_b;  // per op: its A's (B's) cache, -1 for none
+    std::vector<int64_t> prepared_bytes;    // per operand: bytes of its prepared arena with caches
   };
   // Schedule every GEMM op of the program into p.gemm_plans and return the scratch elements the
   // launches need (partial tiles, tickets, slices).

@@ -300,13 +300,15 @@ namespace ttg
       case OpKind::gemm:
       {
         void *scratch = static_cast<char *>(args.workspace) + p.scratch_offset * esize;
+        int *tickets = static_cast<int *>(args.workspace);
         if (args.precision < 0)
           e = launch_gemm_per_block(p, op, src, src2, dst, args.complex, args.stream);
         else if (args.precision > 0 && !args.complex)
           e = launch_gemm_split(p, op, t, i, reinterpret_cast<const double *>(src), reinterpret_cast<const double *>(src2),
-                                reinterpret_cast<double *>(dst), args.precision, scratch, args.stream);
+                                reinterpret_cast<double *>(dst), args.precision, scratch, tickets, args.prepared,
+                                args.stream);
         else
-          e = launch_gemm_f64(p, t, i, src, src2, dst, args.complex, scratch, args.stream);
+          e = launch_gemm_f64(p, t, i, src, src2, dst, args.complex, scratch, tickets, args.stream);
         break;
       }
       }

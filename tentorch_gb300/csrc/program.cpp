@@ -833,6 +833,15 @@ namespace ttg
       // ops of an unprepared operand's phase run as core ops
       for (Op &op : p.ops)
         if (op.phase >= 0 && p.prepared[static_cast<size_t>(op.phase)] < 0) op.phase = -1;
+      // GEMM tickets ahead of the temporaries; every program that uses the workspace at all leaves
+      // that region alone, since one workspace serves the programs of a stream in turn
+      if (p.workspace > 0 ||
+          std::any_of(p.ops.begin(), p.ops.end(), [](const Op &op) { return op.kind == OpKind::gemm; }))
+      {
+        for (Buffer &b : p.buffers)
+          if (b.kind == BufferKind::temp) b.offset += kTicketElements;
+        p.workspace += kTicketElements;
+      }
       p.scratch_offset = p.workspace;
       p.workspace += plan_gemms(p);
       validate(p);

@@ -116,6 +116,13 @@ namespace ttg
     int32_t prepared_of = -1;  // the operand whose prepared value this temporary holds
   };
 
+  // Programs with GEMM ops keep their tickets (the counters by which the last partial tile of a
+  // split output tile is found) in the first kTicketInts ints of the workspace, ahead of their
+  // temporaries.  That region is zero when a workspace is first used, and every execution leaves
+  // it zero (the last finisher of a tile resets its ticket), so no launch has to clear it.
+  constexpr int64_t kTicketInts = 16384;
+  constexpr int64_t kTicketElements = kTicketInts * 4 / 8;  // elements of 8 bytes or more
+
   struct Program
   {
     int32_t n_inputs = 0;

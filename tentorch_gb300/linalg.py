@@ -157,7 +157,8 @@ def _workspace(plan: Plan, device, dtype, stream) -> Optional[torch.Tensor]:
     key = (device.index, stream, dtype)
     pool = _pools.get(key)
     if pool is None or pool.numel() < plan.workspace:
-        pool = _pools[key] = torch.empty(max(plan.workspace, 1 << 16), dtype = dtype, device = device)
+        # zero: the head of a workspace holds the GEMM tickets, which every execution leaves zero
+        pool = _pools[key] = torch.zeros(max(plan.workspace, 1 << 16), dtype = dtype, device = device)
     return pool
 
 

@@ -130,12 +130,18 @@ def test_split_precision_matvec_accuracy(slices):
 
 
 def test_split_precision_is_deterministic():
+    '''Repeated split products are bit-identical, including once head and tail are prepared (from
+    the second call on) and their slices are read from the prepared arenas instead of being cut at
+    each launch: the first S of the eight cached digits are the digits an S-slice cut makes.'''
     head, tail, theta = orc.matvec_inputs(128, seed = 23)
     h, t, v = (to_product(x, tg.u1) for x in (head, tail, theta))
-    with tg.precision(4):
-        a = tg.einsum(orc.MATVEC, h, t, v).data.clone()
-        b = tg.einsum(orc.MATVEC, h, t, v).data.clone()
-    assert torch.equal(a, b)
+    plan = tg.linalg.plan_of(orc.MATVEC, h, t, v)
+    for slices in (4, 6, 8):
+        with tg.precision(slices):
+            runs = [tg.einsum(orc.MATVEC, h, t, v).data.clone() for _ in range(3)]
+            cut_now = tg.linalg.run(plan, [h, t, v], reuse_prepared = False).data
+        assert torch.equal(runs[0], runs[1]) and torch.equal(runs[0], runs[2])
+        assert torch.equal(runs[0], cut_now)
 
 
 def test_large_blocks_split_over_k():
@@ -187,3 +193,24 @@ def test_conjugate_transpose_is_the_blockwise_one(catname):
     want = t.to(device = 'cpu').conj()
     assert got._space is want._space
     assert torch.equal(got.data.cpu(), want.data)
+
+
+def test_gemm_tickets_are_left_zero_in_the_workspace():
+    '''The head of a stream's workspace holds the counters of split output tiles: every launch of
+    the grouped kernels leaves them zero (the last finisher of a tile resets its counter), so runs
+    after runs of plans with and without block products on one workspace stay correct.'''
+    from tentorch_gb300 import linalg as la
+    head, tail, theta = orc.matvec_inputs(256, seed = 11)
+    want = orc.einsum(orc.MATVEC, head, tail, theta)
+    h, t, v = (to_product(x, tg.u1) for x in (head, tail, theta))
+    for precision in (0, 6, 0, 8):
+        with tg.precision(precision):
+            for _ in range(3):
+                got = tg.einsum(orc.MATVEC, h, t, v)
+                moved = v.place([0, 3], [1, 2])  # a program with temporaries and no block products
+        assert max_relative(got, want.blocks) < (TOL if precision in (0, 8) else 1e-10)
+        assert moved is not None
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream().cuda_stream
+    pool = la._pools[(torch.cuda.current_device(), stream, torch.float64)]
+    assert int(torch.count_nonzero(pool[:8192]).item()) == 0
