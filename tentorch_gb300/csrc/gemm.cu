@@ -18,6 +18,7 @@
 
 #include "executor.h"
 #include "gemm.h"
+#include "launch.h"
 
 namespace ttg
 {
@@ -484,6 +485,7 @@ namespace ttg
                       const GemmItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                       int64_t n_reduces, T *__restrict__ partial, int *__restrict__ tickets)
     {
+      dependent_entry();
       constexpr int BM = kF64TileM, BN = kF64TileN, BK = 16, TM = 2, TN = 4;
       extern __shared__ __align__(16) unsigned char smem_raw[];
       const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
@@ -597,6 +599,7 @@ namespace ttg
                        const GemmItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                        int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
     {
+      dependent_entry();
       constexpr int BM = kF64TileM, BN = kF64TileN, BK = kDmmaStepK;
       extern __shared__ __align__(16) unsigned char smem_raw[];
       const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
@@ -781,6 +784,7 @@ namespace ttg
                                        int64_t stride_b, const SplitLine *__restrict__ lines, int64_t lines_a,
                                        int64_t line_begin, int64_t line_end, int slices_n)
     {
+      dependent_entry();
       const int lane = threadIdx.x & 31;
       const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
       const int64_t warps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -896,6 +900,7 @@ namespace ttg
                         const SplitItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
                         int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
     {
+      dependent_entry();
       extern __shared__ __align__(16) unsigned char smem_raw[];
       const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
       uint16_t *sA = reinterpret_cast<uint16_t *>(smem_raw + worker * split_worker_bytes<S>());  // [2][S][32][kRow]
@@ -1087,9 +1092,8 @@ namespace ttg
       if (e != cudaSuccess) return e;
       // one CTA per list the schedule dealt, as many workers as its longest list needs
       const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kSplitWorkers));
-      gemm_split_kernel<S><<<n_ctas, workers * kWorkerThreads, bytes, stream>>>(
-        sa, sb, exps_a, exps_b, stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets);
-      return cudaGetLastError();
+      return launch_dependent(gemm_split_kernel<S>, n_ctas, workers * kWorkerThreads, bytes, stream, sa, sb, exps_a, exps_b,
+                              stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets);
     }
   } // namespace
 
@@ -1124,20 +1128,24 @@ namespace ttg
       const int bytes = std::max<int>(kF64Workers * 2 * 16 * (kF64TileM + 1) * 16, kPinBytes);
       static std::once_flag once;
       if ((e = configure(gemm_f64_kernel<double2>, bytes, once)) != cudaSuccess) return e;
-      gemm_f64_kernel<double2><<<grid, workers * kWorkerThreads, bytes, stream>>>(
-        static_cast<const double2 *>(A), static_cast<const double2 *>(B), static_cast<double2 *>(C), blocks, pairs,
-        sched.items, sched.cta_begin, sched.reduces, sched.n_reduces, static_cast<double2 *>(partial), tickets);
+      e = launch_dependent(gemm_f64_kernel<double2>, grid, workers * kWorkerThreads, bytes, stream,
+                           static_cast<const double2 *>(A), static_cast<const double2 *>(B), static_cast<double2 *>(C), blocks,
+                           pairs, static_cast<const GemmItem *>(sched.items), static_cast<const int32_t *>(sched.cta_begin),
+                           static_cast<const GemmReduce *>(sched.reduces), sched.n_reduces, static_cast<double2 *>(partial),
+                           tickets);
     }
     else
     {
       const int bytes = std::max<int>(kF64Workers * 2 * 2 * kDmmaStepK * 36 * 8, kPinBytes);
       static std::once_flag once;
       if ((e = configure(gemm_dmma_kernel, bytes, once)) != cudaSuccess) return e;
-      gemm_dmma_kernel<<<grid, workers * kWorkerThreads, bytes, stream>>>(
-        static_cast<const double *>(A), static_cast<const double *>(B), static_cast<double *>(C), blocks, pairs,
-        sched.items, sched.cta_begin, sched.reduces, sched.n_reduces, static_cast<double *>(partial), tickets);
+      e = launch_dependent(gemm_dmma_kernel, grid, workers * kWorkerThreads, bytes, stream, static_cast<const double *>(A),
+                           static_cast<const double *>(B), static_cast<double *>(C), blocks, pairs,
+                           static_cast<const GemmItem *>(sched.items), static_cast<const int32_t *>(sched.cta_begin),
+                           static_cast<const GemmReduce *>(sched.reduces), sched.n_reduces, static_cast<double *>(partial),
+                           tickets);
     }
-    return cudaGetLastError();
+    return e;
   }
 
   namespace
@@ -1180,10 +1188,10 @@ namespace ttg
     {
       if (begin >= end) return cudaSuccess;
       const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
-      split_lines_kernel<<<static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 7) / 8, 152 * 16))),
-                           256, 0, stream>>>(A, B, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, lines, sched.n_lines_a,
-                                             begin, end, slices);
-      return cudaGetLastError();
+      return launch_dependent(split_lines_kernel,
+                              static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 7) / 8, 152 * 16))),
+                              256, 0, stream, A, B, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, lines,
+                              sched.n_lines_a, begin, end, slices);
     }
   } // namespace
 

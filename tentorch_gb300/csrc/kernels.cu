@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "executor.h"
+#include "launch.h"
 
 namespace ttg
 {
@@ -31,6 +32,7 @@ namespace ttg
     __global__ void gather_kernel(const T *__restrict__ src, T *__restrict__ dst, const int32_t *__restrict__ index,
                                   int64_t n)
     {
+      dependent_entry();
       for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
            i += static_cast<int64_t>(gridDim.x) * blockDim.x)
       {
@@ -43,6 +45,7 @@ namespace ttg
 
     __global__ void add_f64_kernel(const double *__restrict__ src, double *__restrict__ dst, int64_t n)
     {
+      dependent_entry();
       for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
            i += static_cast<int64_t>(gridDim.x) * blockDim.x)
         dst[i] += src[i];
@@ -69,6 +72,7 @@ namespace ttg
     __global__ void runs_kernel(const double *__restrict__ src, double *__restrict__ dst,
                                 const DevChunk *__restrict__ chunks, const DevTerm *__restrict__ terms, int64_t n_chunks)
     {
+      dependent_entry();
       for (int64_t c = blockIdx.x; c < n_chunks; c += gridDim.x)
       {
         const DevChunk ch = chunks[c];
@@ -114,6 +118,7 @@ namespace ttg
                                                         const Tile *__restrict__ tiles,
                                                         const TileChunk *__restrict__ chunks)
     {
+      dependent_entry();
       const TileChunk ch = chunks[blockIdx.x];
       const Tile &t = tiles[ch.tile];
       if (t.in_base < 0)
@@ -253,33 +258,35 @@ namespace ttg
       case OpKind::add:
       {
         const int64_t n = op.elements * (args.complex ? 2 : 1);
-        add_f64_kernel<<<grid_for(n, 256), 256, 0, args.stream>>>(reinterpret_cast<const double *>(src),
-                                                                 reinterpret_cast<double *>(dst), n);
-        e = check_launch();
+        e = launch_dependent(add_f64_kernel, grid_for(n, 256), 256, 0, args.stream, reinterpret_cast<const double *>(src),
+                             reinterpret_cast<double *>(dst), n);
         break;
       }
       case OpKind::gather:
         if (args.complex)
-          gather_kernel<double2><<<grid_for(op.elements, 256), 256, 0, args.stream>>>(
-            reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst), t.gather + op.begin, op.elements);
+          e = launch_dependent(gather_kernel<double2>, grid_for(op.elements, 256), 256, 0, args.stream,
+                               reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst),
+                               static_cast<const int32_t *>(t.gather + op.begin), op.elements);
         else
-          gather_kernel<double><<<grid_for(op.elements, 256), 256, 0, args.stream>>>(
-            reinterpret_cast<const double *>(src), reinterpret_cast<double *>(dst), t.gather + op.begin, op.elements);
-        e = check_launch();
+          e = launch_dependent(gather_kernel<double>, grid_for(op.elements, 256), 256, 0, args.stream,
+                               reinterpret_cast<const double *>(src), reinterpret_cast<double *>(dst),
+                               static_cast<const int32_t *>(t.gather + op.begin), op.elements);
         break;
       case OpKind::tiles:
         if (op.count > 0)
         {
+          const dim3 grid(static_cast<unsigned>(op.count));
+          const Tile *tiles = t.tiles;
+          const TileChunk *chunks = t.tile_chunks + op.begin;
           if (args.complex && (op.flags & 1))
-            tiles_kernel<double2, true><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
-              reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst), t.tiles, t.tile_chunks + op.begin);
+            e = launch_dependent(tiles_kernel<double2, true>, grid, 256, 0, args.stream, reinterpret_cast<const double2 *>(src),
+                                 reinterpret_cast<double2 *>(dst), tiles, chunks);
           else if (args.complex)
-            tiles_kernel<double2, false><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
-              reinterpret_cast<const double2 *>(src), reinterpret_cast<double2 *>(dst), t.tiles, t.tile_chunks + op.begin);
+            e = launch_dependent(tiles_kernel<double2, false>, grid, 256, 0, args.stream, reinterpret_cast<const double2 *>(src),
+                                 reinterpret_cast<double2 *>(dst), tiles, chunks);
           else
-            tiles_kernel<double, false><<<static_cast<unsigned>(op.count), 256, 0, args.stream>>>(
-              reinterpret_cast<const double *>(src), reinterpret_cast<double *>(dst), t.tiles, t.tile_chunks + op.begin);
-          e = check_launch();
+            e = launch_dependent(tiles_kernel<double, false>, grid, 256, 0, args.stream, reinterpret_cast<const double *>(src),
+                                 reinterpret_cast<double *>(dst), tiles, chunks);
         }
         break;
       case OpKind::runs:
@@ -289,12 +296,11 @@ namespace ttg
           const auto *ch = reinterpret_cast<const DevChunk *>(t.chunks) + op.begin;
           const auto *te = reinterpret_cast<const DevTerm *>(t.terms);
           if (args.complex)
-            runs_kernel<true><<<grid, kChunk, 0, args.stream>>>(reinterpret_cast<const double *>(src),
-                                                                 reinterpret_cast<double *>(dst), ch, te, op.count);
+            e = launch_dependent(runs_kernel<true>, grid, kChunk, 0, args.stream, reinterpret_cast<const double *>(src),
+                                 reinterpret_cast<double *>(dst), ch, te, op.count);
           else
-            runs_kernel<false><<<grid, kChunk, 0, args.stream>>>(reinterpret_cast<const double *>(src),
-                                                                  reinterpret_cast<double *>(dst), ch, te, op.count);
-          e = check_launch();
+            e = launch_dependent(runs_kernel<false>, grid, kChunk, 0, args.stream, reinterpret_cast<const double *>(src),
+                                 reinterpret_cast<double *>(dst), ch, te, op.count);
         }
         break;
       case OpKind::gemm:
