@@ -107,11 +107,28 @@ namespace ttg
       }
     }
 
-    // One chunk of a tile per CTA: a warp per output row, the row's part of the input offset
-    // computed once by its warp and the columns' part per entry (mixed radix over the copies of
-    // the output domain legs, the last fastest).  Writes are coalesced along the columns.
+    // One chunk of a tile per CTA.  The input offset of an entry is the sum of its row's part
+    // (mixed radix over the copies of the output codomain legs) and its column's part (the same
+    // over the domain legs, the last fastest): both are computed once per chunk into shared
+    // memory, then the chunk's entries are dealt to the threads in output order (coalesced
+    // writes, one division per entry).  A chunk wider than the tables falls back to computing the
+    // column part per entry.
     __device__ __forceinline__ double conj_of(double x) { return x; }
     __device__ __forceinline__ double2 conj_of(double2 x) { return make_double2(x.x, -x.y); }
+
+    constexpr int kTileTable = 2048;  // rows and columns of a chunk with precomputed offsets
+
+    __device__ __forceinline__ int64_t radix_offset(const Tile &t, int32_t first, int32_t last, int32_t index)
+    {
+      int64_t off = 0;
+      for (int32_t l = last; l >= first; --l)
+      {
+        const int32_t e = t.extent[l];
+        off += static_cast<int64_t>(index % e) * t.stride[l];
+        index /= e;
+      }
+      return off;
+    }
 
     template <typename T, bool Conj>
     __global__ void __launch_bounds__(256) tiles_kernel(const T *__restrict__ src, T *__restrict__ dst,
@@ -119,38 +136,44 @@ namespace ttg
                                                         const TileChunk *__restrict__ chunks)
     {
       dependent_entry();
+      __shared__ Tile t;
+      __shared__ int64_t row_off[kTileTable];
+      __shared__ int64_t col_off[kTileTable];
       const TileChunk ch = chunks[blockIdx.x];
-      const Tile &t = tiles[ch.tile];
+      if (threadIdx.x == 0) t = tiles[ch.tile];
+      __syncthreads();
       if (t.in_base < 0)
       {
         // the zero pad entry of an odd block
         if (threadIdx.x == 0) dst[t.out_base] = T{};
         return;
       }
-      const int32_t n_row = t.n_row, n_col = t.n_col, cols = t.cols;
-      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-      for (int32_t r = ch.row0 + warp; r < ch.row0 + ch.nrows; r += 8)
+      const int32_t n_row = t.n_row, n_col = t.n_col, cols = t.cols, rows = ch.nrows;
+      if (cols <= kTileTable && rows <= kTileTable)
       {
-        int64_t row_in = t.in_base;
-        int32_t rest = r;
-        for (int32_t l = n_row - 1; l >= 0; --l)
+        for (int32_t c = threadIdx.x; c < cols; c += blockDim.x) col_off[c] = radix_offset(t, n_row, n_row + n_col - 1, c);
+        for (int32_t r = threadIdx.x; r < rows; r += blockDim.x)
+          row_off[r] = t.in_base + radix_offset(t, 0, n_row - 1, ch.row0 + r);
+        __syncthreads();
+        T *out = dst + t.out_base + static_cast<int64_t>(ch.row0) * t.out_ld;
+        const int32_t n = rows * cols;
+        for (int32_t e = threadIdx.x; e < n; e += blockDim.x)
         {
-          const int32_t e = t.extent[l];
-          row_in += static_cast<int64_t>(rest % e) * t.stride[l];
-          rest /= e;
+          const int32_t r = e / cols, c = e - r * cols;
+          const T x = src[row_off[r] + col_off[c]];
+          out[static_cast<int64_t>(r) * t.out_ld + c] = Conj ? conj_of(x) : x;
         }
+        return;
+      }
+      const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+      for (int32_t r = ch.row0 + warp; r < ch.row0 + rows; r += 8)
+      {
+        const int64_t row_in = t.in_base + radix_offset(t, 0, n_row - 1, r);
         T *out = dst + t.out_base + static_cast<int64_t>(r) * t.out_ld;
         for (int32_t c = lane; c < cols; c += 32)
         {
-          int64_t in = row_in;
-          int32_t rc = c;
-          for (int32_t l = n_row + n_col - 1; l >= n_row; --l)
-          {
-            const int32_t e = t.extent[l];
-            in += static_cast<int64_t>(rc % e) * t.stride[l];
-            rc /= e;
-          }
-          out[c] = Conj ? conj_of(src[in]) : src[in];
+          const T x = src[row_in + radix_offset(t, n_row, n_row + n_col - 1, c)];
+          out[c] = Conj ? conj_of(x) : x;
         }
       }
     }

@@ -394,8 +394,9 @@ namespace ttg
                           double tol, T *norms, T *exchange, T *partial, int *flags)
     {
       const int64_t most = rows > vrows ? rows : vrows;
-      // the fewest lanes per pair that hold its rows in registers: per-pair scalar work (the angle,
-      // the norms) runs once per lane of the group
+      // the fewest lanes per pair that hold its rows in registers (measured faster than more lanes
+      // with shorter chains, in FP32 as in FP64, where the per-pair scalar work also runs once per
+      // lane of the group on the narrow FP64 pipe)
       if (most <= kNper) return sweeps<T, 1>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
       if (most <= 2 * kNper) return sweeps<T, 2>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
       if (most <= 4 * kNper) return sweeps<T, 4>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
