@@ -415,7 +415,7 @@ extern "C"
         if (op.kind == ttg::OpKind::gemm && p.gemm_plans && i < p.gemm_plans->f64.size())
         {
           // the FP64 schedule: items dealt to the SMs, K-split tiles and the longest list
-          const ttg::GemmSchedule &s = p.gemm_plans->f64[i];
+          const ttg::GemmSchedule s = ttg::schedule_gemm(p, op, ttg::kF64TileM, ttg::kF64TileN, true);
           int64_t longest = 0;
           for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c) longest = std::max<int64_t>(longest, s.cta_begin[c + 1] - s.cta_begin[c]);
           out += "  fp64 schedule: items " + std::to_string(s.items.size()) + " split tiles " + std::to_string(s.reduces.size()) +

@@ -52,6 +52,8 @@ namespace ttg
     // the split path, the rows and columns to slice
     struct GemmTables
     {
+      bool ready = false;            // built on the op's first FP64 launch, in an allocation of its own
+      void *base = nullptr;
       GemmItem *items = nullptr;
       GemmReduce *reduces = nullptr;
       int32_t *cta_begin = nullptr;  // per CTA, the start of its list of items (n_ctas + 1 entries)

@@ -43,7 +43,7 @@ namespace ttg
     int64_t up256(int64_t bytes) { return (bytes + 255) / 256 * 256; }
   } // namespace
 
-  GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn)
+  GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn, bool full)
   {
     GemmSchedule s;
     // The workers of one SM share its FP64 pipe, so what has to balance is the work per SM: items
@@ -74,6 +74,7 @@ namespace ttg
       double work;
     };
     std::vector<Sized> items;
+    int64_t n_items = 0;
     for (int64_t b = op.begin; b < op.begin + op.count; ++b)
     {
       const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(b)];
@@ -89,22 +90,27 @@ namespace ttg
           kc = std::max<int64_t>(16, (kc + 15) / 16 * 16);
           chunks = ktotal > 0 ? (ktotal + kc - 1) / kc : 1;
           const int32_t bi = static_cast<int32_t>(b);
+          n_items += chunks;
           if (chunks == 1)
           {
-            items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work});
+            if (full) items.push_back({{bi, m0, n0, 0, static_cast<int32_t>(ktotal), -1, -1, 0}, work});
             continue;
           }
           const int32_t slot0 = static_cast<int32_t>(s.slots), reduce = static_cast<int32_t>(s.reduces.size());
           for (int64_t c = 0; c < chunks; ++c)
           {
             const int64_t k0 = c * kc, k1 = std::min(ktotal, (c + 1) * kc);
-            items.push_back({{bi, m0, n0, static_cast<int32_t>(k0), static_cast<int32_t>(k1), static_cast<int32_t>(s.slots++),
-                              reduce, 0},
-                             cost(rows, cols, static_cast<double>(k1 - k0))});
+            if (full)
+              items.push_back({{bi, m0, n0, static_cast<int32_t>(k0), static_cast<int32_t>(k1), static_cast<int32_t>(s.slots),
+                                reduce, 0},
+                               cost(rows, cols, static_cast<double>(k1 - k0))});
+            ++s.slots;
           }
           s.reduces.push_back({bi, m0, n0, slot0, static_cast<int32_t>(chunks), 0});
         }
     }
+    s.n_items = n_items;
+    if (!full) return s;
     // largest first, equal work in the order made
     std::vector<int32_t> order(items.size());
     std::iota(order.begin(), order.end(), 0);
@@ -314,7 +320,7 @@ namespace ttg
     {
       const Op &op = p.ops[i];
       if (op.kind != OpKind::gemm) continue;
-      plans->f64[i] = schedule_gemm(p, op, kF64TileM, kF64TileN);
+      plans->f64[i] = schedule_gemm(p, op, kF64TileM, kF64TileN, false);
       // the split schedule itself is built on the first split launch (most plans never run one);
       // here only its scratch
       need = std::max(need, (f64_bytes(plans->f64[i]) + 7) / 8);
@@ -1101,10 +1107,37 @@ namespace ttg
   // launchers
   // ------------------------------------------------------------------------------------------
 
+  namespace
+  {
+    // The FP64 tables of a GEMM op, built on its first FP64 launch.
+    cudaError_t ensure_f64(const Program &p, DeviceTables &t, size_t op_index)
+    {
+      std::lock_guard<std::mutex> lock(t.mutex);
+      DeviceTables::GemmTables &dst = t.gemm[op_index];
+      if (dst.ready) return cudaSuccess;
+      const GemmSchedule s = schedule_gemm(p, p.ops[op_index], kF64TileM, kF64TileN, true);
+      dst.n_items = static_cast<int64_t>(s.items.size());
+      dst.n_reduces = static_cast<int64_t>(s.reduces.size());
+      dst.slots = s.slots;
+      dst.n_ctas = static_cast<int32_t>(s.cta_begin.size()) - 1;
+      dst.longest = 0;
+      for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c)
+        dst.longest = std::max<int64_t>(dst.longest, s.cta_begin[c + 1] - s.cta_begin[c]);
+      TableStaging staging;
+      staging.add(s.items, reinterpret_cast<void **>(&dst.items));
+      staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
+      staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
+      const cudaError_t e = staging.commit(&dst.base);
+      if (e != cudaSuccess) return e;
+      dst.ready = true;
+      return cudaSuccess;
+    }
+  } // namespace
+
   cudaError_t launch_gemm_f64(const Program &p, DeviceTables &t, size_t op_index, const void *A, const void *B, void *C,
                               bool complex, void *scratch, int *ticket_region, cudaStream_t stream)
   {
-    (void)p;
+    if (const cudaError_t built = ensure_f64(p, t, op_index); built != cudaSuccess) return built;
     const auto &sched = t.gemm[op_index];
     if (sched.n_items == 0) return cudaSuccess;
     const auto *blocks = reinterpret_cast<const DevBlock *>(t.blocks);
@@ -1188,9 +1221,10 @@ namespace ttg
     {
       if (begin >= end) return cudaSuccess;
       const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
+      // a warp per line, two warps per CTA so that the lines spread over every SM
       return launch_dependent(split_lines_kernel,
-                              static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 7) / 8, 152 * 16))),
-                              256, 0, stream, A, B, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, lines,
+                              static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 1) / 2, 152 * 32))),
+                              64, 0, stream, A, B, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, lines,
                               sched.n_lines_a, begin, end, slices);
     }
   } // namespace
@@ -1293,20 +1327,7 @@ namespace ttg
     for (size_t i = 0; i < p.ops.size(); ++i)
     {
       if (p.ops[i].kind != OpKind::gemm) continue;
-      {
-        const GemmSchedule &s = p.gemm_plans->f64[i];
-        DeviceTables::GemmTables &dst = t.gemm[i];
-        dst.n_items = static_cast<int64_t>(s.items.size());
-        dst.n_reduces = static_cast<int64_t>(s.reduces.size());
-        dst.slots = s.slots;
-        dst.n_ctas = static_cast<int32_t>(s.cta_begin.size()) - 1;
-        dst.longest = 0;
-        for (size_t c = 0; c + 1 < s.cta_begin.size(); ++c)
-          dst.longest = std::max<int64_t>(dst.longest, s.cta_begin[c + 1] - s.cta_begin[c]);
-        staging.add(s.items, reinterpret_cast<void **>(&dst.items));
-        staging.add(s.reduces, reinterpret_cast<void **>(&dst.reduces));
-        staging.add(s.cta_begin, reinterpret_cast<void **>(&dst.cta_begin));
-      }
+      // the FP64 tables are built on the op's first FP64 launch (ensure_f64)
     }
   }
 

@@ -38,6 +38,7 @@ namespace ttg
     std::vector<GemmReduce> reduces;
     std::vector<int32_t> cta_begin;  // CTA b runs items [cta_begin[b], cta_begin[b + 1])
     int64_t slots = 0;               // partial tiles of bm x bn doubles
+    int64_t n_items = 0;             // items (also when only the sizes were computed)
   };
   // The CTAs a schedule spreads its items over: one per SM of the GPU.
   constexpr int kScheduleCtas = 152;
@@ -87,7 +88,9 @@ namespace ttg
   constexpr int kMaxSlices = 8;
   constexpr int kExactChunk = 256;  // K over which fp32 sums of slice products stay exact
 
-  GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn);
+  // The FP64 schedule of a GEMM op; with full = false only its sizes (items, partial slots,
+  // reductions), for sizing the scratch: the items are dealt on the op's first FP64 launch.
+  GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn, bool full = true);
 
   // Scratch doubles a program's GEMM ops need at most (FP64 partials, or slices + exponents +
   // partials for split precision), laid out per op from offset 0.

@@ -185,7 +185,6 @@ namespace ttg
       return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, 152 * 8)));
     }
 
-    cudaError_t check_launch() { return cudaGetLastError(); }
   } // namespace
 
   // --------------------------------------------------------------------------------------------
@@ -195,6 +194,8 @@ namespace ttg
   DeviceTables::~DeviceTables()
   {
     if (base) cudaFree(base);
+    for (GemmTables &g : gemm)
+      if (g.base) cudaFree(g.base);
     for (SplitTables &g : split)
       if (g.base) cudaFree(g.base);
   }

@@ -431,6 +431,7 @@ namespace ttg
           const Block &ob = out->blocks[bi];
           const int32_t rr = cod_root.at(ob.key.codomain), cr = dom_root.at(ob.key.domain);
           if (ob.key.copy == 0) block_of[static_cast<size_t>(rr) * dom_root.size() + static_cast<size_t>(cr)] = static_cast<int32_t>(bi);
+          if (ob.key.copy != 0) continue;  // the trees of a root are the same for every copy
           for (const auto &[side, root, number, table, at] :
                {std::make_tuple(&out_cod, ob.key.codomain, rr, &rows_of, &row_at),
                 std::make_tuple(&out_dom, ob.key.domain, cr, &cols_of, &col_at)})

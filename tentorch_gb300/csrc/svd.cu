@@ -55,7 +55,6 @@ namespace ttg
     constexpr int kSvdThreads = 512;
     constexpr int kMaxSweeps = 40;
     constexpr int kMaxCols = 1024;              // k = min(rows, cols) of a block
-    constexpr int kMaxPairs = kMaxCols / 2;     // pairs of a round
     constexpr int kSvdSmemBytes = 227 * 1024;
     constexpr int kStaticBytes = 21 * 1024;     // the norms, their shares, ranks and flags of the kernel
     constexpr int64_t kDynamicBytes = kSvdSmemBytes - kStaticBytes - 1024;

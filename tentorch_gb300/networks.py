@@ -311,16 +311,19 @@ class DMRG:
     `dtype` selects the scalar type of the state and the operator (the reference builds complex128;
     float64 is exact for U(1) and no symmetry).  `generator` draws the starting state reproducibly
     (see `MPS.random`).  `precision` chooses the block products of the Lanczos matvec (0: FP64;
-    k: k bf16 slices, see `tentorch_gb300.precision`); environments, head and tail, SVDs and the
-    Lanczos vector algebra stay FP64.'''
+    k: k bf16 slices, see `tentorch_gb300.precision`); with `all_products` also those of the
+    environments, head and tail and the two-site contraction.  The SVDs, the Lanczos vector algebra
+    and the tridiagonal eigensolve stay FP64 either way.'''
 
     def __init__(self, model: Model, max_bond_dim: int = 50, svd_tol: float = 1e-14, n_iter: int = 5, seed: int = 0,
-                 dtype = None, device = None, generator: Optional[torch.Generator] = None, precision: int = 0) -> None:
+                 dtype = None, device = None, generator: Optional[torch.Generator] = None, precision: int = 0,
+                 all_products: bool = False) -> None:
         self.model = model
         self.max_bond_dim = max_bond_dim
         self.svd_tol = svd_tol
         self.n_iter = n_iter
         self.precision = precision
+        self.all_products = all_products
         self.operator = heisenberg(model.cat, model.length, model.coupling, dtype = dtype, device = device)
         physical = model.physical if model.physical is not None else self.operator.physical
         self.state = MPS.random(model.cat, physical, model.length, model.sector, seed = seed, dtype = dtype,
@@ -381,6 +384,12 @@ class DMRG:
 
     def sweep(self) -> tuple[float, float]:
         '''tentorch/algorithms/dmrg.py:131-161'''
+        if self.all_products and self.precision > 0:
+            with precision(self.precision):
+                return self._sweep()
+        return self._sweep()
+
+    def _sweep(self) -> tuple[float, float]:
         self.state.move_center(0)
         self.cache_environments()
         energy, discarded = 0.0, 0.0

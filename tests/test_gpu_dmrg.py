@@ -3,8 +3,8 @@ two-site DMRG of the Heisenberg chain, in the reference's float64 harness (float
 N(0, 1) in block-key order from `torch.Generator().manual_seed(seed)`, float64 MPO and identities).
 Every sweep energy of the reference (L = 4, 6, 8 with bond 64; L = 16 with bond 32) is met within
 1e-10, the bond dimensions exactly, and the final energies within 1e-10 of exact diagonalisation
-where the bond is not truncating; the split-precision matvec (8 bf16 slices) gives the same
-energies within 1e-10.'''
+where the bond is not truncating; the split-precision matvec (8 bf16 slices), and every block
+product of a sweep in 6 slices, give the same energies within 1e-10.'''
 import numpy as np
 import pytest
 import torch
@@ -18,10 +18,10 @@ pytestmark = pytest.mark.gpu
 ENERGY_TOL = 1e-10
 
 
-def _driver(length, bond, seed = 0, precision = 0, n_iter = 5):
+def _driver(length, bond, seed = 0, precision = 0, n_iter = 5, all_products = False):
     return nw.DMRG(nw.Model(length, cat = tg.u1), max_bond_dim = bond, n_iter = n_iter, seed = seed,
                    dtype = torch.float64, device = 'cuda', generator = torch.Generator().manual_seed(seed),
-                   precision = precision)
+                   precision = precision, all_products = all_products)
 
 
 @pytest.mark.parametrize('length', [4, 6, 8])
@@ -37,9 +37,9 @@ def test_small_chains_match_the_reference_and_exact_diagonalisation(length):
     assert abs(final.real - golden['exact'][str(length)]) < ENERGY_TOL
 
 
-def _config1(precision):
+def _config1(precision, all_products = False):
     golden = load_json('dmrg.json')['config1']
-    driver = _driver(golden['length'], golden['max_bond_dim'], golden['seed'], precision, golden['n_iter'])
+    driver = _driver(golden['length'], golden['max_bond_dim'], golden['seed'], precision, golden['n_iter'], all_products)
     out = []
     for want in golden['sweeps']:
         energy, lost = driver.sweep()
@@ -56,8 +56,11 @@ def test_sixteen_sites_bond_32_matches_the_reference_sweep_by_sweep():
     assert sweeps[-1][0] - golden['exact'] < 1e-8
 
 
-def test_split_precision_sweeps_keep_the_fp64_energies():
-    sweeps, _ = _config1(8)
+@pytest.mark.parametrize('slices, all_products', [(8, False), (6, True)])
+def test_split_precision_sweeps_keep_the_fp64_energies(slices, all_products):
+    '''The Lanczos matvec in split precision, or every block product of the sweep (environments,
+    head and tail too): the reference's FP64 sweep energies within 1e-10, the bonds exactly.'''
+    sweeps, _ = _config1(slices, all_products)
     for energy, lost, bonds, want in sweeps:
         assert abs(energy - want['energy']) < ENERGY_TOL, (energy, want['energy'])
         assert bonds == want['bond']
