@@ -259,10 +259,11 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     in three forms from one FP64 state: `warm` FP64 sweeps grow the bond to chi, then each form
     runs one sweep from a copy of that state, with the plan caches cleared first so that every
     form compiles its plans inside its sweep.  Forms: split (grouped kernels, the Lanczos matvec in
-    split precision), split_all_products (every block product of the sweep in split precision:
-    environments, head and tail too), fp64_grouped (the grouped kernels in FP64) and
-    fp64_per_block (one cuBLAS call per block pair and one SVD per block, as the reference runs on
-    a CUDA device).  Wall time around the sweep, the device synchronised on both sides."""
+    split precision), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one cuBLAS
+    call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
+    around the sweep, the device synchronised on both sides.  (Every block product in split
+    precision, environments included, measured 0.90 s against 0.85 s at 6 slices, with |dE| =
+    2e-10: not the headline form at this bond.)"""
     from tentorch_gb300 import networks as nw
     from tentorch_gb300.linalg import PER_BLOCK, clear_plans
     tg.set_precision(0)
@@ -274,8 +275,7 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     warm_s = time.perf_counter() - start
     snapshot = ([t.clone() for t in driver.state.tensors], driver.state.center)
     out = {}
-    for name, form, every in (('fp64_grouped', 0, False), ('split', precision, False),
-                              ('split_all_products', precision, True), ('fp64_per_block', PER_BLOCK, False)):
+    for name, form, every in (('fp64_grouped', 0, False), ('split', precision, False), ('fp64_per_block', PER_BLOCK, False)):
         driver.state.tensors = [t.clone() for t in snapshot[0]]
         driver.state.center = snapshot[1]
         driver.precision = form
@@ -302,8 +302,6 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     return {'length': length, 'chi': chi, 'n_iter': n_iter, 'warm_fp64_sweeps': warm, 'warm_s': warm_s,
             'forms': out,
             'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
-            'speedup_split_all_products_vs_per_block':
-                out['fp64_per_block']['s_per_sweep'] / out['split_all_products']['s_per_sweep'],
             'speedup_split_vs_fp64_grouped': out['fp64_grouped']['s_per_sweep'] / out['split']['s_per_sweep'],
             'start': f'{warm} FP64 sweeps from the seeded random MPS (N(0,1) float64 blocks in key order, seed {SEED})'}
 

@@ -17,7 +17,8 @@
 //      V <- V + V (I - V^T V) / 2 (quadratic: 1e-6 -> 1e-12 -> round-off).
 //   3. W = A V in FP64 (columns already orthogonal to ~1e-6).
 //   4. FP64 sweeps on W with V accumulated: from a start that close, Jacobi's quadratic
-//      convergence needs two sweeps and a third that finds nothing to rotate.
+//      convergence needs two or three sweeps; a sweep whose cosines were all below sqrt(tol) is
+//      the last (the cosines it leaves are below ~tol).
 // In the FP64 sweeps only the dot product of the pair is taken (the squared column norms are
 // carried along with the exact update of a rotation and recomputed at each sweep's start), and the
 // angle is found in FP32 and then made exactly orthogonal in FP64 (c^2 + s^2 = 1 by a second-order
@@ -261,12 +262,13 @@ namespace ttg
     }
 
     // Jacobi sweeps over W (column-major, `rows` rows) with the rotations accumulated into V
-    // (`vrows` rows), until a sweep rotates nothing (or kMaxSweeps).  Alone, one CTA holds every
+    // (`vrows` rows), until a sweep rotates no pair whose cosine is above sqrt(tol) (or
+    // kMaxSweeps); pairs below tol are not rotated.  Alone, one CTA holds every
     // row; otherwise the rows are dealt to the CTAs of the cluster: per round each CTA takes its
     // rows' share of every pair's dot product, the shares cross the cluster through distributed
     // shared memory and every CTA adds them in the same order, so that all hold the same dot
     // products, angles and norms, and rotates its own rows.  One cluster barrier per round (shares
-    // double-buffered) and two per sweep; whether a sweep rotated anything is read from rank 0, so
+    // double-buffered) and two per sweep; whether a sweep ended the phase is read from rank 0, so
     // every CTA leaves the loop together.  FP32: everything in FP32; FP64: the angle in FP32 made
     // exactly orthogonal in FP64 (exact_rotation; an angle good to 1e-7 still shrinks the pair's
     // cosine by that factor each rotation).  Only the pair's dot product is taken: the squared norms are
@@ -286,6 +288,10 @@ namespace ttg
       constexpr int per_warp = 32 / G;
       const int64_t players = k + (k & 1), pairs = players / 2;
       const T tol2 = static_cast<T>(tol * tol);
+      // a sweep whose rotations all had cosines below sqrt(tol) ends the phase: Jacobi converges
+      // quadratically there, so the cosines it leaves are below ~tol and a further sweep (which
+      // would find nothing above tol to rotate) is not run
+      const T settled2 = static_cast<T>(tol);
       for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
       {
         for (int64_t j = warp; j < k; j += warps)
@@ -342,7 +348,7 @@ namespace ttg
                 const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
                 norms[p] = cc * alpha - cs2 + ss * beta;
                 norms[q] = ss * alpha + cs2 + cc * beta;
-                flags[sweep & 1] = 1;
+                if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
               }
             }
           }
@@ -375,7 +381,7 @@ namespace ttg
                 const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
                 norms[p] = cc * alpha - cs2 + ss * beta;
                 norms[q] = ss * alpha + cs2 + cc * beta;
-                flags[sweep & 1] = 1;
+                if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
               }
             }
           }

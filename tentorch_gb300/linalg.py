@@ -371,8 +371,10 @@ def _factor_blocks(arranged: Tensor):
     stream = torch.cuda.current_stream(device).cuda_stream
     check(lib.tt_svd_blocks(len(present), largest, dev_table.data_ptr(), arranged._data.data_ptr(), u.data_ptr(),
                             sv.data_ptr(), vh.data_ptr(), ws.data_ptr(), info.data_ptr(), stream))
+    # the sweep counts come back with the values: one wait for both
+    info_host = info[:max(len(present), 1)].to('cpu', non_blocking = True)
     host = sv[:s_at].cpu().tolist()
-    if present and int(info[:len(present)].min()) < 0:
+    if present and int(info_host.min()) < 0:
         raise RuntimeError('the Jacobi SVD of a block did not converge')
     factors = [[key, (u_off, rows, k), (s_off, k), (vh_off, k, cols), 0, 0]
                for key, rows, cols, k, u_off, s_off, vh_off in shapes]

@@ -226,8 +226,9 @@ def cases():
 
 
 def dmrg_energies():
-    '''The reference's DMRG in float64 (the harness of SURVEY 8(c)): float64 random MPS blocks drawn
-    in key order from a seeded generator, float64 identities and MPO blocks.'''
+    '''The reference's DMRG in float64: its random MPS patched to draw float64 blocks in key order
+    from a seeded generator, its identities and MPO blocks cast to float64 (the reference builds
+    complex128 by default).'''
     import tentorch.networks.mps as mps_module
     dmrg_module = sys.modules['tentorch.algorithms.dmrg']
     import importlib.util
