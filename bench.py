@@ -261,9 +261,9 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     form compiles its plans inside its sweep.  Forms: split (grouped kernels, the Lanczos matvec in
     split precision), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one cuBLAS
     call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
-    around the sweep, the device synchronised on both sides.  (Every block product in split
-    precision, environments included, measured 0.90 s against 0.85 s at 6 slices, with |dE| =
-    2e-10: not the headline form at this bond.)"""
+    around the sweep, the device synchronised on both sides.  (Every block product of the sweep in
+    split precision, environments included, is the driver's `all_products` option; at this bond it
+    is slower than the matvec alone in split precision and, at 6 slices, outside the 1e-10 bar.)"""
     from tentorch_gb300 import networks as nw
     from tentorch_gb300.linalg import PER_BLOCK, clear_plans
     tg.set_precision(0)
@@ -275,11 +275,10 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     warm_s = time.perf_counter() - start
     snapshot = ([t.clone() for t in driver.state.tensors], driver.state.center)
     out = {}
-    for name, form, every in (('fp64_grouped', 0, False), ('split', precision, False), ('fp64_per_block', PER_BLOCK, False)):
+    for name, form in (('fp64_grouped', 0), ('split', precision), ('fp64_per_block', PER_BLOCK)):
         driver.state.tensors = [t.clone() for t in snapshot[0]]
         driver.state.center = snapshot[1]
         driver.precision = form
-        driver.all_products = every
         tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
         clear_plans()
         mv0 = driver.matvecs
