@@ -1061,18 +1061,6 @@ namespace ttg
       }
     }
 
-    // the persistent grid: one CTA per SM (or fewer when there are fewer items than workers)
-    int sm_count()
-    {
-      static int count = 0;
-      if (!count)
-      {
-        int device = 0;
-        cudaGetDevice(&device);
-        if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || count <= 0) count = 152;
-      }
-      return count;
-    }
 
     // Shared memory that holds one CTA per SM: at least 120 KiB, so a second never fits beside it.
     constexpr int kPinBytes = 120 * 1024;
