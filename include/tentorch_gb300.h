@@ -119,7 +119,10 @@ int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *
  * cap < *count.  For checking compiled leg moves against
  * the reference's per-step plans (tentorch/tensors/place.cpp:199-247). */
 int32_t tt_plan_gather(const tt_plan *plan, int32_t op, int64_t cap, int32_t *index, int64_t *count);
-/* Elements of operand `i`'s prepared arena, 0 when the operand needs no preparation. */
+/* Elements (float64-sized, or of the dtype if larger) of operand `i`'s prepared arena, 0 when the
+ * operand needs no preparation.  The arena holds the operand after its leg moves and, for block
+ * products that read it, its split-precision slices (cut once by tt_plan_prepare, read by every
+ * split execution that is given the arena). */
 int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements);
 /* Execute on `stream` (a cudaStream_t, 0 for the legacy stream).  precision 0: FP64 block
  * products in the grouped persistent kernels; k >= 1: split products on the tensor cores with k
@@ -139,7 +142,9 @@ int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, c
 int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                               const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
                               float *op_ms, int32_t *op_kind);
-/* Run operand `operand`'s preparation only, writing its prepared arena. */
+/* Run operand `operand`'s preparation only, writing its prepared arena (for float64 also the
+ * slices of it that split-precision products read).  The arena stays valid while the operand's
+ * arena is unchanged; a changed operand needs a new preparation. */
 int32_t tt_plan_prepare(const tt_plan *plan, int32_t dtype, int32_t operand, const void *input, void *prepared,
                         void *workspace, void *stream);
 
