@@ -123,3 +123,21 @@ def test_qr_and_rq_factor_the_tensor():
     assert torch.max(torch.abs(tg.contract(l, qq, [1], [0]).data - t.data)).item() < 1e-13
     for v in _blocks(qq).values():
         assert torch.max(torch.abs(v @ v.T - torch.eye(v.shape[0], dtype = torch.float64, device = 'cuda'))).item() < 1e-13
+
+
+def test_a_block_too_large_for_shared_memory_splits_through_the_workspace():
+    '''A 700 x 600 block: its rows dealt over a cluster still do not fit in shared memory, so the
+    FP32 and FP64 sweeps keep W and V in the global workspace.  Values against LAPACK to 1e-12
+    relative, factors orthonormal to 1e-13, the product back to the block to 1e-12.'''
+    t = _tensor({0: 700}, {0: 600}, seed = 7)
+    first, values, second = tg.svd(t)
+    block = t.data[:700 * 600].reshape(700, 600)
+    want = torch.linalg.svdvals(block.cpu())
+    assert torch.allclose(values.cpu(), want, rtol = 1e-12, atol = 0)
+    u = first.data[:700 * 600].reshape(700, 600)
+    vh = second.data[:600 * 600].reshape(600, 600)
+    eye = torch.eye(600, dtype = torch.float64, device = 'cuda')
+    assert torch.max(torch.abs(u.T @ u - eye)).item() < 1e-13
+    assert torch.max(torch.abs(vh @ vh.T - eye)).item() < 1e-13
+    product = (u * values) @ vh
+    assert torch.max(torch.abs(product - block)).item() < 1e-12 * torch.max(torch.abs(block)).item()
