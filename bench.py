@@ -69,6 +69,19 @@ def config(args, precision):
             'parallelism': f'replicas x{args.gpus}'}
 
 
+def job_rate(total_ms, steps, world, device = 'cpu'):
+    """The whole job's rate over `world` replicas that each ran `steps` steps: the slowest rank's
+    time (max over ranks, so every rank returns the same numbers) and the units all ranks processed
+    per second of it."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], dtype = torch.float64, device = device)
+        dist.all_reduce(t, op = dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    return total_ms, world * steps / (total_ms / 1e3)
+
+
 def bond_multiplicities(chi, qmax = 8):
     """The bond of the matvec workload: U(1) charges 2q for q = -qmax..qmax, one multiplet each and
     the rest apportioned proportional to exp(-q^2/8): floors first, the leftover in +-q pairs by
@@ -375,13 +388,8 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize(device)
     if world > 1:
         dist.barrier()
-    total_ms = sum(times)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype = torch.float64, device = device)
-        dist.all_reduce(t, op = dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = job_rate(sum(times), args.steps, world, device)
     ms_per_step = total_ms / args.steps
-    value = world * args.steps / (total_ms / 1e3)
 
     # the other forms on the same GPU and the same inputs
     form_ms = {'split': ms_per_step}
