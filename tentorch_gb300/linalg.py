@@ -113,24 +113,34 @@ _prepared = {}
 # (device index, stream, dtype) -> a workspace arena that grows to the largest plan run on it; the
 # ops of one stream run in order, so consecutive plans share it
 _pools = {}
+# set once a plan has run inside a CUDA graph capture: the graph holds the device addresses of its
+# tables and workspace, so the automatic clear at the budget no longer runs
+_captured = False
 
 
 def clear_plans() -> None:
     '''Forget every compiled plan, here and in the engine (their device tables are freed): the next
-    contraction of each shape compiles again.  Runs by itself when the cache reaches its budget; by
-    hand, for timing compilation.'''
-    global _generation
+    contraction of each shape compiles again.  Runs by itself when the cache reaches its budget
+    (unless a CUDA graph captured plans of this process); by hand, for timing compilation.  A CUDA
+    graph captured before a clear launches freed tables: capture it again after one.'''
+    global _generation, _captured
     _generation += 1
+    _captured = False
     _plans.clear()
     _prepared.clear()
     _pools.clear()
     check(lib.tt_plan_cache_clear())
 
 
+def _note_capture() -> None:
+    global _captured
+    _captured = True
+
+
 def _plan(key, build, cat) -> Plan:
     plan = _plans.get(key)
     if plan is None:
-        if len(_plans) >= _PLAN_BUDGET:
+        if len(_plans) >= _PLAN_BUDGET and not _captured:
             clear_plans()
         handle = vp()
         check(build(ctypes.byref(handle)))
@@ -203,7 +213,9 @@ def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool 
     stream = torch.cuda.current_stream(device).cuda_stream
     ws = _workspace(plan, device, data0.dtype, stream)
     # a captured CUDA graph reads every operand from its own buffer at each replay, never a prepared copy
-    reuse_prepared = reuse_prepared and not torch.cuda.is_current_stream_capturing()
+    if torch.cuda.is_current_stream_capturing():
+        _note_capture()
+        reuse_prepared = False
     prepared = [(_prepared_arena(plan, i, t, ws, stream) if reuse_prepared else None) for i, t in enumerate(tensors)]
     inputs = pointers(t._data.data_ptr() for t in tensors)
     prep = pointers((p.data_ptr() if p is not None else None) for p in prepared)
