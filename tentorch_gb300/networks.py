@@ -363,6 +363,12 @@ class DMRG:
 
     def update(self, direction: Literal['left', 'right']) -> tuple[float, float]:
         '''tentorch/algorithms/dmrg.py:96-129'''
+        energy, lost = self._update(direction)
+        return energy, float(lost)
+
+    def _update(self, direction: Literal['left', 'right']) -> tuple[float, torch.Tensor]:
+        '''One window, with the discarded weight left on the device and the centre normalised there:
+        the window's only host waits are the Krylov loop's and the split's reads of its values.'''
         at = self.center
         first, second = self.state.tensors[at], self.state.tensors[at + 1]
         two = contract(first, second, domain_legs(first), [0])
@@ -379,8 +385,9 @@ class DMRG:
         left, values, right = svd(vector, self.max_bond_dim, self.svd_tol, factor)
         self.state.tensors[at], self.state.tensors[at + 1] = left, right.place([0, 1])
         self.center = at + 1 if direction == 'right' else at
-        self.state.normalize()
-        return energy, 1.0 - float(torch.sum(values * values).real)
+        centre = self.state.tensors[self.center]._data
+        centre.div_(torch.linalg.vector_norm(centre))
+        return energy, 1.0 - torch.sum(values * values).real
 
     def sweep(self) -> tuple[float, float]:
         '''tentorch/algorithms/dmrg.py:131-161'''
@@ -392,21 +399,23 @@ class DMRG:
     def _sweep(self) -> tuple[float, float]:
         self.state.move_center(0)
         self.cache_environments()
-        energy, discarded = 0.0, 0.0
+        energy, lost = 0.0, []
         for at in range(self.L - 1):
-            energy, lost = self.update('right')
-            discarded = max(discarded, lost)
+            energy, weight = self._update('right')
+            lost.append(weight)
             if at < self.L - 2:
                 self.left[at + 1] = self._advance_left(self.left[at], at)
         self.state._right_canonicalize(self.L - 1)
         self.right[self.L - 1] = self._advance_right(self.right[self.L], self.L - 1)
         for at in range(self.L - 3, -1, -1):
             self.center = at
-            energy, lost = self.update('left')
-            discarded = max(discarded, lost)
+            energy, weight = self._update('left')
+            lost.append(weight)
             if at > 0:
                 self.right[at + 1] = self._advance_right(self.right[at + 2], at + 1)
-        return energy, discarded
+        # the largest weight any window discarded, read once per sweep
+        discarded = float(torch.stack(lost).max()) if lost else 0.0
+        return energy, max(discarded, 0.0)
 
     def energy(self) -> complex:
         '''tentorch/algorithms/dmrg.py:163-179'''
