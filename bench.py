@@ -271,14 +271,15 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     """The two-site DMRG of the U(1) Heisenberg chain (tentorch/algorithms/dmrg.py) timed per sweep
     in three forms from one FP64 state: `warm` FP64 sweeps grow the bond to chi, then each form
     runs one sweep from a copy of that state, with the plan caches cleared first so that every
-    form compiles its plans inside its sweep.  Forms: split (grouped kernels, the Lanczos matvec in
+    form compiles its plans inside its sweep, and then the next sweep of its run with the plans
+    kept (`s_per_sweep_continued`: the steady state of a long run, where the shapes recur).  Forms: split (grouped kernels, the Lanczos matvec in
     split precision), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one cuBLAS
     call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
     around the sweep, the device synchronised on both sides.  (Every block product of the sweep in
     split precision, environments included, is the driver's `all_products` option; at this bond it
     is slower than the matvec alone in split precision and, at 6 slices, outside the 1e-10 bar.)"""
     from tentorch_gb300 import networks as nw
-    from tentorch_gb300.linalg import PER_BLOCK, clear_plans
+    from tentorch_gb300.linalg import PER_BLOCK, cached_plans, clear_plans
     tg.set_precision(0)
     driver = nw.DMRG(nw.Model(length, cat = tg.u1), max_bond_dim = chi, n_iter = n_iter, dtype = torch.float64,
                      device = device, generator = torch.Generator().manual_seed(SEED), precision = 0)
@@ -305,6 +306,18 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
         check = driver.energy().real
         out[name] = {'s_per_sweep': elapsed, 'energy': energy, 'energy_fp64_check': check,
                      'discarded': lost, 'matvecs': driver.matvecs - mv0, 'max_bond': max(driver.state.bond_dims)}
+        # the next sweep of the same run, its plans cached by the first where the shapes recur
+        # (as in a long run); it compiles only the shapes that the truncations changed
+        tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
+        plans0 = cached_plans()
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        energy2, _ = driver.sweep()
+        torch.cuda.synchronize(device)
+        out[name]['s_per_sweep_continued'] = time.perf_counter() - t0
+        out[name]['continued_energy'] = energy2
+        out[name]['continued_plans_compiled'] = cached_plans() - plans0
+        tg.set_precision(0)
     tg.set_precision(0)
     clear_plans()
     ref = out['fp64_grouped']['energy']
@@ -315,6 +328,8 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
             'forms': out,
             'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
             'speedup_split_vs_fp64_grouped': out['fp64_grouped']['s_per_sweep'] / out['split']['s_per_sweep'],
+            'speedup_split_vs_per_block_continued': out['fp64_per_block']['s_per_sweep_continued'] /
+                                                    out['split']['s_per_sweep_continued'],
             'start': f'{warm} FP64 sweeps from the seeded random MPS (N(0,1) float64 blocks in key order, seed {SEED})'}
 
 

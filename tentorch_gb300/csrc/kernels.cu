@@ -12,6 +12,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -200,14 +201,50 @@ namespace ttg
       if (g.base) cudaFree(g.base);
   }
 
+  namespace
+  {
+    // A non-blocking stream per device for table uploads.
+    cudaError_t upload_stream(cudaStream_t *stream)
+    {
+      static std::mutex mutex;
+      static std::map<int, cudaStream_t> streams;
+      int device = 0;
+      cudaError_t e = cudaGetDevice(&device);
+      if (e != cudaSuccess) return e;
+      std::lock_guard<std::mutex> lock(mutex);
+      auto found = streams.find(device);
+      if (found == streams.end())
+      {
+        cudaStream_t created = nullptr;
+        if ((e = cudaStreamCreateWithFlags(&created, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        found = streams.emplace(device, created).first;
+      }
+      *stream = found->second;
+      return cudaSuccess;
+    }
+  } // namespace
+
   cudaError_t TableStaging::commit(void **base)
   {
     *base = nullptr;
     if (host.empty()) return cudaSuccess;
-    cudaError_t e = cudaMalloc(base, host.size());
+    // The copy runs on a stream of its own and is waited for here, so the tables are in device
+    // memory before any stream launches a kernel that reads them: a plain copy from pageable
+    // memory may still be in flight when it returns, ordered only against the legacy stream.
+    cudaStream_t stream = nullptr;
+    cudaError_t e = upload_stream(&stream);
     if (e != cudaSuccess) return e;
-    if ((e = cudaMemcpy(*base, host.data(), host.size(), cudaMemcpyHostToDevice)) != cudaSuccess) return e;
-    for (const auto &[at, device] : slots) *device = static_cast<char *>(*base) + at;
+    void *device = nullptr;
+    if ((e = cudaMalloc(&device, host.size())) != cudaSuccess) return e;
+    e = cudaMemcpyAsync(device, host.data(), host.size(), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess)
+    {
+      cudaFree(device);
+      return e;
+    }
+    *base = device;
+    for (const auto &[at, slot] : slots) *slot = static_cast<char *>(device) + at;
     return cudaSuccess;
   }
 

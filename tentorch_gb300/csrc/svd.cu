@@ -80,9 +80,12 @@ namespace ttg
     // One block's global workspace, in doubles: V and its next iterate (k x k each) and G = V^T V
     // for the Newton-Schulz steps; W (len x k) and V (k x k) by rank for working sets that do not
     // fit in shared memory (up to kMaxCluster - 1 padding rows each), in FP64 and again in FP32.
+    // For a block preconditioned by QR: its columns in their sorted order factored in place (R on
+    // and above the diagonal, the Householder vectors below it; len x k, column-major), the
+    // Householder scalars, the sorted order (k indices), and the product Q [J; 0] (len x k).
     struct SvdLayout
     {
-      int64_t v0, v1, g, w_slices, v_slices, w32_slices, v32_slices, total;
+      int64_t v0, v1, g, w_slices, v_slices, w32_slices, v32_slices, f, tau, order, b, total;
     };
     __host__ __device__ inline SvdLayout svd_layout(int64_t len, int64_t k)
     {
@@ -94,10 +97,16 @@ namespace ttg
       l.v_slices = l.w_slices + (len + kMaxCluster) * k;
       l.w32_slices = l.v_slices + (k + kMaxCluster) * k;
       l.v32_slices = l.w32_slices + ((len + kMaxCluster) * k + 1) / 2;
-      l.total = l.v32_slices + ((k + kMaxCluster) * k + 1) / 2;
+      l.f = l.v32_slices + ((k + kMaxCluster) * k + 1) / 2;
+      l.tau = l.f + len * k;
+      l.order = l.tau + k;
+      l.b = l.order + k;
+      l.total = l.b + len * k;
       l.total = (l.total + 31) / 32 * 32;
       return l;
     }
+    // Blocks of at least this many columns (swept over a cluster) are preconditioned by QR.
+    constexpr int64_t kQrMinCols = 32;
 
     // The circle method's pair t of a round (players even, round < players - 1, t < players / 2):
     // player players - 1 stays, the others turn; p < q.  In 32-bit arithmetic with one conditional
@@ -478,15 +487,135 @@ namespace ttg
       double *v_cur = ws + lay.v0, *v_next = ws + lay.v1, *g = ws + lay.g;
       double *stage = reinterpret_cast<double *>(dynamic + kDynamicBytes - kStageBytes);
       const double *src = a + e.a_off;
-      const auto entry = [&](int64_t row, int64_t col) -> double
+      const auto entry_a = [&](int64_t row, int64_t col) -> double
       { return wide ? src[col * n + row] : src[row * n + col]; };  // row < len, col < k
+
+      // 0. Preconditioning (blocks swept over a cluster): the columns sorted by norm, largest
+      // first, and factored A P = Q R by Householder reflections; the sweeps then run on X = R^T
+      // (k x k), whose graded columns the FP32 sweeps orthogonalise in about a third of the
+      // sweeps the block itself takes (Drmac & Veselic, "New fast and accurate Jacobi SVD
+      // algorithm", SIAM J. Matrix Anal. Appl. 29 (2008), with the pivoting of their QR replaced by
+      // the one sort).  The factors of X give those of A: A P = (Q J) S (U_x)^T with X J = U_x S.
+      // Rank r owns the factored columns [q0, q1) (and so the rows [q0, q1) of X, which are its
+      // rows of the sweeps).
+      const bool precond = ranks > 1 && k >= kQrMinCols;
+      double *qf = ws + lay.f, *qtau = ws + lay.tau, *qb = ws + lay.b;
+      int64_t *qorder = reinterpret_cast<int64_t *>(ws + lay.order);
+      const int64_t cpr = (k + ranks - 1) / ranks;
+      const int64_t q0 = min(k, static_cast<int64_t>(rank) * cpr), q1 = min(k, q0 + cpr);
+      if (precond)
+      {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+        // squared column norms in FP32 (the same on every rank) and the order they give
+        float *cn = reinterpret_cast<float *>(partial_raw);
+        for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
+        {
+          float sum = 0.0f;
+          for (int64_t i = 0; i < len; ++i)
+          {
+            const float x = static_cast<float>(entry_a(i, j));
+            sum = fmaf(x, x, sum);
+          }
+          cn[j] = sum;
+        }
+        __syncthreads();
+        for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
+        {
+          const float nj = cn[j];
+          int r = 0;
+          for (int64_t i = 0; i < k; ++i) r += (cn[i] > nj || (cn[i] == nj && i < j)) ? 1 : 0;
+          rank_of[r] = static_cast<int>(j);
+        }
+        __syncthreads();
+        // this rank's columns in shared memory while they are factored when they fit (else in the
+        // global factored matrix); each reflector goes to the global one as it is made
+        const bool qr_smem = (cpr + 1) * len * 8 <= kDynamicBytes;
+        double *own = reinterpret_cast<double *>(dynamic);
+        double *vst = qr_smem ? own + cpr * len : own;  // the reflector of the step, staged
+        const auto colp = [&](int64_t c) -> double * { return qr_smem ? own + (c - q0) * len : qf + c * len; };
+        for (int64_t c = q0; c < q1; ++c)
+        {
+          const int64_t from = rank_of[c];
+          double *to = colp(c);
+          for (int64_t i = threadIdx.x; i < len; i += blockDim.x) to[i] = entry_a(i, from);
+          if (threadIdx.x == 0) qorder[c] = from;
+        }
+        __syncthreads();
+        // step j: the owner of column j makes its reflector (as LAPACK's dlarfg: H = I - tau v v^T,
+        // v_0 = 1, R_jj = beta) and publishes it, the cluster waits for it, and every rank applies
+        // it to its own columns right of j, a warp per column, with v staged in shared memory
+        for (int64_t j = 0; j < k; ++j)
+        {
+          if (j >= q0 && j < q1)
+          {
+            double *col = colp(j);
+            double part = 0.0;
+            for (int64_t i = j + 1 + threadIdx.x; i < len; i += blockDim.x) part = fma(col[i], col[i], part);
+            part = warp_sum(part);
+            if (lane == 0) norms_raw[warp] = part;
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+              double xn = 0.0;
+              for (int w = 0; w < warps; ++w) xn += norms_raw[w];
+              const double alpha = col[j];
+              double beta = alpha, tau = 0.0, scale = 0.0;
+              if (xn > 0.0)
+              {
+                const double norm = sqrt(fma(alpha, alpha, xn));
+                const double d = alpha + copysign(norm, alpha);  // alpha - beta, without cancellation
+                beta = -copysign(norm, alpha);
+                tau = -d / beta;                                 // (beta - alpha) / beta
+                scale = 1.0 / d;
+              }
+              col[j] = beta;
+              qf[j * len + j] = beta;
+              qtau[j] = tau;
+              big = scale;
+            }
+            __syncthreads();
+            const double scale = big;
+            for (int64_t i = j + 1 + threadIdx.x; i < len; i += blockDim.x)
+            {
+              const double x = col[i] * scale;
+              col[i] = x;
+              qf[j * len + i] = x;
+            }
+          }
+          cluster.sync();
+          for (int64_t i = j + 1 + threadIdx.x; i < len; i += blockDim.x) vst[i] = __ldcg(qf + j * len + i);
+          __syncthreads();
+          const double tau = __ldcg(qtau + j);
+          if (tau != 0.0)
+            for (int64_t c = max(q0, j + 1) + warp; c < q1; c += warps)
+            {
+              double *fc = colp(c);
+              double dot = 0.0;
+              for (int64_t i = j + 1 + lane; i < len; i += 32) dot = fma(vst[i], fc[i], dot);
+              dot = warp_sum(dot);
+              const double w = tau * (fc[j] + dot);
+              for (int64_t i = j + 1 + lane; i < len; i += 32) fc[i] = fma(-w, vst[i], fc[i]);
+              if (lane == 0) fc[j] -= w;
+            }
+          __syncthreads();
+        }
+        // R's part of this rank's columns to the global factored matrix
+        if (qr_smem)
+          for (int64_t c = q0; c < q1; ++c)
+            for (int64_t i = threadIdx.x; i <= c && i < len; i += blockDim.x) qf[c * len + i] = colp(c)[i];
+        cluster.sync();
+      }
+      // rows of the swept matrix, and its entries: the block (W orientation) or X = R^T
+      const int64_t xl = precond ? k : len;
+      const auto entry = [&](int64_t row, int64_t col) -> double
+      { return precond ? (col <= row ? __ldcg(qf + row * len + col) : 0.0) : entry_a(row, col); };  // row < xl
 
       // 1. FP32 sweeps on the block scaled to |entries| <= 1, from V = I; V goes out in FP64.
       // Rank 0 alone when W and V fit in its shared memory, else rows dealt over the cluster.
       {
-        const bool alone = ranks == 1 || (k < 32 && (len * k + k * k) * 4 <= kDynamicBytes);
-        const int64_t rows = alone ? len : (len + ranks - 1) / ranks, vrows = alone ? k : (k + ranks - 1) / ranks;
-        const int64_t r0 = alone ? 0 : min(len, static_cast<int64_t>(rank) * rows), r1 = alone ? len : min(len, r0 + rows);
+        const bool alone = ranks == 1 || (k < 32 && (xl * k + k * k) * 4 <= kDynamicBytes);
+        const int64_t rows = alone ? xl : (xl + ranks - 1) / ranks, vrows = alone ? k : (k + ranks - 1) / ranks;
+        const int64_t r0 = alone ? 0 : min(xl, static_cast<int64_t>(rank) * rows), r1 = alone ? xl : min(xl, r0 + rows);
         const int64_t c0 = alone ? 0 : min(k, static_cast<int64_t>(rank) * vrows), c1 = alone ? k : min(k, c0 + vrows);
         const int64_t swap32 = exchange_bytes(k, alone ? 1 : ranks, 4);
         const bool in_smem = (rows + vrows) * k * 4 + swap32 <= kDynamicBytes;
@@ -599,9 +728,9 @@ namespace ttg
       // 3. this rank's rows of W = A V (FP64) and of V.  FP64 sweeps over the cluster for 32
       // columns or more, on rank 0 alone below that.
       const bool alone = ranks == 1 || k < 32;
-      const int64_t rows = alone ? (rank == 0 ? len : 0) : (len + ranks - 1) / ranks;
+      const int64_t rows = alone ? (rank == 0 ? xl : 0) : (xl + ranks - 1) / ranks;
       const int64_t vrows = alone ? (rank == 0 ? k : 0) : (k + ranks - 1) / ranks;
-      const int64_t r0 = alone ? 0 : min(len, static_cast<int64_t>(rank) * rows), r1 = min(len, r0 + rows);
+      const int64_t r0 = alone ? 0 : min(xl, static_cast<int64_t>(rank) * rows), r1 = min(xl, r0 + rows);
       const int64_t c0 = alone ? 0 : min(k, static_cast<int64_t>(rank) * vrows), c1 = min(k, c0 + vrows);
       const int64_t swap64 = exchange_bytes(k, alone ? 1 : ranks, 8);
       const bool slices_in_smem = (rows + vrows) * k * 8 + (swap64 > kStageBytes ? swap64 : kStageBytes) <= kDynamicBytes;
@@ -614,7 +743,7 @@ namespace ttg
         {
           const int64_t tr = tile % nr, tc = tile / nr;
           tile_product<double>(
-            k, [&](int64_t x, int i) { const int64_t row = r0 + tr * kTile + i; return row < r1 ? entry(row, x) : 0.0; }, !wide,
+            k, [&](int64_t x, int i) { const int64_t row = r0 + tr * kTile + i; return row < r1 ? entry(row, x) : 0.0; }, precond || !wide,
             [&](int64_t x, int j) { return tc * kTile + j < k ? __ldcg(vc + (tc * kTile + j) * k + x) : 0.0; }, true,
             stage, stage + kTile * (kTile + 1),
             [&](int i, int j, double sum) {
@@ -631,7 +760,7 @@ namespace ttg
       }
 
       // 4. FP64 sweeps
-      const double tol = 2.220446049250313e-16 * sqrt(static_cast<double>(len));
+      const double tol = 2.220446049250313e-16 * sqrt(static_cast<double>(xl));
       int sweeps_taken = 0;
       if (!alone || rank == 0)
         sweeps_taken = sweeps<double>(cluster, alone, w, rows, v, vrows, k, tol, norms_raw,
@@ -666,27 +795,139 @@ namespace ttg
         if (rank == 0) s[e.s_off + r] = sj;
       }
       __syncthreads();
-      // tall: U = W / sigma (m x k), Vh = V^T; wide: U = V (m x m), Vh = (W / sigma)^T
       double *uo = u + e.u_off, *vo = vh + e.vh_off;
-      for (int64_t i = threadIdx.x; i < rows * k; i += blockDim.x)
+      if (!precond)
       {
-        const int64_t j = i / rows, row = r0 + i % rows;
-        if (row >= r1) continue;
-        const double sj = norms[j];
-        const double x = sj > 0 ? w[i] / sj : 0.0;
-        if (wide)
-          vo[static_cast<int64_t>(rank_of[j]) * n + row] = x;
-        else
-          uo[row * k + rank_of[j]] = x;
+        // tall: U = W / sigma (m x k), Vh = V^T; wide: U = V (m x m), Vh = (W / sigma)^T
+        for (int64_t i = threadIdx.x; i < rows * k; i += blockDim.x)
+        {
+          const int64_t j = i / rows, row = r0 + i % rows;
+          if (row >= r1) continue;
+          const double sj = norms[j];
+          const double x = sj > 0 ? w[i] / sj : 0.0;
+          if (wide)
+            vo[static_cast<int64_t>(rank_of[j]) * n + row] = x;
+          else
+            uo[row * k + rank_of[j]] = x;
+        }
+        for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
+        {
+          const int64_t j = i / vrows, row = c0 + i % vrows;  // entry row of column j of V
+          if (row >= c1) continue;
+          if (wide)
+            uo[row * k + rank_of[j]] = v[i];
+          else
+            vo[static_cast<int64_t>(rank_of[j]) * n + row] = v[i];
+        }
       }
-      for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
+      else
       {
-        const int64_t j = i / vrows, row = c0 + i % vrows;  // entry row of column j of V
-        if (row >= c1) continue;
-        if (wide)
-          uo[row * k + rank_of[j]] = v[i];
+        // the right factor P (W / sigma): row `row` of W is row order[row] of it (tall: Vh is its
+        // transpose; wide: U is it)
+        for (int64_t i = threadIdx.x; i < rows * k; i += blockDim.x)
+        {
+          const int64_t j = i / rows, row = r0 + i % rows;
+          if (row >= r1) continue;
+          const double sj = norms[j];
+          const double x = sj > 0 ? w[i] / sj : 0.0;
+          const int64_t to = __ldcg(qorder + row);
+          if (wide)
+            uo[to * k + rank_of[j]] = x;
+          else
+            vo[static_cast<int64_t>(rank_of[j]) * n + to] = x;
+        }
+        // the left factor Q [J; 0], J = V: V's rows to the workspace (column-major), then each rank
+        // applies the reflectors, the last first, to its columns [q0, q1), a warp per column (tall:
+        // U is it; wide: Vh is its transpose)
+        for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
+        {
+          const int64_t j = i / vrows, row = c0 + i % vrows;
+          if (row < c1) g[j * k + row] = v[i];
+        }
+        cluster.sync();
+        // the reflectors pass through shared memory in batches, and this rank's columns of B stay
+        // there while they are transformed, when both fit (W and V there are no longer read)
+        constexpr int64_t kBatch = 16;
+        if (((cpr + kBatch) * len + kBatch) * 8 <= kDynamicBytes)
+        {
+          double *bcols = reinterpret_cast<double *>(dynamic), *stage = bcols + cpr * len, *stau = stage + kBatch * len;
+          for (int64_t i = threadIdx.x; i < (q1 - q0) * len; i += blockDim.x)
+          {
+            const int64_t c = q0 + i / len, r = i % len;
+            bcols[i] = r < k ? __ldcg(g + c * k + r) : 0.0;
+          }
+          for (int64_t top = k - 1; top >= 0; top -= kBatch)
+          {
+            const int64_t low = max(top - kBatch + 1, static_cast<int64_t>(0));  // reflectors top down to low
+            __syncthreads();
+            for (int64_t i = threadIdx.x; i < (top - low + 1) * len; i += blockDim.x)
+            {
+              const int64_t t = top - i / len, r = i % len;
+              stage[i] = r > t ? __ldcg(qf + t * len + r) : 0.0;
+            }
+            if (threadIdx.x < top - low + 1) stau[threadIdx.x] = __ldcg(qtau + top - threadIdx.x);
+            __syncthreads();
+            for (int64_t c = q0 + warp; c < q1; c += warps)
+            {
+              double *bc = bcols + (c - q0) * len;
+              for (int64_t t = top; t >= low; --t)
+              {
+                const double tau = stau[top - t];
+                if (tau == 0.0) continue;
+                const double *vt = stage + (top - t) * len;
+                double dot = 0.0;
+                for (int64_t i = t + 1 + lane; i < len; i += 32) dot = fma(vt[i], bc[i], dot);
+                dot = warp_sum(dot);
+                const double wt = tau * (bc[t] + dot);
+                for (int64_t i = t + 1 + lane; i < len; i += 32) bc[i] = fma(-wt, vt[i], bc[i]);
+                __syncwarp();
+                if (lane == 0) bc[t] -= wt;
+                __syncwarp();
+              }
+            }
+          }
+          __syncthreads();
+          for (int64_t i = threadIdx.x; i < (q1 - q0) * len; i += blockDim.x)
+          {
+            const int64_t c = q0 + i / len, r = i % len;
+            const int64_t to = rank_of[c];
+            if (wide)
+              vo[to * n + r] = bcols[i];
+            else
+              uo[r * k + to] = bcols[i];
+          }
+        }
         else
-          vo[static_cast<int64_t>(rank_of[j]) * n + row] = v[i];
+        {
+          for (int64_t c = q0 + warp; c < q1; c += warps)
+          {
+            double *bc = qb + c * len;
+            for (int64_t i = lane; i < len; i += 32) bc[i] = i < k ? __ldcg(g + c * k + i) : 0.0;
+            __syncwarp();
+            for (int64_t t = k - 1; t >= 0; --t)
+            {
+              const double tau = __ldcg(qtau + t);
+              if (tau == 0.0) continue;
+              const double *vt = qf + t * len;
+              double dot = 0.0;
+              for (int64_t i = t + 1 + lane; i < len; i += 32) dot = fma(__ldcg(vt + i), bc[i], dot);
+              dot = warp_sum(dot);
+              const double wt = tau * (bc[t] + dot);
+              for (int64_t i = t + 1 + lane; i < len; i += 32) bc[i] = fma(-wt, __ldcg(vt + i), bc[i]);
+              __syncwarp();
+              if (lane == 0) bc[t] -= wt;
+              __syncwarp();
+            }
+            const int64_t to = rank_of[c];
+            for (int64_t i = lane; i < len; i += 32)
+            {
+              if (wide)
+                vo[to * n + i] = bc[i];
+              else
+                uo[i * k + to] = bc[i];
+            }
+          }
+        }
       }
       if (threadIdx.x == 0 && rank == 0) info[block] = sweeps_taken;
       // no CTA leaves while another may still read its shared memory

@@ -132,6 +132,11 @@ def clear_plans() -> None:
     check(lib.tt_plan_cache_clear())
 
 
+def cached_plans() -> int:
+    '''How many compiled plans the cache holds.'''
+    return len(_plans)
+
+
 def _note_capture() -> None:
     global _captured
     _captured = True
