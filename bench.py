@@ -55,7 +55,8 @@ def parse():
     p.add_argument('--cpu-sample', type = int, default = 20, help = 'matvecs in the CPU baseline sample')
     p.add_argument('--dmrg-length', type = int, default = 64, help = 'chain of the DMRG sweep timing (0: skip)')
     p.add_argument('--dmrg-iter', type = int, default = 10, help = 'Lanczos steps per window in the DMRG timing')
-    p.add_argument('--dmrg-warm', type = int, default = 2, help = 'FP64 sweeps before the timed sweeps')
+    p.add_argument('--dmrg-warm', type = int, default = 4,
+                   help = 'FP64 sweeps before the timed sweeps (four bring every bond of the L = 64 chain to chi = 256)')
     p.add_argument('--workload', default = 'matvec', choices = ['matvec', 'svd', 'recoupling', 'windows'],
                    help = 'matvec: the headline line; svd: the truncating split of a two-site tensor; recoupling: '
                           'the SU(2) / Fibonacci einsum; windows: 64 batched matvecs in a CUDA graph')

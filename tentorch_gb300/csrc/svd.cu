@@ -301,6 +301,15 @@ namespace ttg
       // quadratically there, so the cosines it leaves are below ~tol and a further sweep (which
       // would find nothing above tol to rotate) is not run
       const T settled2 = static_cast<T>(tol);
+      // FP64 over a cluster: once a sweep has rotated under a quarter of the pairs, the next ones
+      // rotate only the pairs that need it, a warp per pair (the dense layout, a lane per pair,
+      // costs a whole rotation's FP64 instructions per warp as soon as one of its pairs rotates).
+      // The rotated pairs of a round are listed in `partial` (free during the rounds: the other
+      // ranks read it only at the sweep's start, before the first round's barrier); flags[2 + s % 2]
+      // counts the rotations of sweep s, flags[4] the listed pairs of a round.
+      constexpr bool kCanSparse = std::is_same_v<T, double>;
+      const int64_t all_pairs = k * (k - 1) / 2;
+      bool sparse = false;
       for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
       {
         for (int64_t j = warp; j < k; j += warps)
@@ -311,7 +320,11 @@ namespace ttg
           sum = warp_sum(sum);
           if (lane == 0) partial[j] = sum;
         }
-        if (threadIdx.x == 0) flags[sweep & 1] = 0;
+        if (threadIdx.x == 0)
+        {
+          flags[sweep & 1] = 0;
+          flags[2 + (sweep & 1)] = 0;
+        }
         sync();
         for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
         {
@@ -364,33 +377,90 @@ namespace ttg
           if (!alone)
           {
             cluster.sync();
-            for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
+            if (!(kCanSparse && sparse))
             {
-              const int64_t t = t0 + group;
-              int64_t p, q;
-              circle_pair(round, t, players, p, q);
-              const bool pair = t < pairs && q < k;
-              // lane gl adds ranks gl, gl + G, ...; the group's butterfly sum then gives every lane
-              // of every CTA the same value
-              T gamma = 0;
-              if (pair)
-                for (unsigned r = gl; r < ranks; r += G) gamma += share[static_cast<int64_t>(r) * pairs + t];
-              gamma = group_sum<T, G>(gamma);
-              if (!pair) continue;
-              const T alpha = norms[p], beta = norms[q];
-              if (gamma * gamma <= tol2 * alpha * beta) continue;
-              float cf, sf;
-              if (!angle(alpha, beta, gamma, cf, sf)) continue;
-              T c, sn;
-              exact_rotation(cf, sf, c, sn);
-              cols_rotate<T, G>(w + p * rows, w + q * rows, rows, gl, c, sn);
-              cols_rotate<T, G>(v + p * vrows, v + q * vrows, vrows, gl, c, sn);
-              if (gl == 0)
+              for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
               {
-                const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
-                norms[p] = cc * alpha - cs2 + ss * beta;
-                norms[q] = ss * alpha + cs2 + cc * beta;
-                if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
+                const int64_t t = t0 + group;
+                int64_t p, q;
+                circle_pair(round, t, players, p, q);
+                const bool pair = t < pairs && q < k;
+                // lane gl adds ranks gl, gl + G, ...; the group's butterfly sum then gives every lane
+                // of every CTA the same value
+                T gamma = 0;
+                if (pair)
+                  for (unsigned r = gl; r < ranks; r += G) gamma += share[static_cast<int64_t>(r) * pairs + t];
+                gamma = group_sum<T, G>(gamma);
+                if (!pair) continue;
+                const T alpha = norms[p], beta = norms[q];
+                if (gamma * gamma <= tol2 * alpha * beta) continue;
+                float cf, sf;
+                if (!angle(alpha, beta, gamma, cf, sf)) continue;
+                T c, sn;
+                exact_rotation(cf, sf, c, sn);
+                cols_rotate<T, G>(w + p * rows, w + q * rows, rows, gl, c, sn);
+                cols_rotate<T, G>(v + p * vrows, v + q * vrows, vrows, gl, c, sn);
+                if (gl == 0)
+                {
+                  const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
+                  norms[p] = cc * alpha - cs2 + ss * beta;
+                  norms[q] = ss * alpha + cs2 + cc * beta;
+                  if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
+                  atomicAdd(flags + 2 + (sweep & 1), 1);
+                }
+              }
+            }
+            else
+            {
+              // the pairs to rotate, listed, then a warp per listed pair (lanes over its rows of W
+              // and V); the same sums, tests and rotations as the dense layout
+              int *listed = reinterpret_cast<int *>(partial + pairs);
+              T *listed_gamma = partial;
+              if (threadIdx.x == 0) flags[4] = 0;
+              __syncthreads();
+              for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
+              {
+                const int64_t t = t0 + group;
+                int64_t p, q;
+                circle_pair(round, t, players, p, q);
+                const bool pair = t < pairs && q < k;
+                T gamma = 0;
+                if (pair)
+                  for (unsigned r = gl; r < ranks; r += G) gamma += share[static_cast<int64_t>(r) * pairs + t];
+                gamma = group_sum<T, G>(gamma);
+                if (!pair || gl != 0) continue;
+                if (gamma * gamma <= tol2 * norms[p] * norms[q]) continue;
+                const int at = atomicAdd(flags + 4, 1);
+                listed[at] = static_cast<int>(t);
+                listed_gamma[at] = gamma;
+              }
+              __syncthreads();
+              const int n_listed = flags[4];
+              for (int at = warp; at < n_listed; at += warps)
+              {
+                int64_t p, q;
+                circle_pair(round, listed[at], players, p, q);
+                const T gamma = listed_gamma[at], alpha = norms[p], beta = norms[q];
+                float cf, sf;
+                if (!angle(alpha, beta, gamma, cf, sf)) continue;
+                T c, sn;
+                exact_rotation(cf, sf, c, sn);
+                for (int64_t i = lane; i < rows + vrows; i += 32)
+                {
+                  T *x = i < rows ? w + p * rows + i : v + p * vrows + (i - rows);
+                  T *y = i < rows ? w + q * rows + i : v + q * vrows + (i - rows);
+                  const T a = *x, b = *y;
+                  *x = fma(c, a, -sn * b);
+                  *y = fma(sn, a, c * b);
+                }
+                if (lane == 0)
+                {
+                  const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
+                  norms[p] = cc * alpha - cs2 + ss * beta;
+                  norms[q] = ss * alpha + cs2 + cc * beta;
+                  if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
+                  atomicAdd(flags + 2 + (sweep & 1), 1);
+                }
               }
             }
           }
@@ -399,6 +469,7 @@ namespace ttg
         sync();
         const int any = alone ? flags[sweep & 1] : cluster.map_shared_rank(flags, 0)[sweep & 1];
         if (!any) return sweep + 1;
+        if constexpr (kCanSparse) sparse = !alone && static_cast<int64_t>(flags[2 + (sweep & 1)]) * 4 < all_pairs;
       }
       return -1;
     }
@@ -468,7 +539,7 @@ namespace ttg
       __shared__ double norms_raw[kMaxCols];
       __shared__ double partial_raw[kMaxCols];
       __shared__ int rank_of[kMaxCols];
-      __shared__ int flags[2];
+      __shared__ int flags[5];
       __shared__ double big;
       const cg::cluster_group cluster = cg::this_cluster();
       const unsigned ranks = cluster.num_blocks(), rank = cluster.block_rank();
