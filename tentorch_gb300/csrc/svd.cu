@@ -284,7 +284,7 @@ namespace ttg
     // recomputed at each sweep's start and carried with each rotation's exact update.
     template <typename T, int G>
     __device__ int sweeps(const cg::cluster_group &cluster, bool alone, T *w, int64_t rows, T *v, int64_t vrows, int64_t k,
-                          double tol, T *norms, T *exchange, T *partial, int *flags)
+                          double tol, T *norms, T *exchange, T *partial, int *flags, int *list)
     {
       const unsigned ranks = alone ? 1u : cluster.num_blocks(), me = alone ? 0u : cluster.block_rank();
       const auto sync = [&] {
@@ -301,15 +301,13 @@ namespace ttg
       // quadratically there, so the cosines it leaves are below ~tol and a further sweep (which
       // would find nothing above tol to rotate) is not run
       const T settled2 = static_cast<T>(tol);
-      // FP64 over a cluster: once a sweep has rotated under a quarter of the pairs, the next ones
-      // rotate only the pairs that need it, a warp per pair (the dense layout, a lane per pair,
-      // costs a whole rotation's FP64 instructions per warp as soon as one of its pairs rotates).
-      // The rotated pairs of a round are listed in `partial` (free during the rounds: the other
-      // ranks read it only at the sweep's start, before the first round's barrier); flags[2 + s % 2]
-      // counts the rotations of sweep s, flags[4] the listed pairs of a round.
-      constexpr bool kCanSparse = std::is_same_v<T, double>;
-      const int64_t all_pairs = k * (k - 1) / 2;
-      bool sparse = false;
+      // FP64 over a cluster: after the barrier a group of lanes per pair finds the rotation (the
+      // scalar part) and lists it, then the whole CTA rotates the listed pairs' entries, so that
+      // the FP64 instructions of the rotations spread over every warp instead of the few that hold
+      // the pairs (FP64 issue is the bound of a round).  The rotations of a round are listed in
+      // `list` and `partial` (free during the rounds: the other ranks read `partial` only at the
+      // sweep's start, before the first round's barrier); flags[4] counts them.
+      constexpr bool kSpread = std::is_same_v<T, double>;
       for (int sweep = 0; sweep < kMaxSweeps; ++sweep)
       {
         for (int64_t j = warp; j < k; j += warps)
@@ -320,11 +318,7 @@ namespace ttg
           sum = warp_sum(sum);
           if (lane == 0) partial[j] = sum;
         }
-        if (threadIdx.x == 0)
-        {
-          flags[sweep & 1] = 0;
-          flags[2 + (sweep & 1)] = 0;
-        }
+        if (threadIdx.x == 0) flags[sweep & 1] = 0;
         sync();
         for (int64_t j = threadIdx.x; j < k; j += blockDim.x)
         {
@@ -377,7 +371,54 @@ namespace ttg
           if (!alone)
           {
             cluster.sync();
-            if (!(kCanSparse && sparse))
+            if constexpr (kSpread)
+            {
+              T *lc = partial, *ls = partial + pairs;
+              if (threadIdx.x == 0) flags[4] = 0;
+              __syncthreads();
+              for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
+              {
+                const int64_t t = t0 + group;
+                int64_t p, q;
+                circle_pair(round, t, players, p, q);
+                const bool pair = t < pairs && q < k;
+                T gamma = 0;
+                if (pair)
+                  for (unsigned r = gl; r < ranks; r += G) gamma += share[static_cast<int64_t>(r) * pairs + t];
+                gamma = group_sum<T, G>(gamma);
+                if (!pair || gl != 0) continue;
+                const T alpha = norms[p], beta = norms[q];
+                if (gamma * gamma <= tol2 * alpha * beta) continue;
+                float cf, sf;
+                if (!angle(alpha, beta, gamma, cf, sf)) continue;
+                T c, sn;
+                exact_rotation(cf, sf, c, sn);
+                const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
+                norms[p] = cc * alpha - cs2 + ss * beta;
+                norms[q] = ss * alpha + cs2 + cc * beta;
+                if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
+                const int at = atomicAdd(flags + 4, 1);
+                list[at] = static_cast<int>(t);
+                lc[at] = c;
+                ls[at] = sn;
+              }
+              __syncthreads();
+              // entry i of a listed pair: row i of W (i < rows), else row i - rows of V
+              const int span = static_cast<int>(rows + vrows), items = flags[4] * span;
+              for (int it = threadIdx.x; it < items; it += blockDim.x)
+              {
+                const int at = it / span, i = it - at * span;
+                int64_t p, q;
+                circle_pair(round, list[at], players, p, q);
+                const T c = lc[at], sn = ls[at];
+                T *x = i < rows ? w + p * rows + i : v + p * vrows + (i - rows);
+                T *y = i < rows ? w + q * rows + i : v + q * vrows + (i - rows);
+                const T a = *x, b = *y;
+                *x = fma(c, a, -sn * b);
+                *y = fma(sn, a, c * b);
+              }
+            }
+            else
             {
               for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
               {
@@ -406,60 +447,6 @@ namespace ttg
                   norms[p] = cc * alpha - cs2 + ss * beta;
                   norms[q] = ss * alpha + cs2 + cc * beta;
                   if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
-                  atomicAdd(flags + 2 + (sweep & 1), 1);
-                }
-              }
-            }
-            else
-            {
-              // the pairs to rotate, listed, then a warp per listed pair (lanes over its rows of W
-              // and V); the same sums, tests and rotations as the dense layout
-              int *listed = reinterpret_cast<int *>(partial + pairs);
-              T *listed_gamma = partial;
-              if (threadIdx.x == 0) flags[4] = 0;
-              __syncthreads();
-              for (int64_t t0 = static_cast<int64_t>(warp) * per_warp; t0 < pairs; t0 += static_cast<int64_t>(warps) * per_warp)
-              {
-                const int64_t t = t0 + group;
-                int64_t p, q;
-                circle_pair(round, t, players, p, q);
-                const bool pair = t < pairs && q < k;
-                T gamma = 0;
-                if (pair)
-                  for (unsigned r = gl; r < ranks; r += G) gamma += share[static_cast<int64_t>(r) * pairs + t];
-                gamma = group_sum<T, G>(gamma);
-                if (!pair || gl != 0) continue;
-                if (gamma * gamma <= tol2 * norms[p] * norms[q]) continue;
-                const int at = atomicAdd(flags + 4, 1);
-                listed[at] = static_cast<int>(t);
-                listed_gamma[at] = gamma;
-              }
-              __syncthreads();
-              const int n_listed = flags[4];
-              for (int at = warp; at < n_listed; at += warps)
-              {
-                int64_t p, q;
-                circle_pair(round, listed[at], players, p, q);
-                const T gamma = listed_gamma[at], alpha = norms[p], beta = norms[q];
-                float cf, sf;
-                if (!angle(alpha, beta, gamma, cf, sf)) continue;
-                T c, sn;
-                exact_rotation(cf, sf, c, sn);
-                for (int64_t i = lane; i < rows + vrows; i += 32)
-                {
-                  T *x = i < rows ? w + p * rows + i : v + p * vrows + (i - rows);
-                  T *y = i < rows ? w + q * rows + i : v + q * vrows + (i - rows);
-                  const T a = *x, b = *y;
-                  *x = fma(c, a, -sn * b);
-                  *y = fma(sn, a, c * b);
-                }
-                if (lane == 0)
-                {
-                  const T cc = c * c, ss = sn * sn, cs2 = 2 * c * sn * gamma;
-                  norms[p] = cc * alpha - cs2 + ss * beta;
-                  norms[q] = ss * alpha + cs2 + cc * beta;
-                  if (gamma * gamma > settled2 * alpha * beta) flags[sweep & 1] = 1;
-                  atomicAdd(flags + 2 + (sweep & 1), 1);
                 }
               }
             }
@@ -469,25 +456,24 @@ namespace ttg
         sync();
         const int any = alone ? flags[sweep & 1] : cluster.map_shared_rank(flags, 0)[sweep & 1];
         if (!any) return sweep + 1;
-        if constexpr (kCanSparse) sparse = !alone && static_cast<int64_t>(flags[2 + (sweep & 1)]) * 4 < all_pairs;
       }
       return -1;
     }
 
     template <typename T>
     __device__ int sweeps(const cg::cluster_group &cluster, bool alone, T *w, int64_t rows, T *v, int64_t vrows, int64_t k,
-                          double tol, T *norms, T *exchange, T *partial, int *flags)
+                          double tol, T *norms, T *exchange, T *partial, int *flags, int *list)
     {
       const int64_t most = rows > vrows ? rows : vrows;
       // the fewest lanes per pair that hold its rows in registers (measured faster than more lanes
       // with shorter chains, in FP32 as in FP64, where the per-pair scalar work also runs once per
       // lane of the group on the narrow FP64 pipe)
-      if (most <= kNper) return sweeps<T, 1>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
-      if (most <= 2 * kNper) return sweeps<T, 2>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
-      if (most <= 4 * kNper) return sweeps<T, 4>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
-      if (most <= 8 * kNper) return sweeps<T, 8>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
-      if (most <= 16 * kNper) return sweeps<T, 16>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
-      return sweeps<T, 32>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags);
+      if (most <= kNper) return sweeps<T, 1>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags, list);
+      if (most <= 2 * kNper) return sweeps<T, 2>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags, list);
+      if (most <= 4 * kNper) return sweeps<T, 4>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags, list);
+      if (most <= 8 * kNper) return sweeps<T, 8>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags, list);
+      if (most <= 16 * kNper) return sweeps<T, 16>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags, list);
+      return sweeps<T, 32>(cluster, alone, w, rows, v, vrows, k, tol, norms, exchange, partial, flags, list);
     }
 
     // out(i, j) = sum_x a(x, i) b(x, j) + c(i, j) over a kTile x kTile tile, x < depth, staged
@@ -735,7 +721,7 @@ namespace ttg
         {
           sweeps<float>(cluster, alone, w32, rows, v32, vrows, k, 1e-5, reinterpret_cast<float *>(norms_raw),
                         reinterpret_cast<float *>(dynamic + kDynamicBytes - swap32), reinterpret_cast<float *>(partial_raw),
-                        flags);
+                        flags, rank_of);
           for (int64_t i = threadIdx.x; i < vrows * k; i += blockDim.x)
           {
             const int64_t row = c0 + i % vrows;
@@ -835,7 +821,7 @@ namespace ttg
       int sweeps_taken = 0;
       if (!alone || rank == 0)
         sweeps_taken = sweeps<double>(cluster, alone, w, rows, v, vrows, k, tol, norms_raw,
-                                      reinterpret_cast<double *>(dynamic + kDynamicBytes - swap64), partial_raw, flags);
+                                      reinterpret_cast<double *>(dynamic + kDynamicBytes - swap64), partial_raw, flags, rank_of);
 
       // singular values (column norms over the cluster), their ranks, and this rank's rows of the
       // factors in descending order
