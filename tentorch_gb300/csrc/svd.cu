@@ -11,6 +11,8 @@
 //
 // FP64 on this GPU runs at about 1/64 of the FP32 rate (about two FP64 multiply-adds per clock
 // per SM), so the sweeps are mixed precision and the FP64 part is spread over several SMs:
+//   0. (blocks of 32 columns or more) the columns sorted by norm and factored A P = Q R; steps 1-4
+//      then work on the graded X = R^T, and U = Q J at the end (Drmac & Veselic 2008).
 //   1. FP32 sweeps on a scaled copy of the block until its columns are orthogonal to ~1e-5; they
 //      give a rotation V32 close to the right singular vectors.
 //   2. V = V32 in FP64, made orthonormal to FP64 precision by two Newton-Schulz steps
