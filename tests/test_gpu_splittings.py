@@ -77,6 +77,39 @@ def test_a_spectrum_over_twelve_decades_agrees_with_lapack():
     assert torch.max(torch.abs(values.cpu() - sigma)).item() < 1e-14
 
 
+def test_rank_deficient_and_zero_blocks_through_the_preconditioned_path():
+    """Blocks of 32 columns or more are sorted and QR-factored before the sweeps: a tall and a wide
+    block of rank 12 (the split pairs the bond sectors of q and -q, so the two keep as many values)
+    and an all-zero block (40 columns each) give LAPACK's values, factors that multiply back to the
+    tensor, and singular vectors orthonormal wherever their value is not zero."""
+    t = _tensor({-1: 48, 0: 40, 1: 40}, {-1: 40, 0: 40, 1: 48}, seed = 4)
+    gen = torch.Generator().manual_seed(5)
+    for block in _blocks(t).values():
+        if block.shape == (40, 40):
+            block.zero_()
+        else:
+            m, n = block.shape
+            block.copy_(torch.randn(m, 12, dtype = torch.float64, generator = gen) @
+                        torch.randn(12, n, dtype = torch.float64, generator = gen))
+    # values below 1e-10 of the largest (the zero block's and the rank-12 block's round-off) are cut
+    first, values, second = tg.svd(t, None, 1e-10)
+    with tg.precision(la.PER_BLOCK):
+        _, values_ref, _ = tg.svd(t, None, 1e-10)
+    torch.cuda.synchronize()
+    big = torch.max(torch.abs(values_ref)).item()
+    assert values.shape == values_ref.shape
+    assert torch.max(torch.abs(values - values_ref)).item() < 1e-13 * big
+    scaled, _, rest = tg.svd(t, None, 1e-10, 1)
+    product = tg.contract(scaled, rest, [1], [0])
+    assert torch.max(torch.abs(product.data - t.data)).item() < 1e-12 * torch.max(torch.abs(t.data)).item()
+    for factor, columns in ((first, True), (second, False)):
+        for key, f in _blocks(factor).items():
+            g = f.T @ f if columns else f @ f.T
+            d = torch.diagonal(g)
+            assert torch.all((torch.abs(d - 1) < 1e-13) | (torch.abs(d) < 1e-13))
+            assert torch.max(torch.abs(g - torch.diag(d))).item() < 1e-13
+
+
 @pytest.mark.parametrize('absorb', [0, 1, 2, 3])
 def test_truncating_split_matches_the_per_block_form(absorb):
     rows = {-2: 20, 0: 40, 2: 20}
