@@ -178,8 +178,9 @@ int32_t tt_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const 
 /* ---- truncating splittings (tentorch/linalg/graded/svd.cpp:41-177) -------------------------- */
 
 /* Thin SVDs of `count` float64 blocks in one launch (one-sided Jacobi, mixed precision: FP32 sweeps,
- * then FP64 re-orthonormalisation and FP64 sweeps to full accuracy; a thread-block cluster per
- * block; replaces the per-block at::linalg_svd of svd.cpp:57-62).  `table` is a DEVICE array of 7
+ * then FP64 re-orthonormalisation and FP64 sweeps to full accuracy; blocks of 32 columns or more
+ * sorted by column norm and QR-factored first, the sweeps then working on R^T; a thread-block
+ * cluster per block; replaces the per-block at::linalg_svd of svd.cpp:57-62).  `table` is a DEVICE array of 7
  * int64 per block: a_off, rows, cols, u_off, s_off, vh_off, ws_off (offsets in doubles), best
  * ordered largest block first; `largest` is the largest min(rows, cols) among them (it sets the
  * cluster size).  Block i is rows x cols row-major at a + a_off; with k = min(rows, cols) <= 1024
