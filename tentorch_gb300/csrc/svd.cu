@@ -527,7 +527,7 @@ namespace ttg
       __shared__ double norms_raw[kMaxCols];
       __shared__ double partial_raw[kMaxCols];
       __shared__ int rank_of[kMaxCols];
-      __shared__ int flags[5];
+      __shared__ int flags[5];  // [0], [1]: a sweep rotated above sqrt(tol), by sweep parity; [4]: the rotations listed in a round
       __shared__ double big;
       const cg::cluster_group cluster = cg::this_cluster();
       const unsigned ranks = cluster.num_blocks(), rank = cluster.block_rank();
