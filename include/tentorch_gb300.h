@@ -110,8 +110,9 @@ int32_t tt_plan_cache_clear(void);
 /* The output space, workspace elements, GEMM flops, recoupled elements and op count of a plan. */
 int32_t tt_plan_info(const tt_plan *plan, int32_t *out_space, int64_t *workspace, double *gemm_flops,
                      int64_t *moved_elements, int32_t *n_ops);
-/* A text listing of the plan's operations and GEMM block shapes (m, n, K per pair), for diagnosis;
- * writes at most cap-1 characters and a terminating zero, *length the full size. */
+/* A text listing of the plan's operations and GEMM block shapes (m, n, K per pair), and for an
+ * einsum the order it folds its operands in (einsum.cpp:216-301), for diagnosis; writes at most
+ * cap-1 characters and a terminating zero, *length the full size. */
 int32_t tt_plan_describe(const tt_plan *plan, int64_t cap, char *text, int64_t *length);
 /* The gather index of operation `op` when it is a gather or a tiles pass (a composed chain of leg
  * moves whose F and R symbols are all 1; tiles are expanded entry by entry): output entry i reads

@@ -406,6 +406,12 @@ extern "C"
       const ttg::Program &p = *plan->program;
       static const char *kinds[] = {"zero", "gather", "runs", "gemm", "add", "copy", "tiles"};
       std::string out;
+      if (!p.fold.empty())
+      {
+        out += "fold order";
+        for (const int32_t o : p.fold) out += " " + std::to_string(o);
+        out += "\n";
+      }
       for (size_t i = 0; i < p.ops.size(); ++i)
       {
         const ttg::Op &op = p.ops[i];
@@ -708,6 +714,8 @@ extern "C"
                   double *out, void *stream)
   {
     if (count <= 0) return TT_OK;
+    if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128)
+      return fail(TT_EINVAL, "unknown dtype " + std::to_string(dtype));
     const bool complex = dtype == TT_DTYPE_COMPLEX128;
     const cudaError_t e = ttg::arena_dots(reinterpret_cast<const double *const *>(as), count,
                                           static_cast<const double *>(b), n * (complex ? 2 : 1), complex, scratch, out,

@@ -675,335 +675,342 @@ namespace ttg
   // ------------------------------------------------------------------------------------------
   // per-step plans
   // ------------------------------------------------------------------------------------------
+  //
+  // One step of a leg move regroups the entries of one block of its `before` space into blocks of
+  // its `after` space.  Its plan is, per target block, a list of pieces {first, last, from_step,
+  // to_step, run, c}: target[last + i * to_step] += c * source[first + i * from_step] for i < run
+  // (the reference's Piece / Shift of tentorch/tensors/regroup.h:22-60; the set of pieces of every
+  // shift is the same as the reference's, checked piece by piece).  Both kinds of step touch one or
+  // two vertices of a tree: each source tree is mapped to the trees it recouples into by building
+  // those trees directly and looking them up in the target layout.
 
   namespace
   {
-    // tentorch/tensors/regroup.cpp:16-22
-    Sector chain_at(const Category &cat, const Tree &tree, int64_t last)
+    // The charge the first n legs of a tree fuse to: trivial for no leg, the first sector for one,
+    // the root for all of them, else the inner charge after leg n - 1.
+    Sector fused_through(const Category &cat, const Tree &tree, int32_t n)
     {
-      if (last < 0) return cat.trivial();
-      if (last + 1 == static_cast<int64_t>(tree.sectors.size())) return tree.coupled;
-      if (last == 0) return tree.sectors[0];
-      return tree.inner[static_cast<size_t>(last - 1)];
+      const int32_t legs = static_cast<int32_t>(tree.sectors.size());
+      if (n <= 0) return cat.trivial();
+      if (n >= legs) return tree.coupled;
+      if (n == 1) return tree.sectors[0];
+      return tree.inner[static_cast<size_t>(n - 2)];
     }
 
-    void push_sector(std::vector<int64_t> &out, const Sector &s)
+    // The multiplicity index of the vertex at which leg v (v >= 1) joins the legs before it; leg 0
+    // joins nothing and reads 0.
+    int32_t joining_copy(const Tree &tree, int32_t v) { return v >= 1 ? tree.copies[static_cast<size_t>(v - 1)] : 0; }
+
+    int32_t find_index(const std::vector<FIndex> &list, const Sector &sector, int32_t inner, int32_t outer)
     {
-      for (int32_t i = 0; i < s.size; ++i) out.push_back(s[i]);
+      for (size_t i = 0; i < list.size(); ++i)
+        if (list[i].sector == sector && list[i].inner == inner && list[i].outer == outer) return static_cast<int32_t>(i);
+      return -1;
     }
+
+    // A recoupling coefficient this small is a cancellation that should have been zero: the
+    // entries of F, R and their products are of order one.
+    constexpr double kNegligible = 1e-13;
+
+    // The exchange of two adjacent legs b, c between the charges y (of the legs before them) and d
+    // (of the legs through them), as a matrix from the local bracketings before the exchange (the
+    // rows of F^d_{y b c}: inner charge e, the copies of y x b -> e and e x c -> d) to those after
+    // it (the rows of F^d_{y c b}):  Q = F_{ycb} . B . F_{ybc}^dagger, where B carries the braiding
+    // R_{bc} between the right bracketings (f, copy of b x c -> f, copy of y x f -> d) that share f
+    // and the outer copy.
+    Matrix exchange_matrix(const Category &cat, const Sector &y, const Sector &b, const Sector &c, const Sector &d)
+    {
+      const Matrix &before = cat.F(y, b, c, d);
+      const Matrix &after = cat.F(y, c, b, d);
+      const std::vector<FIndex> right_before = cat.f_columns(y, b, c, d);
+      const std::vector<FIndex> right_after = cat.f_columns(y, c, b, d);
+      const Matrix &braid = cat.R(b, c);
+      // the row (or column) of the braiding that a fusion channel (f, copy) of b and c takes
+      std::vector<std::pair<Sector, int32_t>> channel_start;
+      int32_t start = 0;
+      for (const Outcome &o : cat.outcomes(b, c))
+      {
+        channel_start.emplace_back(o.sector, start);
+        start += o.multiplicity;
+      }
+      const auto channel = [&](const FIndex &index)
+      {
+        for (const auto &entry : channel_start)
+          if (entry.first == index.sector) return entry.second + index.inner;
+        return -1;
+      };
+      // middle[i][j]: from right bracketing j before the exchange to i after it
+      const int32_t ni = static_cast<int32_t>(right_after.size()), nj = static_cast<int32_t>(right_before.size());
+      std::vector<cplx> middle(static_cast<size_t>(ni) * nj, cplx(0.0, 0.0));
+      for (int32_t i = 0; i < ni; ++i)
+        for (int32_t j = 0; j < nj; ++j)
+        {
+          if (right_after[static_cast<size_t>(i)].sector != right_before[static_cast<size_t>(j)].sector ||
+              right_after[static_cast<size_t>(i)].outer != right_before[static_cast<size_t>(j)].outer)
+            continue;
+          const int32_t row = channel(right_after[static_cast<size_t>(i)]), col = channel(right_before[static_cast<size_t>(j)]);
+          if (row >= 0 && col >= 0) middle[static_cast<size_t>(i) * nj + j] = braid.at(row, col);
+        }
+      // carried[i][s] = sum_j middle[i][j] conj(before[s][j]), then Q[t][s] = sum_i after[t][i] carried[i][s]
+      std::vector<cplx> carried(static_cast<size_t>(ni) * before.rows, cplx(0.0, 0.0));
+      for (int32_t i = 0; i < ni; ++i)
+        for (int32_t s = 0; s < before.rows; ++s)
+        {
+          cplx sum(0.0, 0.0);
+          for (int32_t j = 0; j < nj; ++j)
+          {
+            const cplx m = middle[static_cast<size_t>(i) * nj + j];
+            if (m != cplx(0.0, 0.0)) sum += m * std::conj(before.at(s, j));
+          }
+          carried[static_cast<size_t>(i) * before.rows + s] = sum;
+        }
+      Matrix q;
+      q.rows = after.rows;
+      q.cols = before.rows;
+      q.v.assign(static_cast<size_t>(q.rows) * q.cols, cplx(0.0, 0.0));
+      for (int32_t t = 0; t < q.rows; ++t)
+        for (int32_t s = 0; s < q.cols; ++s)
+        {
+          cplx sum(0.0, 0.0);
+          for (int32_t i = 0; i < ni; ++i) sum += after.at(t, i) * carried[static_cast<size_t>(i) * before.rows + s];
+          q.v[static_cast<size_t>(t) * q.cols + s] = sum;
+        }
+      return q;
+    }
+
+    // Shifts kept by their target block while a bend builds them, handed out in key order.
+    struct ShiftsByTarget
+    {
+      BlockKey source;
+      std::map<BlockKey, Shift> held;
+      std::vector<Piece> &into(const BlockKey &to, int64_t rows, int64_t cols)
+      {
+        auto it = held.find(to);
+        if (it == held.end()) it = held.emplace(to, Shift{source, to, rows, cols, {}}).first;
+        return it->second.pieces;
+      }
+      std::vector<Shift> take()
+      {
+        std::vector<Shift> out;
+        out.reserve(held.size());
+        for (auto &entry : held) out.push_back(std::move(entry.second));
+        return out;
+      }
+    };
   } // namespace
 
-  // tentorch/tensors/regroup.cpp:25-258: the trees that agree outside the pair recouple by
-  // F^d_{ycb} R_{bc} (F^d_{ybc})^dagger; classes of equal multiplicity shape move as digit
-  // permutations of the width index, coalesced into runs.
+  // Exchange of the codomain legs p and p + 1 of one block (the step of
+  // tentorch/tensors/regroup.cpp:25-258).  A tree (legs a_0 .. a_n-1) changes only at the two
+  // vertices where a_p and a_p+1 join; its images are the trees of the exchanged legs that agree
+  // with it everywhere else, one per local bracketing after the exchange, with the coefficient of
+  // exchange_matrix.  Entries keep their place in the row but for the two legs' copy digits, which
+  // trade places: when either leg carries a single copy the whole tree moves as one run, otherwise
+  // in runs over the copies of the legs after the pair.
   std::vector<Shift> exchange_plan(const Category &cat, const std::vector<Leg> &codomain,
                                    const std::vector<Leg> &domain, const BlockKey &key, const Sector &qtotal,
                                    int32_t p)
   {
     (void)qtotal;
-    const int32_t count = static_cast<int32_t>(codomain.size());
-    std::vector<Leg> exchanged = codomain;
-    std::swap(exchanged[static_cast<size_t>(p)], exchanged[static_cast<size_t>(p + 1)]);
-    const Layout &source = layout_of(cat, codomain, key.codomain);
-    const Layout &target = layout_of(cat, exchanged, key.codomain);
-    const int64_t stride = layout_of(cat, domain, key.domain).rows();
-    std::vector<Shift> plan;
-    plan.push_back(Shift{key, key, 0, 0, {}});
+    const int32_t legs = static_cast<int32_t>(codomain.size());
+    std::vector<Leg> swapped = codomain;
+    std::swap(swapped[static_cast<size_t>(p)], swapped[static_cast<size_t>(p + 1)]);
+    const Layout &before = layout_of(cat, codomain, key.codomain);
+    const Layout &after = layout_of(cat, swapped, key.codomain);
+    const int64_t row_length = layout_of(cat, domain, key.domain).rows();
+    Shift shift{key, key, 0, 0, {}};
+    std::map<std::array<Sector, 4>, Matrix> local;  // exchange_matrix per (y, b, c, d)
 
-    const auto signature = [&](const Tree &tree, bool exchanged_tree)
+    for (size_t s = 0; s < before.trees.size(); ++s)
     {
-      std::vector<int64_t> out;
-      for (int32_t axis = 0; axis < count; ++axis)
+      const Tree &tree = before.trees[s];
+      const Sector &b = tree.sectors[static_cast<size_t>(p)], &c = tree.sectors[static_cast<size_t>(p + 1)];
+      const Sector y = fused_through(cat, tree, p), d = fused_through(cat, tree, p + 2);
+      auto found = local.find({y, b, c, d});
+      if (found == local.end()) found = local.emplace(std::array<Sector, 4>{y, b, c, d}, exchange_matrix(cat, y, b, c, d)).first;
+      const Matrix &q = found->second;
+      const int32_t column = find_index(cat.f_rows(y, b, c, d), fused_through(cat, tree, p + 1), joining_copy(tree, p),
+                                        joining_copy(tree, p + 1));
+      if (column < 0) throw LogicError("a tree of the codomain is not a bracketing of its F symbol");
+      // the copies of the two legs, of the legs after them, and of the whole tree
+      const int64_t mb = codomain[static_cast<size_t>(p)]->multiplicity_of(b);
+      const int64_t mc = codomain[static_cast<size_t>(p + 1)]->multiplicity_of(c);
+      int64_t tail = 1, width = 1;
+      for (int32_t l = 0; l < legs; ++l)
       {
-        const int32_t from = exchanged_tree && (axis == p || axis == p + 1) ? (axis == p ? p + 1 : p) : axis;
-        push_sector(out, tree.sectors[static_cast<size_t>(from)]);
+        const int64_t m = codomain[static_cast<size_t>(l)]->multiplicity_of(tree.sectors[static_cast<size_t>(l)]);
+        width *= m;
+        if (l > p + 1) tail *= m;
       }
-      for (int32_t at = 0; at < static_cast<int32_t>(tree.inner.size()); ++at)
-        if (at != p - 1) push_sector(out, tree.inner[static_cast<size_t>(at)]);
-      for (int32_t at = 0; at < static_cast<int32_t>(tree.copies.size()); ++at)
-        if (at != p - 1 && at != p) out.push_back(tree.copies[static_cast<size_t>(at)]);
-      return out;
-    };
-    const auto moved = [p](int32_t axis) { return axis == p ? p + 1 : axis == p + 1 ? p : axis; };
-    const auto shape_of = [&](const Tree &tree, const std::vector<Leg> &legs)
-    {
-      std::vector<int64_t> out;
-      for (int32_t axis = 0; axis < count; ++axis)
-        out.push_back(legs[static_cast<size_t>(axis)]->multiplicity_of(tree.sectors[static_cast<size_t>(axis)]));
-      return out;
-    };
-
-    std::map<std::vector<int64_t>, std::vector<int32_t>> groups, partners;
-    for (size_t at = 0; at < source.trees.size(); ++at)
-      groups[signature(source.trees[at], false)].push_back(static_cast<int32_t>(at));
-    for (size_t at = 0; at < target.trees.size(); ++at)
-      partners[signature(target.trees[at], true)].push_back(static_cast<int32_t>(at));
-
-    std::map<std::pair<int32_t, int32_t>, cplx> factors;
-    for (const auto &[marks, olds] : groups)
-    {
-      const auto found = partners.find(marks);
-      if (found == partners.end()) throw LogicError("the exchange has no image for a tree of the codomain");
-      const std::vector<int32_t> &news = found->second;
-      const Tree &sample = source.trees[static_cast<size_t>(olds.front())];
-      const Sector y = chain_at(cat, sample, p - 1);
-      const Sector d = chain_at(cat, sample, p + 1);
-      const Sector &b = sample.sectors[static_cast<size_t>(p)];
-      const Sector &c = sample.sectors[static_cast<size_t>(p + 1)];
-      const Matrix &straight = cat.F(y, b, c, d);
-      const Matrix &braided = cat.F(y, c, b, d);
-      if (straight.rows != static_cast<int32_t>(olds.size()) || braided.rows != static_cast<int32_t>(news.size()))
-        throw LogicError("the exchange does not match the trees of the block");
-      std::vector<std::pair<Sector, int32_t>> offset;
-      int32_t at = 0;
-      for (const Outcome &o : cat.outcomes(b, c))
+      const std::vector<FIndex> images = cat.f_rows(y, c, b, d);
+      for (size_t r = 0; r < images.size(); ++r)
       {
-        offset.emplace_back(o.sector, at);
-        at += o.multiplicity;
-      }
-      const std::vector<FIndex> from = cat.f_columns(y, b, c, d);
-      const std::vector<FIndex> to = cat.f_columns(y, c, b, d);
-      const Matrix &braid = cat.R(b, c);
-      const auto braid_at = [&](const FIndex &index) -> int32_t
-      {
-        for (const auto &[sector, start] : offset)
-          if (sector == index.sector) return start + index.inner;
-        return -1;
-      };
-      struct Term
-      {
-        int32_t i, braid_row, braid_col, j;
-      };
-      std::vector<Term> terms;
-      for (size_t i = 0; i < to.size(); ++i)
-      {
-        const int32_t r = braid_at(to[i]);
-        if (r < 0) continue;
-        for (size_t j = 0; j < from.size(); ++j)
+        const cplx coefficient = q.at(static_cast<int32_t>(r), column);
+        if (std::abs(coefficient) <= kNegligible) continue;
+        // the image: legs p and p + 1 swapped, the local bracketing of row r
+        Tree image = tree;
+        std::swap(image.sectors[static_cast<size_t>(p)], image.sectors[static_cast<size_t>(p + 1)]);
+        if (p >= 1)
         {
-          const int32_t cc = braid_at(from[j]);
-          if (cc < 0) continue;
-          if (!(to[i].sector == from[j].sector) || to[i].outer != from[j].outer) continue;
-          terms.push_back({static_cast<int32_t>(i), r, cc, static_cast<int32_t>(j)});
+          // the charge after the first of the pair and the copy of its vertex (with no leg before
+          // the pair that charge is the first sector itself and the vertex has one copy)
+          image.inner[static_cast<size_t>(p - 1)] = images[r].sector;
+          image.copies[static_cast<size_t>(p - 1)] = images[r].inner;
         }
+        image.copies[static_cast<size_t>(p)] = images[r].outer;
+        const int32_t t = after.find(image);
+        if (t < 0) throw LogicError("the exchange has no image for a tree of the codomain");
+        const int64_t from = before.offsets[s], to = after.offsets[static_cast<size_t>(t)];
+        // source copy digits (high, beta, gamma, low) land at (high, gamma, beta, low): runs of
+        // `tail` entries, merged where the next one continues the last on both sides (always when
+        // either leg carries one copy, and across the step from one high digit to the next)
+        const size_t first_piece = shift.pieces.size();
+        const int64_t highs = width / (mb * mc * tail);
+        for (int64_t h = 0; h < highs; ++h)
+          for (int64_t beta = 0; beta < mb; ++beta)
+            for (int64_t gamma = 0; gamma < mc; ++gamma)
+            {
+              const int64_t src = (from + ((h * mb + beta) * mc + gamma) * tail) * row_length;
+              const int64_t dst = (to + ((h * mc + gamma) * mb + beta) * tail) * row_length;
+              if (shift.pieces.size() > first_piece)
+              {
+                Piece &last = shift.pieces.back();
+                if (last.first + last.run == src && last.last + last.run == dst)
+                {
+                  last.run += tail * row_length;
+                  continue;
+                }
+              }
+              shift.pieces.push_back(Piece{src, dst, 1, 1, tail * row_length, coefficient});
+            }
       }
-      for (size_t one = 0; one < news.size(); ++one)
-        for (size_t other = 0; other < olds.size(); ++other)
-        {
-          cplx value(0.0, 0.0);
-          for (const Term &t : terms)
-            value += braided.at(static_cast<int32_t>(one), t.i) * braid.at(t.braid_row, t.braid_col) *
-                     std::conj(straight.at(static_cast<int32_t>(other), t.j));
-          if (value.real() == 0.0 && value.imag() == 0.0) continue;
-          factors.emplace(std::make_pair(news[one], olds[other]), value);
-        }
     }
-
-    std::map<std::vector<int64_t>, std::vector<int32_t>> before_classes, after_classes;
-    std::vector<std::vector<int64_t>> after_shapes(target.trees.size());
-    for (size_t at = 0; at < source.trees.size(); ++at)
-      before_classes[shape_of(source.trees[at], codomain)].push_back(static_cast<int32_t>(at));
-    for (size_t at = 0; at < target.trees.size(); ++at)
-    {
-      const std::vector<int64_t> shape = shape_of(target.trees[at], exchanged);
-      std::vector<int64_t> back(shape.size(), 0);
-      for (int32_t axis = 0; axis < count; ++axis) back[static_cast<size_t>(moved(axis))] = shape[static_cast<size_t>(axis)];
-      after_shapes[at] = shape;
-      after_classes[back].push_back(static_cast<int32_t>(at));
-    }
-    std::vector<Piece> &pieces = plan.back().pieces;
-    std::vector<int64_t> width_of, digits(static_cast<size_t>(count)), placed(static_cast<size_t>(count));
-    for (const auto &[shape, olds] : before_classes)
-    {
-      const auto partner = after_classes.find(shape);
-      if (partner == after_classes.end()) throw LogicError("the exchange has no image for a block of trees");
-      const std::vector<int32_t> &news = partner->second;
-      int64_t width = 1;
-      for (int64_t f : shape) width *= f;
-      const std::vector<int64_t> &target_shape = after_shapes[static_cast<size_t>(news.front())];
-      width_of.assign(static_cast<size_t>(width), 0);
-      for (int64_t at = 0; at < width; ++at)
-      {
-        int64_t left = at;
-        for (int32_t axis = count - 1; axis >= 0; --axis)
-        {
-          digits[static_cast<size_t>(axis)] = left % shape[static_cast<size_t>(axis)];
-          left /= shape[static_cast<size_t>(axis)];
-        }
-        for (int32_t axis = 0; axis < count; ++axis) placed[static_cast<size_t>(moved(axis))] = digits[static_cast<size_t>(axis)];
-        int64_t index = 0;
-        for (int32_t axis = 0; axis < count; ++axis)
-          index = index * target_shape[static_cast<size_t>(axis)] + placed[static_cast<size_t>(axis)];
-        width_of[static_cast<size_t>(at)] = index;
-      }
-      for (const int32_t one : news)
-        for (const int32_t other : olds)
-        {
-          const auto factor = factors.find(std::make_pair(one, other));
-          if (factor == factors.end()) continue;
-          for (int64_t at = 0; at < width;)
-          {
-            int64_t run = 1;
-            while (at + run < width && width_of[static_cast<size_t>(at + run)] == width_of[static_cast<size_t>(at)] + run) ++run;
-            pieces.push_back(Piece{(source.offsets[static_cast<size_t>(other)] + at) * stride,
-                                   (target.offsets[static_cast<size_t>(one)] + width_of[static_cast<size_t>(at)]) * stride,
-                                   1, 1, run * stride, factor->second});
-            at += run;
-          }
-        }
-    }
-    return plan;
+    return {std::move(shift)};
   }
 
-  // tentorch/tensors/regroup.cpp:260-417: the giving side loses its last vertex, the taking side
-  // gains one, and F^q(first, middle, last) carries the copies of the bent leg across; the bent
-  // leg's sector reads as its dual on the other side.
+  // Bend of the last leg of one side onto the end of the other, for one block (the step of
+  // tentorch/tensors/regroup.cpp:260-417).  The giving tree loses the vertex where the leg joins it
+  // (charge x of its other legs, copy mu), the taking tree gains a vertex for the leg, which it
+  // reads as the dual sector.  With Q the total charge, the recoupling is one row (codomain to
+  // domain) or column (domain to codomain) of F^Q: for a leg q bent down from codomain root r onto
+  // domain root s, F^Q_{x q s-bar} at row (r, mu, block copy) gives per column (f, kappa, lambda)
+  // the new domain root f-bar, the new vertex's copy kappa and the block copy lambda; for a leg
+  // bent up from domain root s onto codomain root r, F^Q_{r q-bar x-bar} at column (s-bar, mu,
+  // block copy) gives per row (e, kappa, lambda) the new codomain root e.  The leg's copies are
+  // the fastest digit of the tree that gains it, so one piece carries the copies of the leg for
+  // one entry of the other legs (bent down), or one entry of the taking tree and one copy carry the
+  // whole kept tree (bent up).
   std::vector<Shift> bend_plan(const Category &cat, const std::vector<Leg> &codomain,
                                const std::vector<Leg> &domain, const BlockKey &key, const Sector &qtotal,
                                bool from_codomain)
   {
     const std::vector<Leg> &giving = from_codomain ? codomain : domain;
     const std::vector<Leg> &taking = from_codomain ? domain : codomain;
-    const Leg moved_leg = giving.back();
+    const Leg leg = giving.back();
     // The bent leg keeps its blocks and its sector reads as the dual one on the other side, so the
     // copies of a sector land in the rows of its dual: the two have to carry the same multiplets.
     // The reference assumes it (tentorch/linalg/graded/svd.cpp:97-100) and writes past its blocks
     // when it does not hold; here it is an error.
-    for (size_t b = 0; b < moved_leg->sectors.size(); ++b)
+    for (size_t b = 0; b < leg->sectors.size(); ++b)
     {
-      const Sector d = cat.dual(moved_leg->sectors[b]);
-      const auto it = std::lower_bound(moved_leg->sectors.begin(), moved_leg->sectors.end(), d);
-      if (it != moved_leg->sectors.end() && *it == d &&
-          moved_leg->mult[static_cast<size_t>(it - moved_leg->sectors.begin())] != moved_leg->mult[b])
+      const Sector d = cat.dual(leg->sectors[b]);
+      const auto it = std::lower_bound(leg->sectors.begin(), leg->sectors.end(), d);
+      if (it != leg->sectors.end() && *it == d && leg->mult[static_cast<size_t>(it - leg->sectors.begin())] != leg->mult[b])
         throw InvalidArgument("a leg bent across the tensor needs each sector and its dual to carry the same "
-                              "multiplets, but " + moved_leg->sectors[b].str() + " has " +
-                              std::to_string(moved_leg->mult[b]) + " and " + d.str() + " has " +
-                              std::to_string(moved_leg->mult[static_cast<size_t>(it - moved_leg->sectors.begin())]));
+                              "multiplets, but " + leg->sectors[b].str() + " has " + std::to_string(leg->mult[b]) +
+                              " and " + d.str() + " has " +
+                              std::to_string(leg->mult[static_cast<size_t>(it - leg->sectors.begin())]));
     }
-    const std::vector<Leg> kept_giving(giving.begin(), giving.end() - 1);
-    std::vector<Leg> kept_taking = taking;
-    kept_taking.push_back(moved_leg);
-    const std::vector<Leg> &out_codomain = from_codomain ? kept_giving : kept_taking;
-    const std::vector<Leg> &out_domain = from_codomain ? kept_taking : kept_giving;
-    const Layout &moved_side = layout_of(cat, from_codomain ? codomain : domain, from_codomain ? key.codomain : key.domain);
-    const Layout &gains_side = layout_of(cat, from_codomain ? domain : codomain, from_codomain ? key.domain : key.codomain);
-    const Sector moved_root = from_codomain ? key.codomain : key.domain;
-    const Sector gains_root = from_codomain ? key.domain : key.codomain;
-    const int64_t source_stride = (from_codomain ? gains_side : moved_side).rows();
+    std::vector<Leg> shorter(giving.begin(), giving.end() - 1), longer = taking;
+    longer.push_back(leg);
+    const std::vector<Leg> &new_codomain = from_codomain ? shorter : longer;
+    const std::vector<Leg> &new_domain = from_codomain ? longer : shorter;
+    const Sector &giving_root = from_codomain ? key.codomain : key.domain;
+    const Sector &taking_root = from_codomain ? key.domain : key.codomain;
+    const Layout &givers = layout_of(cat, giving, giving_root);
+    const Layout &takers = layout_of(cat, taking, taking_root);
+    const int64_t source_cols = (from_codomain ? takers : givers).rows();
+    ShiftsByTarget shifts{key, {}};
 
-    std::vector<Shift> plan;
-    std::map<BlockKey, size_t> at_of;
-    std::map<std::pair<Sector, Sector>, std::pair<const Layout *, const Layout *>> out_layouts;
-    const auto index_of = [&](const BlockKey &to, int64_t rows, int64_t cols) -> size_t
+    for (size_t g = 0; g < givers.trees.size(); ++g)
     {
-      const auto found = at_of.find(to);
-      if (found != at_of.end()) return found->second;
-      const size_t index = plan.size();
-      at_of.emplace(to, index);
-      plan.push_back(Shift{key, to, rows, cols, {}});
-      return index;
-    };
-
-    for (size_t gains_at = 0; gains_at < gains_side.trees.size(); ++gains_at)
-    {
-      const Tree &gains_tree = gains_side.trees[gains_at];
-      const int64_t gains = gains_side.offsets[gains_at + 1] - gains_side.offsets[gains_at];
-      for (size_t moved_at = 0; moved_at < moved_side.trees.size(); ++moved_at)
+      const Tree &tree = givers.trees[g];
+      const int32_t n = static_cast<int32_t>(tree.sectors.size());
+      const Sector q = tree.sectors.back();
+      const Sector x = fused_through(cat, tree, n - 1);
+      const int32_t mu = joining_copy(tree, n - 1);
+      const int64_t copies = leg->multiplicity_of(q);
+      const int64_t kept_width = (givers.offsets[g + 1] - givers.offsets[g]) / copies;
+      const Tree kept = trimmed(cat, tree);
+      // the F symbol of the bend, the index this tree names and the indices it may land on
+      const Sector a = from_codomain ? x : taking_root;
+      const Sector b = from_codomain ? q : cat.dual(q);
+      const Sector c = from_codomain ? cat.dual(taking_root) : cat.dual(x);
+      const Matrix &f = cat.F(a, b, c, qtotal);
+      const std::vector<FIndex> rows = cat.f_rows(a, b, c, qtotal), cols = cat.f_columns(a, b, c, qtotal);
+      const int32_t named = from_codomain ? find_index(rows, giving_root, mu, key.copy)
+                                          : find_index(cols, cat.dual(giving_root), mu, key.copy);
+      if (named < 0) continue;
+      const std::vector<FIndex> &landings = from_codomain ? cols : rows;
+      for (size_t l = 0; l < landings.size(); ++l)
       {
-        const Tree &moved_tree = moved_side.trees[moved_at];
-        const Sector charge = moved_tree.sectors.back();
-        const int64_t copies = moved_leg->multiplicity_of(charge);
-        const int64_t span = moved_side.offsets[moved_at + 1] - moved_side.offsets[moved_at];
-        const int64_t inside = span / copies;
-        const Tree kept_tree = trimmed(cat, moved_tree);
-        const Sector prefix = kept_tree.coupled;
-        const int32_t copy = moved_tree.sectors.size() >= 2 ? moved_tree.copies.back() : 0;
-        const Sector first = from_codomain ? prefix : gains_root;
-        const Sector middle = from_codomain ? charge : cat.dual(charge);
-        const Sector last = from_codomain ? cat.dual(gains_root) : cat.dual(prefix);
-        const Matrix &coefficients = cat.F(first, middle, last, qtotal);
-        const std::vector<FIndex> across = cat.f_rows(first, middle, last, qtotal);
-        const std::vector<FIndex> along = cat.f_columns(first, middle, last, qtotal);
-        const std::vector<FIndex> &named = from_codomain ? across : along;
-        const std::vector<FIndex> &free = from_codomain ? along : across;
-        const Sector named_root = from_codomain ? moved_root : cat.dual(moved_root);
-        std::vector<int32_t> taken;
-        for (size_t at = 0; at < named.size(); ++at)
-          if (named[at].sector == named_root && named[at].inner == copy && named[at].outer == key.copy)
-            taken.push_back(static_cast<int32_t>(at));
-        if (taken.empty()) continue;
-        const int64_t source_row = moved_side.offsets[moved_at];
-        const int64_t source_column = gains_side.offsets[gains_at];
-        for (const int32_t index : taken)
-          for (size_t column = 0; column < free.size(); ++column)
-          {
-            const FIndex &taken_side = free[column];
-            // entry [index * width + column] of the row-major matrix (regroup.cpp:350)
-            const cplx value = coefficients.v[static_cast<size_t>(index) * coefficients.cols + column];
-            if (value.real() == 0.0 && value.imag() == 0.0) continue;
-            const Sector extended_root = from_codomain ? cat.dual(taken_side.sector) : taken_side.sector;
-            Tree extended = gains_tree;
-            extended.sectors.push_back(cat.dual(charge));
-            if (gains_tree.sectors.size() >= 2) extended.inner.push_back(gains_root);
-            if (gains_tree.sectors.size() >= 1) extended.copies.push_back(taken_side.inner);
-            extended.coupled = extended_root;
-            const Sector out_codomain_root = from_codomain ? prefix : extended_root;
-            const Sector out_domain_root = from_codomain ? extended_root : prefix;
-            const auto roots = std::make_pair(out_codomain_root, out_domain_root);
-            auto found = out_layouts.find(roots);
-            if (found == out_layouts.end())
-              found = out_layouts
-                        .emplace(roots, std::make_pair(&layout_of(cat, out_codomain, out_codomain_root),
-                                                       &layout_of(cat, out_domain, out_domain_root)))
-                        .first;
-            const Layout &rows_layout = *found->second.first;
-            const Layout &cols_layout = *found->second.second;
-            const int32_t row_at = rows_layout.find(from_codomain ? kept_tree : extended);
-            const int32_t column_at = cols_layout.find(from_codomain ? extended : kept_tree);
-            if (row_at < 0 || column_at < 0) continue;
-            const int64_t row = rows_layout.offsets[static_cast<size_t>(row_at)];
-            const int64_t column_offset = cols_layout.offsets[static_cast<size_t>(column_at)];
-            const int64_t target_stride = cols_layout.rows();
-            std::vector<Piece> &pieces =
-              plan[index_of(BlockKey{out_codomain_root, out_domain_root, taken_side.outer}, rows_layout.rows(),
-                            cols_layout.rows())]
-                .pieces;
-            if (from_codomain)
-            {
-              for (int64_t shifted = 0; shifted < inside; ++shifted)
-                for (int64_t gain = 0; gain < gains; ++gain)
-                  pieces.push_back(Piece{(source_row + shifted * copies) * source_stride + source_column + gain,
-                                         (row + shifted) * target_stride + column_offset + gain * copies,
-                                         source_stride, 1, copies, value});
-            }
-            else
-            {
-              for (int64_t gain = 0; gain < gains; ++gain)
-                for (int64_t copy_at = 0; copy_at < copies; ++copy_at)
-                  pieces.push_back(Piece{(source_column + gain) * source_stride + source_row + copy_at,
-                                         (row + gain * copies + copy_at) * target_stride + column_offset, copies, 1,
-                                         inside, value});
-            }
-          }
+        const FIndex &land = landings[l];
+        // F is square; the reference reads it at (named index, landing index) in both directions
+        const cplx coefficient = f.at(named, static_cast<int32_t>(l));
+        if (coefficient == cplx(0.0, 0.0)) continue;
+        const Sector grown_root = from_codomain ? cat.dual(land.sector) : land.sector;
+        const Sector &row_root = from_codomain ? x : grown_root, &col_root = from_codomain ? grown_root : x;
+        const Layout &out_rows = layout_of(cat, new_codomain, row_root);
+        const Layout &out_cols = layout_of(cat, new_domain, col_root);
+        const int64_t out_cols_n = out_cols.rows();
+        for (size_t t = 0; t < takers.trees.size(); ++t)
+        {
+          const Tree &taker = takers.trees[t];
+          Tree grown = taker;
+          grown.sectors.push_back(cat.dual(q));
+          if (taker.sectors.size() >= 2) grown.inner.push_back(taking_root);
+          if (taker.sectors.size() >= 1) grown.copies.push_back(land.inner);
+          grown.coupled = grown_root;
+          const int32_t kept_at = (from_codomain ? out_rows : out_cols).find(kept);
+          const int32_t grown_at = (from_codomain ? out_cols : out_rows).find(grown);
+          if (kept_at < 0 || grown_at < 0) continue;
+          const int64_t kept_offset = (from_codomain ? out_rows : out_cols).offsets[static_cast<size_t>(kept_at)];
+          const int64_t grown_offset = (from_codomain ? out_cols : out_rows).offsets[static_cast<size_t>(grown_at)];
+          const int64_t taker_offset = takers.offsets[t], taker_width = takers.offsets[t + 1] - takers.offsets[t];
+          std::vector<Piece> &pieces = shifts.into(BlockKey{row_root, col_root, land.outer}, out_rows.rows(), out_cols_n);
+          if (from_codomain)
+            // source (row givers.offsets[g] + i * copies + k, column taker_offset + e) lands at
+            // (row kept_offset + i, column grown_offset + e * copies + k); a piece runs over k
+            for (int64_t i = 0; i < kept_width; ++i)
+              for (int64_t e = 0; e < taker_width; ++e)
+                pieces.push_back(Piece{(givers.offsets[g] + i * copies) * source_cols + taker_offset + e,
+                                       (kept_offset + i) * out_cols_n + grown_offset + e * copies, source_cols, 1, copies,
+                                       coefficient});
+          else
+            // source (row taker_offset + e, column givers.offsets[g] + j * copies + k) lands at
+            // (row grown_offset + e * copies + k, column kept_offset + j); a piece runs over j
+            for (int64_t e = 0; e < taker_width; ++e)
+              for (int64_t k = 0; k < copies; ++k)
+                pieces.push_back(Piece{(taker_offset + e) * source_cols + givers.offsets[g] + k,
+                                       (grown_offset + e * copies + k) * out_cols_n + kept_offset, copies, 1, kept_width,
+                                       coefficient});
+        }
       }
     }
-    return plan;
+    return shifts.take();
   }
 
-  // tentorch/tensors/place.cpp:199-214: the leading domain legs a place leaves where they are
-  // (none when a codomain leg goes below)
+  // The leading domain legs a place leaves where they are: the longest prefix of `below` that
+  // names the domain legs in their own order, or none when a codomain leg goes below (then every
+  // domain leg is lifted before the sort).
   int32_t chain_kept(int32_t height, int32_t depth, const std::vector<int32_t> &below)
   {
-    bool descends = false;
-    for (size_t at = 0; !descends && at < below.size(); ++at) descends = below[at] < height;
+    if (std::any_of(below.begin(), below.end(), [height](int32_t leg) { return leg < height; })) return 0;
+    const int32_t limit = std::min<int32_t>(depth, static_cast<int32_t>(below.size()));
     int32_t kept = 0;
-    while (!descends && kept < depth && kept < static_cast<int32_t>(below.size()) &&
-           below[static_cast<size_t>(kept)] == height + kept)
-      ++kept;
+    while (kept < limit && below[static_cast<size_t>(kept)] == height + kept) ++kept;
     return kept;
   }
 
-  // tentorch/tensors/place.cpp:41-107,199-247
   // tentorch/tensors/place.cpp:183-197: every leg named exactly once
   void check_place(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
   {
@@ -1047,56 +1054,56 @@ namespace ttg
     return true;
   }
 
+  // The steps of a place (the sequence tentorch/tensors/place.cpp:199-247 takes), tracking the legs
+  // of each side by their number in `space`: (1) every domain leg behind the kept prefix is bent
+  // up, the last first; (2) the codomain is brought to `above` followed by the legs that go below
+  // (after the kept ones) last named first, each slot filled from left to right by exchanging its
+  // leg leftwards one position at a time; (3) the tail of the codomain is bent down, the last leg
+  // first, which lands the domain in the named order.
   std::vector<Step> chain(Space space, const std::vector<int32_t> &above, const std::vector<int32_t> &below)
   {
     const int32_t height = static_cast<int32_t>(space->codomain.size());
     const int32_t depth = static_cast<int32_t>(space->domain.size());
     check_place(space, above, below);
+    const int32_t kept = chain_kept(height, depth, below);
+    const std::vector<Leg> legs = space->legs();
+    std::vector<int32_t> top(static_cast<size_t>(height)), bottom(static_cast<size_t>(depth));
+    std::iota(top.begin(), top.end(), 0);
+    std::iota(bottom.begin(), bottom.end(), height);
     std::vector<Step> steps;
-    std::vector<Leg> cod = space->codomain, dom = space->domain;
     Space current = space;
-    const auto add = [&](int32_t kind, int32_t arm)
+    const auto record = [&](int32_t kind, int32_t arm)
     {
-      Space next = make_space(space->cat, cod, dom, space->qtotal);
+      std::vector<Leg> cod, dom;
+      for (const int32_t l : top) cod.push_back(legs[static_cast<size_t>(l)]);
+      for (const int32_t l : bottom) dom.push_back(legs[static_cast<size_t>(l)]);
+      Space next = make_space(space->cat, std::move(cod), std::move(dom), space->qtotal);
       steps.push_back(Step{kind, arm, current, next});
       current = next;
     };
-    const auto fold = [&](bool from_codomain)
+    while (static_cast<int32_t>(bottom.size()) > kept)
     {
-      if (from_codomain)
-      {
-        dom.push_back(cod.back());
-        cod.pop_back();
-      }
-      else
-      {
-        cod.push_back(dom.back());
-        dom.pop_back();
-      }
-      add(from_codomain ? 1 : 2, 0);
-    };
-    const int32_t kept = chain_kept(height, depth, below);
-    for (int32_t at = kept; at < depth; ++at) fold(false);
-    const auto position_of = [height, depth](int32_t leg)
-    { return leg < height ? leg : height + (depth - 1 - (leg - height)); };
-    std::vector<int32_t> order;
-    for (const int32_t leg : above) order.push_back(position_of(leg));
-    for (auto leg = below.rbegin(); leg != below.rend() - kept; ++leg) order.push_back(position_of(*leg));
-    std::vector<int32_t> which(cod.size());
-    std::iota(which.begin(), which.end(), 0);
-    for (int32_t at = 0; at < static_cast<int32_t>(order.size()); ++at)
+      top.push_back(bottom.back());
+      bottom.pop_back();
+      record(2, 0);
+    }
+    std::vector<int32_t> wanted = above;
+    wanted.insert(wanted.end(), below.rbegin(), below.rend() - kept);
+    for (size_t slot = 0; slot < wanted.size(); ++slot)
     {
-      int32_t from = at;
-      while (which[static_cast<size_t>(from)] != order[static_cast<size_t>(at)]) ++from;
-      while (from > at)
+      size_t at = static_cast<size_t>(std::find(top.begin() + static_cast<std::ptrdiff_t>(slot), top.end(), wanted[slot]) - top.begin());
+      for (; at > slot; --at)
       {
-        std::swap(cod[static_cast<size_t>(from - 1)], cod[static_cast<size_t>(from)]);
-        add(0, from - 1);
-        std::swap(which[static_cast<size_t>(from - 1)], which[static_cast<size_t>(from)]);
-        --from;
+        std::swap(top[at - 1], top[at]);
+        record(0, static_cast<int32_t>(at - 1));
       }
     }
-    for (int32_t at = kept; at < static_cast<int32_t>(below.size()); ++at) fold(true);
+    for (size_t n = static_cast<size_t>(kept); n < below.size(); ++n)
+    {
+      bottom.push_back(top.back());
+      top.pop_back();
+      record(1, 0);
+    }
     return steps;
   }
 

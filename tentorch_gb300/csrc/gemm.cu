@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <numeric>
 #include <cmath>
 #include <map>
@@ -67,7 +68,7 @@ namespace ttg
         for (int32_t n0 = 0; n0 < blk.n; n0 += bn)
           total += cost(std::min(bm, blk.m - m0), std::min(bn, blk.n - n0), static_cast<double>(ktotal));
     }
-    const double target = std::max(total / (kScheduleCtas * 6.0), cost(bm, bn, 16.0));
+    const double target = std::max(total / (p.ctas * 6.0), cost(bm, bn, 16.0));
     struct Sized
     {
       GemmItem item;
@@ -118,7 +119,7 @@ namespace ttg
               { return items[static_cast<size_t>(a)].work > items[static_cast<size_t>(b)].work ||
                        (items[static_cast<size_t>(a)].work == items[static_cast<size_t>(b)].work && a < b); });
     // LPT: each item to the CTA with the least work so far (ties to the lower index)
-    const int ctas = static_cast<int>(std::min<size_t>(kScheduleCtas, std::max<size_t>(items.size(), 1)));
+    const int ctas = static_cast<int>(std::min<size_t>(static_cast<size_t>(p.ctas), std::max<size_t>(items.size(), 1)));
     std::vector<std::pair<double, int>> heap;
     heap.reserve(static_cast<size_t>(ctas));
     for (int c = 0; c < ctas; ++c) heap.push_back({0.0, c});
@@ -210,7 +211,7 @@ namespace ttg
     // items: one pair's K range each (a multiple of 32), about two per worker, never below a tile
     // over 128 of K
     const double target =
-      std::max(op_work(p, op) / (152.0 * kSplitWorkers * 2.0), static_cast<double>(kSplitTileM) * kSplitTileN * 128.0);
+      std::max(op_work(p, op) / (p.ctas * kSplitWorkers * 2.0), static_cast<double>(kSplitTileM) * kSplitTileN * 128.0);
     struct Sized
     {
       SplitItem item;
@@ -269,7 +270,7 @@ namespace ttg
     if (!full) return s;
     std::stable_sort(items.begin(), items.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
     // dealt to the SMs like the FP64 items (largest first onto the least loaded)
-    const int ctas = static_cast<int>(std::min<size_t>(kScheduleCtas, std::max<size_t>(items.size(), 1)));
+    const int ctas = static_cast<int>(std::min<size_t>(static_cast<size_t>(p.ctas), std::max<size_t>(items.size(), 1)));
     std::vector<std::vector<SplitItem>> lists(static_cast<size_t>(ctas));
     std::vector<std::pair<double, int>> heap;
     for (int c = 0; c < ctas; ++c) heap.push_back({0.0, c});
@@ -308,8 +309,29 @@ namespace ttg
     }
   } // namespace
 
+  int device_sms()
+  {
+    static std::atomic<int> cached[64] = {};
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64)
+    {
+      cudaGetLastError();
+      return 152;
+    }
+    int n = cached[device].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || n <= 0)
+    {
+      cudaGetLastError();
+      return 152;
+    }
+    cached[device].store(n, std::memory_order_relaxed);
+    return n;
+  }
+
   int64_t plan_gemms(Program &p)
   {
+    p.ctas = device_sms();
     auto plans = std::make_shared<GemmPlans>();
     plans->f64.resize(p.ops.size());
     plans->split.resize(p.ops.size());
@@ -1211,7 +1233,7 @@ namespace ttg
       const auto *lines = reinterpret_cast<const SplitLine *>(sched.lines);
       // a warp per line, two warps per CTA so that the lines spread over every SM
       return launch_dependent(split_lines_kernel,
-                              static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 1) / 2, 152 * 32))),
+                              static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((end - begin + 1) / 2, device_sms() * 32))),
                               64, 0, stream, A, B, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, lines,
                               sched.n_lines_a, begin, end, slices);
     }

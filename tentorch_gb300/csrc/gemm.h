@@ -40,8 +40,10 @@ namespace ttg
     int64_t slots = 0;               // partial tiles of bm x bn doubles
     int64_t n_items = 0;             // items (also when only the sizes were computed)
   };
-  // The CTAs a schedule spreads its items over: one per SM of the GPU.
-  constexpr int kScheduleCtas = 152;
+  // The SMs of the current device (cached per device), or 152, a GB300's count, when no device is
+  // visible (plans compiled on a host without a GPU).  A plan's persistent GEMM launches spread
+  // their items over this many CTAs, one per SM (Program::ctas, fixed when the plan is compiled).
+  int device_sms();
 
   // Split precision works pair by pair: an item is one pair's K range (a multiple of 32 long, but
   // for the pair's last one), so a tile with several pairs or chunks always goes through partials.

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "executor.h"
+#include "tentorch_gb300.h"
 #include "launch.h"
 
 namespace ttg
@@ -181,9 +182,9 @@ namespace ttg
 
     int grid_for(int64_t n, int threads)
     {
-      // enough CTAs to cover the arena, capped at 8 waves of the 152 SMs
+      // enough CTAs to cover the arena, capped at 8 waves of the device's SMs
       const int64_t want = (n + threads - 1) / threads;
-      return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, 152 * 8)));
+      return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, device_sms() * 8)));
     }
 
   } // namespace
@@ -353,7 +354,7 @@ namespace ttg
       case OpKind::runs:
         if (op.count > 0)
         {
-          const int grid = static_cast<int>(std::min<int64_t>(op.count, 152 * 16));
+          const int grid = static_cast<int>(std::min<int64_t>(op.count, device_sms() * 16));
           const auto *ch = reinterpret_cast<const DevChunk *>(t.chunks) + op.begin;
           const auto *te = reinterpret_cast<const DevTerm *>(t.terms);
           if (args.complex)
@@ -519,15 +520,16 @@ namespace
 extern "C" int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n,
                                    double *out, void *stream)
 {
-  if (count <= 0) return 0;
+  if (count <= 0) return TT_OK;
   if (count > kNoAllocMaxVectors)
-    return ttg::report(1, "tt_dots_noalloc takes at most " + std::to_string(kNoAllocMaxVectors) + " vectors, got " +
+    return ttg::report(TT_EINVAL, "tt_dots_noalloc takes at most " + std::to_string(kNoAllocMaxVectors) + " vectors, got " +
                             std::to_string(count) + "; call tt_dots with caller-provided scratch instead");
-  if (dtype != 0 && dtype != 1) return ttg::report(1, "unknown dtype");
+  if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128)
+    return ttg::report(TT_EINVAL, "unknown dtype " + std::to_string(dtype));
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
-  if (e != cudaSuccess) return ttg::report(4, std::string("CUDA: ") + cudaGetErrorString(e));
-  if (device < 0 || device >= kNoAllocMaxDevices) return ttg::report(1, "device index beyond the static table");
+  if (e != cudaSuccess) return ttg::report(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= kNoAllocMaxDevices) return ttg::report(TT_EINVAL, "device index beyond the static table");
   double *scratch = nullptr;
   {
     // set-up, once per device, with that device current: the device address of the array (host
@@ -537,7 +539,7 @@ extern "C" int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *con
     {
       void *address = nullptr;
       e = cudaGetSymbolAddress(&address, tt_dots_noalloc_scratch);
-      if (e != cudaSuccess) return ttg::report(4, std::string("CUDA: ") + cudaGetErrorString(e));
+      if (e != cudaSuccess) return ttg::report(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
       noalloc_scratch[device] = static_cast<double *>(address);
     }
     scratch = noalloc_scratch[device];
@@ -547,7 +549,7 @@ extern "C" int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *con
   const bool complex = dtype == 1;
   e = ttg::arena_dots(reinterpret_cast<const double *const *>(as), count, static_cast<const double *>(b),
                       n * (complex ? 2 : 1), complex, scratch, out, static_cast<cudaStream_t>(stream));
-  if (e != cudaSuccess) return ttg::report(4, std::string("CUDA: ") + cudaGetErrorString(e));
-  return 0;
+  if (e != cudaSuccess) return ttg::report(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  return TT_OK;
 }
 

@@ -84,7 +84,7 @@ namespace ttg
       }
     }
 
-    int grid_of(int64_t n_doubles) { return static_cast<int>(std::clamp<int64_t>((n_doubles + 255) / 256, 1, 152 * 8)); }
+    int grid_of(int64_t n_doubles) { return static_cast<int>(std::clamp<int64_t>((n_doubles + 255) / 256, 1, device_sms() * 8)); }
 
     // Eigenpairs of a small symmetric matrix by cyclic Jacobi rotations (C. G. J. Jacobi, 1846; the
     // rotation as in Golub & Van Loan, "Matrix Computations", the symmetric Schur decomposition):

@@ -914,84 +914,120 @@ namespace ttg
       return out;
     }
 
-    double tensor_size(const std::vector<char> &labels, const std::map<char, double> &dims)
+    // A set of einsum labels as a bit mask over the equation's letters, with the size of a tensor
+    // over them: the product of their dimensions, multiplied in the order the labels joined the set
+    // (the order the reference multiplies them in, tentorch/linalg/graded/einsum.cpp:170-176, so
+    // that equal costs compare equal there and here).
+    struct LabelSet
     {
-      double out = 1;
-      for (char l : labels) out *= dims.at(l);
-      return out;
-    }
+      uint64_t bits = 0;
+      double size = 1;
+    };
 
-    // tentorch/linalg/graded/einsum.cpp:216-301
+    // The order the operands of an einsum are folded in (the rule of
+    // tentorch/linalg/graded/einsum.cpp:211-301): operand 0 first, then every other operand once,
+    // so that the sum of the products' sizes is smallest, the size of a product being that of every
+    // label the accumulator has met (summed labels included).
+    //
+    // Up to 12 operands the order is exact: over the subsets S of the other operands,
+    //   best(S) = min over o in S of best(S - o) + size(labels of operand 0 and of S),
+    // with o allowed only when it shares a label with operand 0 and S - o (outer products only when
+    // no order without them exists).  Equal costs go to the step that sums more labels, then to the
+    // operand written later.  Beyond 12 operands: greedily the operand whose product with the
+    // accumulator is smallest, operands sharing a label first, the one written first on ties.
     std::vector<int32_t> fold_order(const std::vector<std::vector<char>> &inputs, const std::map<char, double> &dims)
     {
       const int32_t count = static_cast<int32_t>(inputs.size());
-      std::vector<int32_t> order;
+      std::map<char, int32_t> letter;
+      for (const auto &labels : inputs)
+        for (const char l : labels) letter.emplace(l, static_cast<int32_t>(letter.size()));
+      std::vector<uint64_t> mask_of(inputs.size(), 0);
+      for (size_t i = 0; i < inputs.size(); ++i)
+        for (const char l : inputs[i]) mask_of[i] |= uint64_t(1) << letter[l];
+      const auto joined = [&](LabelSet set, int32_t operand)
+      {
+        for (const char l : inputs[static_cast<size_t>(operand)])
+        {
+          const uint64_t bit = uint64_t(1) << letter[l];
+          if (set.bits & bit) continue;
+          set.bits |= bit;
+          set.size *= dims.at(l);
+        }
+        return set;
+      };
+      const auto sums = [&](const LabelSet &set, int32_t operand)
+      { return static_cast<int32_t>(__builtin_popcountll(set.bits & mask_of[static_cast<size_t>(operand)])); };
+      std::vector<int32_t> order{0};
       if (count <= 12)
       {
-        const int64_t masks = int64_t(1) << (count - 1);
-        std::vector<std::vector<char>> labels(static_cast<size_t>(masks), inputs.front());
-        for (int64_t mask = 1; mask < masks; ++mask)
+        const int32_t others = count - 1;
+        const size_t subsets = size_t(1) << others;
+        // the labels of operand 0 and of subset S, joined highest operand first (as the reference
+        // builds them: S's lowest operand joins the labels of the rest of S)
+        std::vector<LabelSet> met(subsets);
+        met[0] = joined(LabelSet{}, 0);
+        for (size_t set = 1; set < subsets; ++set)
         {
-          const int bit = __builtin_ctzll(static_cast<unsigned long long>(mask));
-          labels[static_cast<size_t>(mask)] = union_of(labels[static_cast<size_t>(mask ^ (int64_t(1) << bit))], inputs[static_cast<size_t>(bit + 1)]);
+          const int32_t low = __builtin_ctzll(static_cast<unsigned long long>(set));
+          met[set] = joined(met[set & (set - 1)], low + 1);
         }
-        for (int pass = 0; pass < 2; ++pass)
+        for (const bool outer : {false, true})
         {
-          std::vector<double> cost(static_cast<size_t>(masks), std::numeric_limits<double>::infinity());
-          std::vector<int64_t> summed(static_cast<size_t>(masks), 0), last(static_cast<size_t>(masks), 0);
-          cost[0] = 0;
-          for (int64_t mask = 1; mask < masks; ++mask)
-            for (int64_t bit = 0; bit < count - 1; ++bit)
-              if (mask & (int64_t(1) << bit))
-              {
-                const int64_t prev = mask ^ (int64_t(1) << bit);
-                const std::vector<char> shared = shared_of(labels[static_cast<size_t>(prev)], inputs[static_cast<size_t>(bit + 1)]);
-                if (pass == 0 && shared.empty()) continue;
-                const double candidate = cost[static_cast<size_t>(prev)] + tensor_size(labels[static_cast<size_t>(mask)], dims);
-                const size_t m = static_cast<size_t>(mask);
-                const bool better = candidate < cost[m] ||
-                                    (candidate == cost[m] && static_cast<int64_t>(shared.size()) > summed[m]) ||
-                                    (candidate == cost[m] && static_cast<int64_t>(shared.size()) == summed[m] && bit > last[m]);
-                if (better)
-                {
-                  cost[m] = candidate;
-                  summed[m] = static_cast<int64_t>(shared.size());
-                  last[m] = bit;
-                }
-              }
-          if (cost[static_cast<size_t>(masks - 1)] == std::numeric_limits<double>::infinity()) continue;
-          for (int64_t mask = masks - 1; mask; mask ^= int64_t(1) << last[static_cast<size_t>(mask)])
-            order.push_back(static_cast<int32_t>(last[static_cast<size_t>(mask)] + 1));
-          order.push_back(0);
-          std::reverse(order.begin(), order.end());
-          return order;
-        }
-      }
-      std::vector<bool> taken(inputs.size(), false);
-      std::vector<char> live = inputs.front();
-      order.push_back(0);
-      taken[0] = true;
-      for (int32_t step = 1; step < count; ++step)
-      {
-        int32_t best = -1;
-        double best_size = 0;
-        bool found = false;
-        for (int pass = 0; pass < 2 && !found; ++pass)
-          for (int32_t at = 0; at < count; ++at)
+          std::vector<double> best(subsets, std::numeric_limits<double>::infinity());
+          std::vector<int32_t> step(subsets, -1);
+          best[0] = 0;
+          for (size_t set = 1; set < subsets; ++set)
           {
-            if (taken[static_cast<size_t>(at)]) continue;
-            if (shared_of(live, inputs[static_cast<size_t>(at)]).empty() != (pass == 1)) continue;
-            const double size = tensor_size(union_of(live, inputs[static_cast<size_t>(at)]), dims);
-            if (!found || size < best_size)
+            int32_t chosen_sums = -1;
+            for (int32_t o = 0; o < others; ++o)
             {
-              found = true;
-              best = at;
-              best_size = size;
+              if (!(set >> o & 1)) continue;
+              const size_t rest = set & ~(size_t(1) << o);
+              if (best[rest] == std::numeric_limits<double>::infinity()) continue;
+              const int32_t summed = sums(met[rest], o + 1);
+              if (!outer && summed == 0) continue;
+              const double cost = best[rest] + met[set].size;
+              // (cost, -summed, -o) smallest wins; operands are visited in increasing o
+              if (cost < best[set] || (cost == best[set] && summed >= chosen_sums))
+              {
+                best[set] = cost;
+                chosen_sums = summed;
+                step[set] = o;
+              }
             }
           }
-        order.push_back(best);
-        taken[static_cast<size_t>(best)] = true;
-        live = union_of(live, inputs[static_cast<size_t>(best)]);
+          if (step[subsets - 1] < 0 && subsets > 1) continue;
+          std::vector<int32_t> tail;
+          for (size_t set = subsets - 1; set; set &= ~(size_t(1) << step[set])) tail.push_back(step[set] + 1);
+          order.insert(order.end(), tail.rbegin(), tail.rend());
+          return order;
+        }
+        return order;
+      }
+      std::vector<bool> taken(inputs.size(), false);
+      taken[0] = true;
+      LabelSet live = joined(LabelSet{}, 0);
+      while (static_cast<int32_t>(order.size()) < count)
+      {
+        int32_t pick = -1;
+        double pick_size = 0;
+        for (const bool outer : {false, true})
+        {
+          for (int32_t o = 1; o < count; ++o)
+          {
+            if (taken[static_cast<size_t>(o)] || (sums(live, o) == 0) != outer) continue;
+            const double size = joined(live, o).size;
+            if (pick < 0 || size < pick_size)
+            {
+              pick = o;
+              pick_size = size;
+            }
+          }
+          if (pick >= 0) break;
+        }
+        order.push_back(pick);
+        taken[static_cast<size_t>(pick)] = true;
+        live = joined(live, pick);
       }
       return order;
     }
@@ -1294,6 +1330,7 @@ namespace ttg
     }
     if (results.empty()) throw InvalidArgument("no way for the charges of '" + spec + "' to fuse to " + charge.str());
     finish(*p, b, results);
+    p->fold = order;
     return p;
   }
 

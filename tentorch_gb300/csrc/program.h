@@ -132,6 +132,8 @@ namespace ttg
     std::vector<Op> ops;
     int64_t workspace = 0;  // elements
     int64_t scratch_offset = 0;  // elements: GEMM scratch (partial tiles, slices) at the end of the workspace
+    int32_t ctas = 152;          // CTAs of its persistent GEMM launches: the SMs of the device it was compiled for
+    std::vector<int32_t> fold;   // an einsum's operands in the order it folds them (empty for other plans)
     // per operand: the buffer holding its prepared value (the input itself when no op prepares it)
     std::vector<int32_t> prepared;
     // descriptor tables

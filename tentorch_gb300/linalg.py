@@ -113,6 +113,8 @@ _prepared = {}
 # (device index, stream, dtype) -> a workspace arena that grows to the largest plan run on it; the
 # ops of one stream run in order, so consecutive plans share it
 _pools = {}
+# workspaces replaced by larger ones after a capture (a captured graph may still address them)
+_superseded = []
 # set once a plan has run inside a CUDA graph capture: the graph holds the device addresses of its
 # tables and workspace, so the automatic clear at the budget no longer runs
 _captured = False
@@ -129,6 +131,7 @@ def clear_plans() -> None:
     _plans.clear()
     _prepared.clear()
     _pools.clear()
+    _superseded.clear()
     check(lib.tt_plan_cache_clear())
 
 
@@ -172,6 +175,10 @@ def _workspace(plan: Plan, device, dtype, stream) -> Optional[torch.Tensor]:
     key = (device.index, stream, dtype)
     pool = _pools.get(key)
     if pool is None or pool.numel() < plan.workspace:
+        if pool is not None and _captured:
+            # a CUDA graph captured earlier may hold this pool's address: keep it allocated, so that
+            # a replay never writes into memory the caching allocator has handed to another tensor
+            _superseded.append(pool)
         # zero: the head of a workspace holds the GEMM tickets, which every execution leaves zero
         pool = _pools[key] = torch.zeros(max(plan.workspace, 1 << 16), dtype = dtype, device = device)
     return pool

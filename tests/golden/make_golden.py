@@ -225,10 +225,10 @@ def cases():
     return out
 
 
-def dmrg_energies():
-    '''The reference's DMRG in float64: its random MPS patched to draw float64 blocks in key order
-    from a seeded generator, its identities and MPO blocks cast to float64 (the reference builds
-    complex128 by default).'''
+def float64_harness():
+    '''Patch the reference's DMRG to run in float64: its random MPS draws float64 blocks in key order
+    from a seeded generator, its identities and MPO blocks are cast to float64 (the reference builds
+    complex128 by default).  Returns the patched DMRG module and the exact-diagonalisation helper.'''
     import tentorch.networks.mps as mps_module
     dmrg_module = sys.modules['tentorch.algorithms.dmrg']
     import importlib.util
@@ -284,6 +284,12 @@ def dmrg_energies():
         mpo.tensors = sites
         return mpo
     dmrg_module.heisenberg = heisenberg64
+    return dmrg_module, exact_energy_of
+
+
+def dmrg_energies():
+    '''The reference's float64 DMRG at small lengths, against exact diagonalisation, and config 1.'''
+    dmrg_module, exact_energy_of = float64_harness()
     out = {'exact': {}, 'small': {}, 'config1': {}}
     for length in (4, 6, 8):
         model = tt.Model(length, cat = tt.u1)
@@ -301,8 +307,31 @@ def dmrg_energies():
     return out
 
 
+def dmrg_chi256(sweeps = 6):
+    '''The reference's float64 DMRG of the U(1) Heisenberg chain at L = 64, max bond 256, n_iter = 10,
+    seed 0: per sweep its energy (the last window's Ritz value), the largest discarded weight and the
+    bond dimensions, and after the last sweep the expectation `DMRG.energy()`.  The first four sweeps
+    bring every bond to 256; the later ones are the steady state.'''
+    import time
+    dmrg_module, _ = float64_harness()
+    driver = dmrg_module.DMRG(tt.Model(64, cat = tt.u1), max_bond_dim = 256, n_iter = 10, seed = 0)
+    out = []
+    for _ in range(sweeps):
+        start = time.perf_counter()
+        energy, lost = driver.sweep()
+        out.append({'energy': energy, 'discarded': lost, 'bond': driver.state.bond_dims,
+                    'seconds': time.perf_counter() - start, 'threads': torch.get_num_threads()})
+        print('sweep', len(out), energy, lost, max(driver.state.bond_dims), out[-1]['seconds'], flush = True)
+    return {'length': 64, 'max_bond_dim': 256, 'n_iter': 10, 'seed': 0, 'svd_tol': driver.svd_tol,
+            'sweeps': out, 'energy': driver.energy().real}
+
+
 if __name__ == '__main__':
     sys.path.insert(0, HERE)
+    if sys.argv[1:] == ['dmrg_chi256']:
+        # about a minute and a half per sweep on eight cores: run on its own, not by default
+        json.dump(dmrg_chi256(), open(os.path.join(HERE, 'dmrg_chi256.json'), 'w'), indent = 1)
+        raise SystemExit(0)
     if sys.argv[1:] == ['dmrg']:
         # the reference's buffer pool is keyed by shape and not by dtype (tentorch/tensors/cache.cpp:
         # 120-130), so the float64 DMRG runs in a process that never held a complex128 tensor

@@ -92,8 +92,9 @@ def step_plan(space_id, kind, arm, key):
 
 
 def test_step_plans_match_the_reference_bit_for_bit():
-    '''Every piece of every shift of every block of every step: first, last, steps and run exactly,
-    the coefficient to 1e-12.'''
+    '''Every shift of every block of every step, matched by the block it writes: the same pieces
+    (first, last, steps and run exactly, the coefficient to 1e-12), in whatever order each side
+    lists them.'''
     kinds = {'x': 0, 'down': 1, 'up': 2}
     checked = 0
     for record in load_json('plans.json'):
@@ -102,17 +103,17 @@ def test_step_plans_match_the_reference_bit_for_bit():
             space = Space.of(cat, legs(cat, step['codomain']), legs(cat, step['domain']), tuple(record['qtotal']))
             for block in step['blocks']:
                 key = (tuple(block['key'][0]), tuple(block['key'][1]), block['key'][2])
-                got = step_plan(space.id, kinds[step['kind']], step['arm'], key)
-                want = block['shifts']
-                assert len(got) == len(want)
-                for mine, theirs in zip(got, want):
+                got = {tuple(shift[1]): shift for shift in step_plan(space.id, kinds[step['kind']], step['arm'], key)}
+                want = {tuple(s[1][0] + s[1][1] + [s[1][2]]): s for s in block['shifts']}
+                assert set(got) == set(want)
+                for to, theirs in want.items():
+                    mine = got[to]
                     assert list(mine[0]) == theirs[0][0] + theirs[0][1] + [theirs[0][2]]
-                    assert list(mine[1]) == theirs[1][0] + theirs[1][1] + [theirs[1][2]]
                     assert (mine[2], mine[3]) == (theirs[2], theirs[3])
-                    assert [tuple(int(x) for x in p[:5]) for p in mine[4]] == [tuple(p[:5]) for p in theirs[4]]
-                    coef = np.array([p[5] + 1j * p[6] for p in mine[4]])
-                    ref = np.array([p[5] + 1j * p[6] for p in theirs[4]])
-                    assert np.abs(coef - ref).max(initial = 0) < 1e-12
+                    ours = sorted((tuple(int(x) for x in p[:5]), p[5] + 1j * p[6]) for p in mine[4])
+                    ref = sorted((tuple(p[:5]), p[5] + 1j * p[6]) for p in theirs[4])
+                    assert [k for k, _ in ours] == [k for k, _ in ref]
+                    assert max((abs(a - b) for (_, a), (_, b) in zip(ours, ref)), default = 0.0) < 1e-12
                     checked += len(mine[4])
     assert checked > 1000
 
@@ -153,6 +154,14 @@ def test_errors_map_to_the_reference_exceptions():
         tg.einsum('ABc->ABc', t, charge = (1,))
     with pytest.raises(RuntimeError, match = 'CUDA device'):
         tg.einsum('ABc->ABc', t, outcharge = (1,))
+
+
+def test_dot_entry_points_refuse_an_unknown_dtype_before_any_device_work():
+    # both dot products check their arguments on the host, so the refusal needs no GPU
+    for call in (lambda: _lib.lib.tt_dots(7, 1, None, None, 16, None, None, None),
+                 lambda: _lib.lib.tt_dots_noalloc(7, 1, None, None, 16, None, None)):
+        with pytest.raises(ValueError, match = 'unknown dtype'):
+            _lib.check(call())
 
 
 def test_einsum_plan_compiles_on_the_host():
@@ -323,3 +332,57 @@ def test_plan_cache_clears_wholesale_at_its_budget_and_held_plans_recompile(monk
     assert first.generation == la._generation
     assert first.describe() == text
     la.clear_plans()
+
+
+def _random_network(rng, count, sizes):
+    '''A random einsum over `count` operands: every label joins two different operands or stays
+    open (one to three open labels), legs of no symmetry whose multiplets are drawn from `sizes`.'''
+    while True:
+        slots = [list(range(int(rng.integers(2, 4)))) for _ in range(count)]
+        ends = [(o, s) for o, legs_of in enumerate(slots) for s in legs_of]
+        rng.shuffle(ends)
+        labels = [[None] * len(legs_of) for legs_of in slots]
+        letters = iter('abcdefghijklmnopqrstuvwxyz')
+        open_left = int(rng.integers(1, 4))
+        pending = list(ends)
+        while pending:
+            o, s = pending.pop()
+            partner = next((i for i, (o2, _) in enumerate(pending) if o2 != o), None)
+            letter = next(letters, None)
+            if letter is None:
+                break
+            labels[o][s] = letter
+            if partner is not None and (open_left == 0 or rng.random() < 0.8):
+                o2, s2 = pending.pop(partner)
+                labels[o2][s2] = letter
+            else:
+                open_left -= 1
+        if any(l is None for ls in labels for l in ls):
+            continue
+        opened = [l for ls in labels for l in ls if sum(l in other for other in labels) == 1]
+        if opened:
+            break
+    dims = {l: int(rng.choice(sizes)) for ls in labels for l in ls}
+    leg_of = {l: tg.Leg(tg.no_symmetry, [(0,)], [dims[l]]) for l in dims}
+    tensors = [tg.Tensor(tg.no_symmetry, [leg_of[l] for l in ls], [], (0,), device = 'cpu') for ls in labels]
+    spec = ','.join(''.join(ls) for ls in labels) + '->' + ''.join(opened)
+    return spec, labels, {l: float(d) for l, d in dims.items()}, tensors
+
+
+def test_einsum_fold_order_is_the_reference_rule():
+    '''The order an einsum folds its operands in (tentorch/linalg/graded/einsum.cpp:216-301), on
+    random networks of 2 to 14 operands whose leg sizes tie often, against the oracle's restatement:
+    the exact search up to 12 operands (ties broken by the labels a step sums, then the operand
+    written later) and the greedy rule beyond.'''
+    from oracle import engine as orc
+    rng = np.random.default_rng(11)
+    checked = 0
+    for trial in range(60):
+        count = int(rng.integers(2, 8)) if trial < 50 else int(rng.integers(13, 15))
+        spec, labels, dims, tensors = _random_network(rng, count, [2, 3] if trial % 2 else [2, 3, 5, 7])
+        text = tg.linalg.plan_of(spec, *tensors).describe()
+        line = next(l for l in text.splitlines() if l.startswith('fold order'))
+        got = [int(x) for x in line.split()[2:]]
+        assert got == orc.fold_order(labels, dims), spec
+        checked += 1
+    assert checked == 60
