@@ -126,7 +126,9 @@ int32_t tt_plan_gather(const tt_plan *plan, int32_t op, int64_t cap, int32_t *in
  * split execution that is given the arena). */
 int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *elements);
 /* Execute on `stream` (a cudaStream_t, 0 for the legacy stream).  precision 0: FP64 block
- * products in the grouped persistent kernels; k >= 1: split products on the tensor cores with k
+ * products in the grouped persistent kernels (a product whose result a leg move with unit
+ * coefficients relabels for a second product, as in the two-site matvec, runs with that move and
+ * that product as ONE launch; in split precision the first product stores through the move); k >= 1: split products on the tensor cores with k
  * bf16 slices per operand; TT_PRECISION_PER_BLOCK (-1): the plain per-block FP64 form, one cuBLAS
  * call per block pair as the reference issues them on a CUDA device
  * (tentorch/linalg/graded/contract.cpp:148-163), the comparison arm of the grouped kernels.
@@ -137,9 +139,23 @@ int32_t tt_plan_prepared_size(const tt_plan *plan, int32_t operand, int64_t *ele
  * stream (they must not run concurrently on it). */
 int32_t tt_plan_execute(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                         const void *const *prepared, void *output, void *workspace, void *stream);
-/* The same, synchronously, recording a CUDA event pair around every operation on `stream`: per op
- * its device milliseconds (-1 when it did not run) and its kind (0 zero, 1 gather, 2 runs, 3 gemm,
- * 4 add, 5 copy, 6 tiles).  For measurement; the caller's stream is synchronised before it returns. */
+/* `count` plans executed on `stream`, each as tt_plan_execute would (per plan its operand arenas
+ * inputs[i], prepared arenas prepared[i] (may be NULL), output arena outputs[i] and its OWN workspace
+ * workspaces[i], zeroed when first used).  When every plan is an FP64 product chain (the two-site
+ * matvec: its operations besides the chain prepare operands) and count <= 64, the chains of all of
+ * them run as ONE persistent launch, their work items dealt together over the SMs (the deal cached
+ * per list of plans); otherwise, and in split precision, one plan after another.  *launched (may be
+ * NULL) receives the number of launches of the plans' products made (1 for the batched one).  For
+ * many independent DMRG windows of different bond dimension (tentorch/algorithms/dmrg.py:116-118 runs
+ * one window at a time). */
+int32_t tt_plan_execute_batch(int32_t count, const tt_plan *const *plans, int32_t dtype, int32_t precision,
+                              const void *const *const *inputs, const void *const *const *prepared,
+                              void *const *outputs, void *const *workspaces, void *stream, int32_t *launched);
+/* The same as tt_plan_execute, synchronously, recording a CUDA event pair around every operation on
+ * `stream`: per op its device milliseconds (-1 when it did not run) and its kind (0 zero, 1 gather,
+ * 2 runs, 3 gemm, 4 add, 5 copy, 6 tiles, 7 a product, the leg move of its result and the product
+ * that reads it run as one FP64 launch, timed on the first product's op).  For measurement; the
+ * caller's stream is synchronised before it returns. */
 int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                               const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
                               float *op_ms, int32_t *op_kind);

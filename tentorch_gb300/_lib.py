@@ -55,6 +55,7 @@ _declare('tt_plan_describe', vp, i64, ctypes.c_char_p, P(i64))
 _declare('tt_plan_cache_clear')
 _declare('tt_plan_gather', vp, i32, i64, P(i32), P(i64))
 _declare('tt_plan_execute', vp, i32, i32, P(vp), P(vp), vp, vp, vp)
+_declare('tt_plan_execute_batch', i32, P(vp), i32, i32, P(vp), P(vp), P(vp), P(vp), vp, P(i32))
 _declare('tt_plan_execute_timed', vp, i32, i32, P(vp), P(vp), vp, vp, vp, i32, P(ctypes.c_float), P(i32))
 _declare('tt_plan_prepare', vp, i32, i32, vp, vp, vp, vp)
 _declare('tt_step_plan', i32, i32, i32, i64, i64, i32, i64, P(i64), i64, P(f64), P(i64), P(i64))
@@ -96,4 +97,4 @@ EXPORTED = ['tt_last_error', 'tt_version', 'tt_category', 'tt_outcomes', 'tt_dua
             'tt_R_symbol', 'tt_leg', 'tt_leg_blocks', 'tt_reachable_charges', 'tt_fusion_trees', 'tt_space',
             'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_conj', 'tt_plan_contract', 'tt_plan_einsum',
             'tt_plan_info', 'tt_plan_describe', 'tt_plan_cache_clear', 'tt_plan_gather', 'tt_plan_prepared_size', 'tt_plan_execute', 'tt_plan_execute_timed', 'tt_plan_prepare', 'tt_step_plan', 'tt_chain', 'tt_svd_workspace', 'tt_lanczos_scratch', 'tt_lanczos', 'tt_svd_blocks', 'tt_svd_keep',
-            'tt_dots', 'tt_dots_noalloc']
+            'tt_dots', 'tt_dots_noalloc', 'tt_plan_execute_batch']

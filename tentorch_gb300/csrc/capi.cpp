@@ -371,24 +371,8 @@ extern "C"
       // the index the tiles amount to, entry by entry
       *count = o.elements;
       if (cap < o.elements) return;
-      std::fill(index, index + o.elements, -1);
-      for (int64_t c = o.begin; c < o.begin + o.count; ++c)
-      {
-        const ttg::TileChunk &ch = p.tile_chunks[static_cast<size_t>(c)];
-        const ttg::Tile &t = p.tiles[static_cast<size_t>(ch.tile)];
-        if (t.in_base < 0) continue;  // a zero pad entry
-        for (int32_t r = ch.row0; r < ch.row0 + ch.nrows; ++r)
-          for (int32_t col = 0; col < t.cols; ++col)
-          {
-            int64_t in = t.in_base;
-            int32_t rest = r;
-            for (int32_t l = t.n_row - 1; l >= 0; --l) in += static_cast<int64_t>(rest % t.extent[l]) * t.stride[l], rest /= t.extent[l];
-            rest = col;
-            for (int32_t l = t.n_row + t.n_col - 1; l >= t.n_row; --l)
-              in += static_cast<int64_t>(rest % t.extent[l]) * t.stride[l], rest /= t.extent[l];
-            index[t.out_base + static_cast<int64_t>(r) * t.out_ld + col] = static_cast<int32_t>(in);
-          }
-      }
+      const std::vector<int32_t> expanded = ttg::expand_move(p, o);
+      std::copy(expanded.begin(), expanded.end(), index);
     });
   }
 
@@ -396,6 +380,7 @@ extern "C"
   {
     return guarded([&] {
       std::lock_guard<std::recursive_mutex> lock(registry_mutex);
+      ttg::clear_chain_batches();
       plan_cache().clear();
     });
   }
@@ -406,6 +391,9 @@ extern "C"
       const ttg::Program &p = *plan->program;
       static const char *kinds[] = {"zero", "gather", "runs", "gemm", "add", "copy", "tiles"};
       std::string out;
+      if (p.chain_first >= 0)
+        out += "chain ops " + std::to_string(p.chain_first) + " " + std::to_string(p.chain_move) + " " +
+               std::to_string(p.chain_second) + "\n";
       if (!p.fold.empty())
       {
         out += "fold order";
@@ -488,6 +476,85 @@ extern "C"
     return TT_OK;
   }
 
+  int32_t tt_plan_execute_batch(int32_t count, const tt_plan *const *plans, int32_t dtype, int32_t precision,
+                                const void *const *const *inputs, const void *const *const *prepared,
+                                void *const *outputs, void *const *workspaces, void *stream, int32_t *launched)
+  {
+    if (count < 0 || (count > 0 && (!plans || !inputs || !outputs || !workspaces)))
+      return fail(TT_EINVAL, "a batch needs its plans, inputs, outputs and workspaces");
+    if (precision < TT_PRECISION_PER_BLOCK || precision > 8)
+      return fail(TT_EINVAL, "precision is 0 (FP64), 1..8 slices, or -1 (per-block FP64)");
+    if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128) return fail(TT_EINVAL, "unknown dtype");
+    if (precision > 0 && dtype != TT_DTYPE_FLOAT64) return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
+    for (int32_t i = 0; i < count; ++i)
+      if (!plans[i]) return fail(TT_EINVAL, "no plan");
+    if (launched) *launched = 0;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const auto args_of = [&](int32_t i)
+    {
+      ttg::ExecArgs args;
+      args.complex = dtype == TT_DTYPE_COMPLEX128;
+      args.precision = precision;
+      args.inputs = inputs[i];
+      args.prepared = prepared ? prepared[i] : nullptr;
+      args.output = outputs[i];
+      args.workspace = workspaces[i];
+      args.stream = s;
+      return args;
+    };
+    cudaError_t e = cudaSuccess;
+    // one launch when every plan is an FP64 chain whose other ops are prepare phases
+    bool one = count > 0 && count <= ttg::kChainBatch && dtype == TT_DTYPE_FLOAT64 && precision == 0;
+    for (int32_t i = 0; i < count && one; ++i)
+    {
+      const ttg::Program &p = *plans[i]->program;
+      if (p.chain_first < 0) one = false;
+      for (size_t j = 0; j < p.ops.size() && one; ++j)
+        if (p.ops[j].phase < 0 && static_cast<int32_t>(j) != p.chain_first && static_cast<int32_t>(j) != p.chain_move &&
+            static_cast<int32_t>(j) != p.chain_second)
+          one = false;
+    }
+    if (one)
+    {
+      std::vector<ttg::ChainBatchEntry> entries;
+      for (int32_t i = 0; i < count && e == cudaSuccess; ++i)
+      {
+        const ttg::Program &p = *plans[i]->program;
+        ttg::ExecArgs args = args_of(i);
+        if ((e = plans[i]->tables->ensure(p)) != cudaSuccess) break;
+        // the phases the caller has no prepared arena for run first, one plan after another
+        args.phases_only = true;
+        if ((e = ttg::execute(p, *plans[i]->tables, args)) != cudaSuccess) break;
+        args.phases_only = false;
+        const std::vector<char *> ptr = ttg::buffer_pointers(p, args);
+        const ttg::Op &first = p.ops[static_cast<size_t>(p.chain_first)], &move = p.ops[static_cast<size_t>(p.chain_move)],
+                      &second = p.ops[static_cast<size_t>(p.chain_second)];
+        entries.push_back({&p, plans[i]->tables.get(), reinterpret_cast<const double *>(ptr[static_cast<size_t>(first.src)]),
+                           reinterpret_cast<const double *>(ptr[static_cast<size_t>(first.src2)]),
+                           reinterpret_cast<const double *>(ptr[static_cast<size_t>(second.src2)]),
+                           reinterpret_cast<double *>(ptr[static_cast<size_t>(move.dst)]),
+                           reinterpret_cast<double *>(ptr[static_cast<size_t>(second.dst)]), workspaces[i]});
+      }
+      bool used = false;
+      if (e == cudaSuccess) e = ttg::launch_chain_batch(entries, s, &used);
+      if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+      if (used)
+      {
+        if (launched) *launched = 1;
+        return TT_OK;
+      }
+    }
+    // one plan after another (a plan whose phases already ran above runs them again, to the same values)
+    for (int32_t i = 0; i < count && e == cudaSuccess; ++i)
+    {
+      ttg::ExecArgs args = args_of(i);
+      e = ttg::execute(*plans[i]->program, *plans[i]->tables, args);
+    }
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    if (launched) *launched = count;
+    return TT_OK;
+  }
+
   int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                                 const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
                                 float *op_ms, int32_t *op_kind)
@@ -513,6 +580,8 @@ extern "C"
       args.workspace = workspace;
       args.stream = static_cast<cudaStream_t>(stream);
       args.events = events.data();
+      bool chained = false;
+      args.chain_ran = &chained;
       e = ttg::execute(p, *plan->tables, args);
       if (e == cudaSuccess) e = cudaStreamSynchronize(args.stream);
       for (size_t i = 0; i < n && e == cudaSuccess; ++i)
@@ -525,7 +594,8 @@ extern "C"
         if (static_cast<int32_t>(i) < cap)
         {
           op_ms[i] = ms;
-          op_kind[i] = static_cast<int32_t>(p.ops[i].kind);
+          // 7: the product chain as one launch (timed on its first op)
+          op_kind[i] = chained && static_cast<int32_t>(i) == p.chain_first ? 7 : static_cast<int32_t>(p.ops[i].kind);
         }
       }
     }

@@ -34,6 +34,10 @@ namespace ttg
     cudaError_t commit(void **base);
   };
 
+  // A non-blocking stream of this library per device, for building tables before any launch reads
+  // them (each build is waited for on the host).
+  cudaError_t upload_stream(cudaStream_t *stream);
+
   // The descriptor tables of one program, uploaded on first execution (plan-compile time, never
   // inside a timed or captured region once warmed up), all in one device allocation.
   struct DeviceTables
@@ -73,8 +77,35 @@ namespace ttg
       int64_t n_items = 0, n_reduces = 0, n_lines_a = 0, n_lines_b = 0, slice_a = 0, slice_b = 0, exps_a = 0, exps = 0,
               slots = 0;
     };
+    // the tile lists of split products on the tensor cores (split_tc.cu), built on first use
+    struct TcTables
+    {
+      bool ready = false;
+      void *base = nullptr;
+      void *items = nullptr;
+      int32_t *cta_begin = nullptr;
+      int32_t n_ctas = 0;
+    };
     std::vector<GemmTables> gemm;
     std::vector<SplitTables> split;
+    std::vector<TcTables> tc;
+    // the program's product chain (chain.cu): the relabelling table of its move (built on its first
+    // launch in any form) and the one-launch FP64 tables (built on its first FP64 launch)
+    struct ChainTables
+    {
+      bool tried = false, ok = false;                  // the one-launch FP64 tables
+      bool relabel_tried = false, relabel_ok = false;  // the relabelling table
+      void *base = nullptr;
+      const ChainItem *items = nullptr;
+      const int32_t *cta_begin = nullptr;
+      const ChainReduce *reduces = nullptr;
+      void *relabel_base = nullptr;
+      const int32_t *relabel = nullptr;    // per entry of the first product's result: its place after the move, or -1
+      int32_t n_ctas = 0;
+      int64_t longest = 0, n_items = 0, n_reduces = 0, first_tiles = 0, slots = 0, moved_from = 0;
+      std::vector<ChainItem> host_items;  // every item, first product first, before the deal (for batches)
+      std::vector<double> host_work;      // their work estimates
+    } chain;
 
     cudaError_t ensure(const Program &p);
     ~DeviceTables();
@@ -93,23 +124,61 @@ namespace ttg
     int32_t only_phase = -1;               // >= 0: run only this operand's prepare phase
     void *prepared_out = nullptr;          // where that phase writes its prepared arena
     cudaEvent_t *events = nullptr;         // when set: 2 per op, recorded around every op that runs
+    bool *chain_ran = nullptr;             // when set: whether the product chain ran as one launch
+                                           // (its events are those of the chain's first op)
+    bool phases_only = false;              // run only the prepare phases that have to run
   };
 
   cudaError_t execute(const Program &p, DeviceTables &t, const ExecArgs &args);
+  // Where every buffer of the program lives for these arguments (inputs, output, prepared arenas,
+  // workspace offsets).
+  std::vector<char *> buffer_pointers(const Program &p, const ExecArgs &args);
 
   // The grouped GEMM of one op (gemm.cu): FP64 / complex128, or split precision with `slices`.
   // `tickets` is the workspace's ticket region (kTicketInts ints, zero, left zero).
   cudaError_t launch_gemm_f64(const Program &p, DeviceTables &t, size_t op_index, const void *A, const void *B, void *C,
                               bool complex, void *scratch, int *tickets, cudaStream_t stream);
   // `prepared`: the caller's prepared arenas (or null); a side read from one uses the slices cut
-  // into it by fill_slice_caches.
+  // into it by fill_slice_caches.  With `relabel` (chain_relabel) every entry of C is stored at its
+  // place after the program's chain move instead (C then being the move's destination).
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, int *tickets,
-                                const void *const *prepared, cudaStream_t stream);
+                                const void *const *prepared, cudaStream_t stream, const int32_t *relabel = nullptr);
+  // The device table of the program's chain move (chain.cu): per entry of the first product's
+  // result its place after the move, or -1; built on first use, null when the move does not write
+  // every entry the second product reads.
+  cudaError_t chain_relabel(const Program &p, DeviceTables &t, const int32_t **relabel);
   // Cut the slices of the GEMM operands that are operand `operand`'s prepared value into its arena.
   cudaError_t fill_slice_caches(const Program &p, DeviceTables &t, int32_t operand, const void *arena,
                                 cudaStream_t stream);
   void stage_gemm(const Program &p, DeviceTables &t, TableStaging &staging);
+  // The product chain of a program (Program::chain_*) in one FP64 launch (chain.cu): the first
+  // product A1 B1 lands in the moved layout `moved`, the second reads it as its A.  *used is false
+  // when the chain cannot run as one launch (then nothing is launched and the ops run one by one).
+  cudaError_t launch_chain_f64(const Program &p, DeviceTables &t, const double *A1, const double *B1, double *moved,
+                               const double *B2, double *C, void *workspace, cudaStream_t stream, bool *used);
+  // `count` programs' chains (one per window of a batch) as ONE FP64 launch: per program its operands,
+  // outputs and its own workspace (tickets at its head, scratch at p.scratch_offset).  *used is false
+  // when some program's chain cannot join (then nothing is launched).  The deal of all the programs'
+  // items is cached per list of programs (clear_chain_batches forgets them with the plans).
+  struct ChainBatchEntry
+  {
+    const Program *program;
+    DeviceTables *tables;
+    const double *a1, *b1, *b2;
+    double *moved, *c;
+    void *workspace;
+  };
+  cudaError_t launch_chain_batch(const std::vector<ChainBatchEntry> &entries, cudaStream_t stream, bool *used);
+  void clear_chain_batches();
+  // Split products on the tensor cores (split_tc.cu): whether an op's blocks fill its 128 x 64 tiles
+  // well enough, and the launch (slices and exponents as launch_gemm_split lays them out; `error`
+  // an int of the workspace's ticket region, raised when a wait gives up).
+  bool split_tc_suits(const Program &p, const Op &op, int32_t slices);
+  cudaError_t launch_split_tc(const Program &p, const Op &op, DeviceTables &t, size_t op_index, int32_t slices,
+                              const uint16_t *sa, const uint16_t *sb, const int16_t *exps_a, const int16_t *exps_b,
+                              int64_t stride_a, int64_t stride_b, const void *spairs, double *C, int *error,
+                              cudaStream_t stream);
   // The plain per-block form (per_block.cu): one cuBLAS call per block pair.
   cudaError_t launch_gemm_per_block(const Program &p, const Op &op, const void *A, const void *B, void *C, bool complex,
                                     cudaStream_t stream);

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <numeric>
 #include <cmath>
 #include <map>
@@ -19,6 +20,7 @@
 
 #include "executor.h"
 #include "gemm.h"
+#include "gemm_device.cuh"
 #include "launch.h"
 
 namespace ttg
@@ -346,6 +348,10 @@ namespace ttg
       // the split schedule itself is built on the first split launch (most plans never run one);
       // here only its scratch
       need = std::max(need, (f64_bytes(plans->f64[i]) + 7) / 8);
+      // a chain's one launch holds the partial tiles of both its products at once
+      if (static_cast<int32_t>(i) == p.chain_second)
+        need = std::max(need, (up256((plans->f64[static_cast<size_t>(p.chain_first)].slots + plans->f64[i].slots) *
+                                     kF64TileM * kF64TileN * 8) + 7) / 8);
       const SplitSchedule sizes = schedule_split(p, op, false);
       need = std::max(need, (split_bytes(sizes, kMaxSlices) + 7) / 8);
       // the slices of a prepared operand's value go into its arena
@@ -385,71 +391,12 @@ namespace ttg
 
   namespace
   {
-    struct DevBlock
-    {
-      int64_t c;
-      int32_t m, n, pair_begin, pair_count;
-    };
-    struct DevPair
-    {
-      int64_t a, b;
-      int32_t k, pad;
-    };
-    struct DevSplitPair
-    {
-      int64_t sa, sb;
-      int32_t kp, ea, eb, pad;
-    };
-
-    __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c)
-    {
-      c.x = fma(a.x, b.x, fma(-a.y, b.y, c.x));
-      c.y = fma(a.x, b.y, fma(a.y, b.x, c.y));
-      return c;
-    }
-    __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
-    __device__ __forceinline__ double2 fma_t(double2 a, double2 b, double2 c) { return cfma(a, b, c); }
-    template <typename T>
-    __device__ __forceinline__ T zero_t();
-    template <>
-    __device__ __forceinline__ double zero_t<double>() { return 0.0; }
-    template <>
-    __device__ __forceinline__ double2 zero_t<double2>() { return make_double2(0.0, 0.0); }
-    __device__ __forceinline__ double add_t(double a, double b) { return a + b; }
-    __device__ __forceinline__ double2 add_t(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-
-    // a barrier over one worker's 128 threads (named barrier 1 + worker)
-    __device__ __forceinline__ void worker_sync(int worker)
-    {
-      asm volatile("bar.sync %0, %1;\n" ::"r"(worker + 1), "r"(kWorkerThreads) : "memory");
-    }
-
-    // 8-byte asynchronous copy global -> shared; `in` false fills the destination with zeros and
-    // reads nothing
-    __device__ __forceinline__ void copy8(double *dst, const double *src, bool in)
-    {
-      const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(in ? 8 : 0) : "memory");
-    }
-    __device__ __forceinline__ void copy_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-    __device__ __forceinline__ void copy_wait_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
-    // The next entry of the CTA's own list for a worker.
-    __device__ __forceinline__ int64_t local_claim(int worker, int lt, int *slot, int *taken)
-    {
-      if (lt == 0) *slot = atomicAdd(taken, 1);
-      worker_sync(worker);
-      const int64_t idx = *slot;
-      worker_sync(worker);
-      return idx;
-    }
-
     // After a worker has written a partial tile: take the tile's ticket; the worker holding the last
     // ticket sums every partial of the tile in slot order into C.  The fences order the partial
     // writes before the ticket and the ticket before the reads (reads bypass L1).
     template <typename T, int BM, int BN>
     __device__ void finish_partial(int worker, int lt, int *flag, int *tickets, const GemmReduce *reduces, int reduce,
-                                   const DevBlock *blocks, const T *partial, T *C)
+                                   const DevBlock *blocks, const T *partial, T *C, const int32_t *relabel = nullptr)
     {
       __threadfence();
       worker_sync(worker);
@@ -492,10 +439,15 @@ namespace ttg
       {
         const int e = lt + k * kWorkerThreads;
         const int gm = r.m0 + e / BN, gn = r.n0 + e % BN;
-        if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = sum[k];
+        if (gm >= blk.m || gn >= blk.n) continue;
+        const int64_t at = blk.c + static_cast<int64_t>(gm) * blk.n + gn;
+        if (!relabel)
+          C[at] = sum[k];
+        else if (relabel[at] >= 0)
+          C[relabel[at]] = sum[k];  // straight to its place after the leg move that follows
       }
       const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (lt == 0 && r.m0 + BM >= blk.m && r.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
+      if (!relabel && lt == 0 && r.m0 + BM >= blk.m && r.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
     }
 
     // ---------------------------------------------------------------------------------------
@@ -605,17 +557,6 @@ namespace ttg
         const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
         if (lt == 0 && it.m0 + BM >= blk.m && it.n0 + BN >= blk.n && (entries & 1)) C[blk.c + entries] = zero_t<T>();
       }
-    }
-
-    // D = A B + D on a 16 x 8 x 8 FP64 fragment.  Lane l (g = l / 4, t = l % 4) holds A at rows
-    // g, g + 8 and columns t, t + 4 (a0: (g, t), a1: (g + 8, t), a2: (g, t + 4), a3: (g + 8, t + 4)),
-    // B at rows t, t + 4 of column g, and D at rows g (c0, c1) and g + 8 (c2, c3) of columns 2t, 2t + 1.
-    __device__ __forceinline__ void dmma16(double (&c)[4], const double (&a)[4], const double (&b)[2])
-    {
-      asm volatile("mma.sync.aligned.m16n8k8.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                   "{%0,%1,%2,%3};\n"
-                   : "+d"(c[0]), "+d"(c[1]), "+d"(c[2]), "+d"(c[3])
-                   : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(b[0]), "d"(b[1]));
     }
 
     // The float64 form of gemm_f64_kernel on the FP64 matrix instruction (mma m16n8k8 f64): each of
@@ -755,53 +696,6 @@ namespace ttg
     // split precision
     // ---------------------------------------------------------------------------------------
 
-    // FP64 runs at a sixty-fourth of the FP32 rate on this GPU, so the slicing works on the bits of
-    // the doubles with integer instructions.
-    //
-    // frexp's exponent of a non-negative double given by its bits: x = f 2^e with f in [0.5, 1)
-    // (0 for zero).
-    __device__ __forceinline__ int frexp_exponent(unsigned long long bits)
-    {
-      if (bits == 0) return 0;
-      const int field = static_cast<int>(bits >> 52);
-      if (field != 0) return field - 1022;
-      return (64 - __clzll(static_cast<long long>(bits))) - 1074;  // subnormal: bits * 2^-1074
-    }
-
-    // __double2ll_rn(ldexp(x, k)) for |x| < 2^(63 - k) on the bits of x: the significand shifted by
-    // the exponent, rounded to nearest with ties to even.
-    __device__ __forceinline__ long long scaled_integer(double x, int k)
-    {
-      const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(x));
-      const int field = static_cast<int>((bits >> 52) & 0x7ff);
-      unsigned long long mant = bits & 0xfffffffffffffull;
-      if (field != 0) mant |= 1ull << 52;
-      const int shift = (field != 0 ? field : 1) - 1075 + k;  // x 2^k = mant 2^shift
-      unsigned long long q;
-      if (mant == 0)
-        q = 0;
-      else if (shift >= 0)
-        q = mant << shift;
-      else if (shift < -62)
-        q = 0;
-      else
-      {
-        const int down = -shift;
-        q = mant >> down;
-        const unsigned long long rem = mant & ((1ull << down) - 1), half = 1ull << (down - 1);
-        if (rem > half || (rem == half && (q & 1ull))) ++q;
-      }
-      const long long v = static_cast<long long>(q);
-      return (bits >> 63) ? -v : v;
-    }
-
-    // 2^k as a double built from its bits (k in the normal range), else through ldexp
-    __device__ __forceinline__ double pow2(int k)
-    {
-      if (k > -1023 && k < 1024) return __longlong_as_double(static_cast<long long>(k + 1023) << 52);
-      return ldexp(1.0, k);
-    }
-
     // One warp per line (a row of A or a column of B), lines of A from `a` and lines of B from `b`:
     // the power of two 2^e that bounds the line, then each entry as the integer round(x 2^(56-e))
     // cut into `slices` balanced 7-bit digits (|q_1| <= 128, |q_t| <= 64 after it), exact in bf16,
@@ -882,34 +776,6 @@ namespace ttg
       }
     }
 
-    __device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
-    {
-      asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                   "{%0,%1,%2,%3};\n"
-                   : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                   : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-    }
-
-    __device__ __forceinline__ void ldmatrix_x4(uint32_t (&r)[4], const void *smem)
-    {
-      const uint32_t at = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-      asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                   : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                   : "r"(at));
-    }
-
-    // 16 bytes global -> shared; `bytes` 0 writes zeros and reads nothing
-    __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, int bytes)
-    {
-      const uint32_t at = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(at), "l"(gmem), "r"(bytes));
-    }
-    __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-    template <int N>
-    __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
-
-    constexpr int kRow = kSplitStepK + 8;  // shared row of 32 slice entries plus 8 of padding (80 bytes)
-
     template <int S>
     __host__ __device__ constexpr int split_worker_bytes() { return 2 * S * (kSplitTileM + kSplitTileN) * kRow * 2; }
 
@@ -926,7 +792,8 @@ namespace ttg
                         int64_t stride_b, double *__restrict__ C,
                         const DevBlock *__restrict__ blocks, const DevSplitPair *__restrict__ spairs,
                         const SplitItem *__restrict__ items, const int32_t *__restrict__ cta_begin, const GemmReduce *__restrict__ reduces,
-                        int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets)
+                        int64_t n_reduces, double *__restrict__ partial, int *__restrict__ tickets,
+                        const int32_t *__restrict__ relabel)
     {
       dependent_entry();
       extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1067,7 +934,7 @@ namespace ttg
             for (int q = 0; q < 4; ++q)
               out[(wm * 16 + g + (q >= 2 ? 8 : 0)) * kSplitTileN + wn * 16 + ns * 8 + tig * 2 + (q & 1)] = acc[ns][q];
           finish_partial<double, kSplitTileM, kSplitTileN>(worker, lt, flags + worker, tickets, reduces, it.reduce, blocks,
-                                                           partial, C);
+                                                           partial, C, relabel);
           continue;
         }
 #pragma unroll
@@ -1076,10 +943,16 @@ namespace ttg
           for (int q = 0; q < 4; ++q)
           {
             const int gm = r0 + (q >= 2 ? 8 : 0), gn = c0 + ns * 8 + (q & 1);
-            if (gm < blk.m && gn < blk.n) C[blk.c + static_cast<int64_t>(gm) * blk.n + gn] = acc[ns][q];
+            if (gm >= blk.m || gn >= blk.n) continue;
+            const int64_t at = blk.c + static_cast<int64_t>(gm) * blk.n + gn;
+            if (!relabel)
+              C[at] = acc[ns][q];
+            else if (relabel[at] >= 0)
+              C[relabel[at]] = acc[ns][q];  // straight to its place after the leg move that follows
           }
         const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-        if (lt == 0 && it.m0 + kSplitTileM >= blk.m && it.n0 + kSplitTileN >= blk.n && (entries & 1)) C[blk.c + entries] = 0.0;
+        if (!relabel && lt == 0 && it.m0 + kSplitTileM >= blk.m && it.n0 + kSplitTileN >= blk.n && (entries & 1))
+          C[blk.c + entries] = 0.0;
       }
     }
 
@@ -1100,7 +973,7 @@ namespace ttg
                                int64_t stride_a, int64_t stride_b, double *C, const DevBlock *blocks, const DevSplitPair *spairs,
                                const SplitItem *items, const int32_t *cta_begin, int32_t n_ctas, int64_t longest,
                                const GemmReduce *reduces, int64_t n_reduces, double *partial, int *tickets,
-                               cudaStream_t stream)
+                               const int32_t *relabel, cudaStream_t stream)
     {
       const int bytes = std::max(kSplitWorkers * split_worker_bytes<S>(), kPinBytes);
       static std::once_flag once;
@@ -1109,7 +982,8 @@ namespace ttg
       // one CTA per list the schedule dealt, as many workers as its longest list needs
       const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kSplitWorkers));
       return launch_dependent(gemm_split_kernel<S>, n_ctas, workers * kWorkerThreads, bytes, stream, sa, sb, exps_a, exps_b,
-                              stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets);
+                              stride_a, stride_b, C, blocks, spairs, items, cta_begin, reduces, n_reduces, partial, tickets,
+                              relabel);
     }
   } // namespace
 
@@ -1264,7 +1138,7 @@ namespace ttg
 
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, int *ticket_region,
-                                const void *const *prepared, cudaStream_t stream)
+                                const void *const *prepared, cudaStream_t stream, const int32_t *relabel)
   {
     cudaError_t e = ensure_split(p, op, t, op_index);
     if (e != cudaSuccess) return e;
@@ -1309,6 +1183,15 @@ namespace ttg
       }
     }
     if ((e = launch_lines(sched, A, B, sa, sb, exps_a, exps_b, begin, end, slices, stream)) != cudaSuccess) return e;
+    // large blocks: whole 128 x 64 tiles on the tensor cores (tcgen05), no partial tiles
+    static const bool tc_enabled = []
+    {
+      const char *v = std::getenv("TENTORCH_GB300_TCGEN05");
+      return !(v && v[0] == '0');
+    }();
+    if (tc_enabled && !relabel && split_tc_suits(p, op, slices))
+      return launch_split_tc(p, op, t, op_index, slices, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, sched.pairs,
+                             C, ticket_region + kTicketInts - 1, stream);
     const auto *blocks = reinterpret_cast<const DevBlock *>(t.blocks);
     const auto *spairs = reinterpret_cast<const DevSplitPair *>(sched.pairs);
     const auto *items = reinterpret_cast<const SplitItem *>(sched.items);
@@ -1318,7 +1201,7 @@ namespace ttg
   case S:                                                                                                               \
     e = launch_split_s<S>(sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, C, blocks, spairs, items,              \
                           sched.cta_begin, sched.n_ctas, sched.longest, sched.reduces, sched.n_reduces, partial, tickets,  \
-                          stream);                                                                                      \
+                          relabel, stream);                                                                             \
     break;
       TTG_SPLIT(1) TTG_SPLIT(2) TTG_SPLIT(3) TTG_SPLIT(4) TTG_SPLIT(5) TTG_SPLIT(6) TTG_SPLIT(7) TTG_SPLIT(8)
 #undef TTG_SPLIT
@@ -1333,6 +1216,7 @@ namespace ttg
   {
     t.gemm.assign(p.ops.size(), {});
     t.split.assign(p.ops.size(), {});
+    t.tc.assign(p.ops.size(), {});
     if (!p.gemm_plans) return;
     for (size_t i = 0; i < p.ops.size(); ++i)
     {

@@ -122,6 +122,22 @@ namespace ttg
   // launches need (partial tiles, tickets, slices).
   int64_t plan_gemms(Program &p);
 
+  // Find a product -> leg move -> product chain among the program's ops (Program::chain_*), from
+  // the ops alone; whether the move is a one-to-one relabelling is checked on its first launch.
+  void detect_chain(Program &p);
+  // One FP64 work item of a chain: stage 0 items belong to the first product (their results go to
+  // the moved layout), stage 1 items to the second (they start once every stage 0 tile is done).
+  struct ChainItem
+  {
+    int32_t stage, block, m0, n0, k0, k1, slot, reduce, window, pad;  // window: the program of a batched launch
+  };
+  struct ChainReduce
+  {
+    int32_t stage, block, m0, n0, slot0, nslots, pad0, pad1;
+  };
+  // Programs a batched chain launch takes at most (tt_plan_execute_batch).
+  constexpr int kChainBatch = 64;
+
   // The distinct left blocks (offset, rows, cols) and right blocks of one GEMM op.
   struct OperandBlock
   {

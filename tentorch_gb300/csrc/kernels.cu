@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -196,16 +197,18 @@ namespace ttg
   DeviceTables::~DeviceTables()
   {
     if (base) cudaFree(base);
+    if (chain.base) cudaFree(chain.base);
+    if (chain.relabel_base) cudaFree(chain.relabel_base);
+    for (TcTables &g : tc)
+      if (g.base) cudaFree(g.base);
     for (GemmTables &g : gemm)
       if (g.base) cudaFree(g.base);
     for (SplitTables &g : split)
       if (g.base) cudaFree(g.base);
   }
 
-  namespace
-  {
-    // A non-blocking stream per device for table uploads.
-    cudaError_t upload_stream(cudaStream_t *stream)
+  // A non-blocking stream per device for table uploads.
+  cudaError_t upload_stream(cudaStream_t *stream)
     {
       static std::mutex mutex;
       static std::map<int, cudaStream_t> streams;
@@ -223,7 +226,6 @@ namespace ttg
       *stream = found->second;
       return cudaSuccess;
     }
-  } // namespace
 
   cudaError_t TableStaging::commit(void **base)
   {
@@ -272,10 +274,8 @@ namespace ttg
   // executor
   // --------------------------------------------------------------------------------------------
 
-  cudaError_t execute(const Program &p, DeviceTables &t, const ExecArgs &args)
+  std::vector<char *> buffer_pointers(const Program &p, const ExecArgs &args)
   {
-    cudaError_t e = t.ensure(p);
-    if (e != cudaSuccess) return e;
     const size_t esize = args.complex ? 16 : 8;
     std::vector<char *> ptr(p.buffers.size(), nullptr);
     for (size_t i = 0; i < p.buffers.size(); ++i)
@@ -292,15 +292,29 @@ namespace ttg
     }
     if (args.only_phase >= 0 && args.prepared_out)
       ptr[static_cast<size_t>(p.prepared[static_cast<size_t>(args.only_phase)])] = static_cast<char *>(args.prepared_out);
-    for (size_t i = 0; i < p.ops.size(); ++i)
+    return ptr;
+  }
+
+  cudaError_t execute(const Program &p, DeviceTables &t, const ExecArgs &args)
+  {
+    cudaError_t e = t.ensure(p);
+    if (e != cudaSuccess) return e;
+    const size_t esize = args.complex ? 16 : 8;
+    const std::vector<char *> ptr = buffer_pointers(p, args);
+    // whether op i runs in this execution: a prepare-only call runs its operand's phase; otherwise
+    // the ops of a phase whose prepared arena the caller holds are skipped (and with phases_only
+    // only the phases run)
+    const auto runs_now = [&](size_t i)
     {
       const Op &op = p.ops[i];
-      if (args.only_phase >= 0)
-      {
-        if (op.phase != args.only_phase) continue;
-      }
-      else if (op.phase >= 0 && args.prepared && args.prepared[op.phase])
-        continue;  // the caller holds this operand's prepared arena
+      if (args.only_phase >= 0) return op.phase == args.only_phase;
+      if (args.phases_only && op.phase < 0) return false;
+      return !(op.phase >= 0 && args.prepared && args.prepared[op.phase]);
+    };
+    const auto run_op = [&](size_t i) -> cudaError_t
+    {
+      const Op &op = p.ops[i];
+      cudaError_t e = cudaSuccess;
       if (args.events)
       {
         e = cudaEventRecord(args.events[2 * i], args.stream);
@@ -381,11 +395,75 @@ namespace ttg
       }
       }
       if (e != cudaSuccess) return e;
-      if (args.events)
+      if (args.events) e = cudaEventRecord(args.events[2 * i + 1], args.stream);
+      return e;
+    };
+    // the product chain (chain.cu): in FP64 one launch for both products and the move between them;
+    // in split precision the first product stores through the move's relabelling (float64 arenas,
+    // full executions only)
+    static const bool chain_enabled = []
+    {
+      const char *v = std::getenv("TENTORCH_GB300_CHAIN");
+      return !(v && v[0] == '0');
+    }();
+    const bool chain = chain_enabled && p.chain_first >= 0 && args.only_phase < 0 && !args.phases_only && !args.complex &&
+                       args.precision >= 0;
+    std::vector<char> done(p.ops.size(), 0);
+    if (args.chain_ran) *args.chain_ran = false;
+    for (size_t i = 0; i < p.ops.size(); ++i)
+    {
+      if (done[i] || !runs_now(i)) continue;
+      if (chain && static_cast<int32_t>(i) == p.chain_first)
       {
-        e = cudaEventRecord(args.events[2 * i + 1], args.stream);
+        // ops between the move and the second product prepare other operands: run them first
+        for (size_t j = static_cast<size_t>(p.chain_move) + 1; j < static_cast<size_t>(p.chain_second); ++j)
+          if (runs_now(j))
+          {
+            if ((e = run_op(j)) != cudaSuccess) return e;
+            done[j] = 1;
+          }
+        const Op &first = p.ops[i], &move = p.ops[static_cast<size_t>(p.chain_move)],
+                 &second = p.ops[static_cast<size_t>(p.chain_second)];
+        if (args.precision > 0)
+        {
+          // split products: the first one stores its result at its places after the move, which
+          // then does not run; the second product runs in its turn
+          const int32_t *relabel = nullptr;
+          if ((e = chain_relabel(p, t, &relabel)) != cudaSuccess) return e;
+          if (relabel)
+          {
+            if (args.events && (e = cudaEventRecord(args.events[2 * i], args.stream)) != cudaSuccess) return e;
+            e = launch_gemm_split(p, first, t, i, reinterpret_cast<const double *>(ptr[static_cast<size_t>(first.src)]),
+                                  reinterpret_cast<const double *>(ptr[static_cast<size_t>(first.src2)]),
+                                  reinterpret_cast<double *>(ptr[static_cast<size_t>(move.dst)]), args.precision,
+                                  static_cast<char *>(args.workspace) + p.scratch_offset * esize,
+                                  static_cast<int *>(args.workspace), args.prepared, args.stream, relabel);
+            if (e != cudaSuccess) return e;
+            if (args.events && (e = cudaEventRecord(args.events[2 * i + 1], args.stream)) != cudaSuccess) return e;
+            done[static_cast<size_t>(p.chain_move)] = 1;
+            continue;
+          }
+          if ((e = run_op(i)) != cudaSuccess) return e;
+          continue;
+        }
+        if (args.events && (e = cudaEventRecord(args.events[2 * i], args.stream)) != cudaSuccess) return e;
+        bool used = false;
+        e = launch_chain_f64(p, t, reinterpret_cast<const double *>(ptr[static_cast<size_t>(first.src)]),
+                             reinterpret_cast<const double *>(ptr[static_cast<size_t>(first.src2)]),
+                             reinterpret_cast<double *>(ptr[static_cast<size_t>(move.dst)]),
+                             reinterpret_cast<const double *>(ptr[static_cast<size_t>(second.src2)]),
+                             reinterpret_cast<double *>(ptr[static_cast<size_t>(second.dst)]), args.workspace,
+                             args.stream, &used);
         if (e != cudaSuccess) return e;
+        if (used)
+        {
+          if (args.events && (e = cudaEventRecord(args.events[2 * i + 1], args.stream)) != cudaSuccess) return e;
+          done[static_cast<size_t>(p.chain_move)] = done[static_cast<size_t>(p.chain_second)] = 1;
+          if (args.chain_ran) *args.chain_ran = true;
+          continue;
+        }
       }
+      if ((e = run_op(i)) != cudaSuccess) return e;
     }
     return cudaSuccess;
   }

@@ -844,6 +844,7 @@ namespace ttg
         p.workspace += kTicketElements;
       }
       p.scratch_offset = p.workspace;
+      detect_chain(p);
       p.workspace += plan_gemms(p);
       validate(p);
     }
@@ -1034,6 +1035,33 @@ namespace ttg
 
     constexpr int64_t kMaxCharges = 4096;
   } // namespace
+
+  std::vector<int32_t> expand_move(const Program &p, const Op &op)
+  {
+    if (op.kind == OpKind::gather)
+      return std::vector<int32_t>(p.gather_index.begin() + op.begin, p.gather_index.begin() + op.begin + op.count);
+    if (op.kind != OpKind::tiles) throw InvalidArgument("an operation that is neither a gather nor tiles");
+    std::vector<int32_t> index(static_cast<size_t>(op.elements), -1);
+    for (int64_t c = op.begin; c < op.begin + op.count; ++c)
+    {
+      const TileChunk &ch = p.tile_chunks[static_cast<size_t>(c)];
+      const Tile &t = p.tiles[static_cast<size_t>(ch.tile)];
+      if (t.in_base < 0) continue;  // a zero pad entry
+      for (int32_t r = ch.row0; r < ch.row0 + ch.nrows; ++r)
+        for (int32_t col = 0; col < t.cols; ++col)
+        {
+          // mixed radix over the copies of the row legs, then of the column legs, the last fastest
+          int64_t in = t.in_base;
+          int32_t rest = r;
+          for (int32_t l = t.n_row - 1; l >= 0; --l) in += static_cast<int64_t>(rest % t.extent[l]) * t.stride[l], rest /= t.extent[l];
+          rest = col;
+          for (int32_t l = t.n_row + t.n_col - 1; l >= t.n_row; --l)
+            in += static_cast<int64_t>(rest % t.extent[l]) * t.stride[l], rest /= t.extent[l];
+          index[static_cast<size_t>(t.out_base + static_cast<int64_t>(r) * t.out_ld + col)] = static_cast<int32_t>(in);
+        }
+    }
+    return index;
+  }
 
   std::shared_ptr<Program> compile_conj(Space space)
   {

@@ -134,6 +134,11 @@ namespace ttg
     int64_t scratch_offset = 0;  // elements: GEMM scratch (partial tiles, slices) at the end of the workspace
     int32_t ctas = 152;          // CTAs of its persistent GEMM launches: the SMs of the device it was compiled for
     std::vector<int32_t> fold;   // an einsum's operands in the order it folds them (empty for other plans)
+    // A product whose result only a leg move with unit coefficients reads, whose result in turn only
+    // the A side of a second product reads (the two-site matvec): in FP64 the three ops run as one
+    // launch, in split precision the first product stores through the move (chain.cu).  Ops between
+    // the move and the second product belong to prepare phases.
+    int32_t chain_first = -1, chain_move = -1, chain_second = -1;
     // per operand: the buffer holding its prepared value (the input itself when no op prepares it)
     std::vector<int32_t> prepared;
     // descriptor tables
@@ -151,6 +156,10 @@ namespace ttg
     int64_t moved_elements = 0;
     bool complex_coefficients = false;  // some RUNS term has an imaginary part
   };
+
+  // The entry-by-entry index a TILES or GATHER op amounts to: output entry i reads input entry
+  // index[i], -1 where it writes zero (op.elements entries).
+  std::vector<int32_t> expand_move(const Program &p, const Op &op);
 
   // Compile the conjugate-transpose of a tensor (its bra): every block (r, s, c) becomes block
   // (s, r, c) of the space with codomain and domain swapped and the dual charge, transposed and,

@@ -131,6 +131,7 @@ def clear_plans() -> None:
     _plans.clear()
     _prepared.clear()
     _pools.clear()
+    _batch_pools.clear()
     _superseded.clear()
     check(lib.tt_plan_cache_clear())
 
@@ -297,6 +298,56 @@ def einsum(spec: str, *tensors: Tensor, **options) -> Tensor:
     plan = _plan(('einsum', spec, tuple(t._space.id for t in tensors), has, q),
                  lambda out: lib.tt_plan_einsum(spec.encode(), n, ids, int(has), q, out), cat)
     return run(plan, list(tensors))
+
+
+# per (device, stream, dtype, window): the workspace of one window of a batch (a batch's windows run
+# together, so each needs its own)
+_batch_pools = {}
+# launches of block products the last einsum_batch made (1 when its windows ran as one launch)
+last_batch_launches = 0
+
+
+def einsum_batch(spec: str, operand_lists, outcharge = None) -> list:
+    '''`[einsum(spec, *ops) for ops in operand_lists]` as one call (tt_plan_execute_batch): in FP64
+    the two-site matvecs of many windows (different bond dimensions allowed) run as ONE persistent
+    launch with their work items dealt together over the SMs; in split precision, or for equations
+    that are not a product chain, one window after another.  At most 64 windows per launch (longer
+    lists are cut into launches of 64).  Operands are prepared per window as `einsum` prepares them.'''
+    global last_batch_launches
+    operand_lists = [list(ops) for ops in operand_lists]
+    if len(operand_lists) > 64:
+        return einsum_batch(spec, operand_lists[:64], outcharge) + einsum_batch(spec, operand_lists[64:], outcharge)
+    if not operand_lists:
+        return []
+    first = operand_lists[0][0]
+    device, dtype = first._data.device, first._data.dtype
+    stream = torch.cuda.current_stream(device).cuda_stream
+    handles, outs, keep, inputs, prepared, workspaces = [], [], [], [], [], []
+    for w, ops in enumerate(operand_lists):
+        _check_device(ops)
+        plan = plan_of(spec, *ops, outcharge = outcharge)
+        key = (device.index, stream, dtype, w)
+        pool = _batch_pools.get(key)
+        if pool is None or pool.numel() < plan.workspace:
+            if pool is not None and _captured:
+                _superseded.append(pool)
+            pool = _batch_pools[key] = torch.zeros(max(plan.workspace, 1 << 16), dtype = dtype, device = device)
+        prep = [_prepared_arena(plan, i, t, pool, stream) for i, t in enumerate(ops)]
+        out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = dtype, device = device))
+        handles.append(plan.handle.value)
+        outs.append(out)
+        ins = pointers(t._data.data_ptr() for t in ops)
+        pre = pointers((p.data_ptr() if p is not None else None) for p in prep)
+        keep += [ins, pre, prep]
+        inputs.append(ctypes.cast(ins, vp).value)
+        prepared.append(ctypes.cast(pre, vp).value)
+        workspaces.append(pool.data_ptr())
+    launched = i32()
+    check(lib.tt_plan_execute_batch(len(handles), pointers(handles), _DTYPE[dtype], _precision, pointers(inputs),
+                                    pointers(prepared), pointers(o._data.data_ptr() for o in outs),
+                                    pointers(workspaces), stream, ctypes.byref(launched)))
+    last_batch_launches = launched.value
+    return outs
 
 
 def plan_of(spec: str, *tensors: Tensor, outcharge = None) -> Plan:
