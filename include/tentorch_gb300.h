@@ -183,7 +183,7 @@ int32_t tt_chain(int32_t space, int32_t nabove, const int32_t *above, int32_t nb
 int32_t tt_lanczos_scratch(int64_t n, int32_t n_iter, int32_t dtype, int64_t *doubles);
 /* The lowest eigenpair of the Hermitian action v -> plan(inputs with v as operand `vector_operand`)
  * by n_iter Krylov steps from `start` with full reorthogonalisation, all on `stream` with one host
- * synchronisation at the end: *energy is the lowest Ritz value, `result` the normalised Ritz vector
+ * synchronisation at the end (to read the energy and the size): *energy is the lowest Ritz value, `result` the normalised Ritz vector
  * and *size the Krylov dimension used (the steps before the first norm below `tol`, as the
  * reference stops).  The plan's output space must be the vector operand's space.  `prepared` as
  * for tt_plan_execute; `workspace` the plan's workspace; `scratch` tt_lanczos_scratch doubles. */
@@ -191,6 +191,14 @@ int32_t tt_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const 
                    const void *const *prepared, int32_t vector_operand, const void *start, int32_t n_iter,
                    double tol, void *workspace, void *scratch, void *result, double *energy, int32_t *size,
                    void *stream);
+/* The same with no host wait at all (the tridiagonal's eigenpair is solved on the device): `energy`
+ * and `size` are DEVICE pointers written on `stream`, like `result`.  The reference reads a norm and
+ * inner products with .item() at every step (tentorch/linalg/lanczos.py:36-64,
+ * tentorch/linalg/graded/compare.cpp:41). */
+int32_t tt_lanczos_async(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                         const void *const *prepared, int32_t vector_operand, const void *start, int32_t n_iter,
+                         double tol, void *workspace, void *scratch, void *result, double *energy, int32_t *size,
+                         void *stream);
 
 /* ---- truncating splittings (tentorch/linalg/graded/svd.cpp:41-177) -------------------------- */
 

@@ -707,39 +707,77 @@ extern "C"
     });
   }
 
+  namespace
+  {
+    // The checks and the Krylov loop of tt_lanczos / tt_lanczos_async.
+    int32_t run_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                        const void *const *prepared, int32_t vector_operand, const void *start, int32_t n_iter,
+                        double tol, void *workspace, void *scratch, void *result, double *energy_dev, int32_t *size_dev,
+                        void *stream)
+    {
+      if (!plan) return fail(TT_EINVAL, "no plan");
+      if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128) return fail(TT_EINVAL, "unknown dtype");
+      if (precision < TT_PRECISION_PER_BLOCK || precision > 8)
+        return fail(TT_EINVAL, "precision is 0 (FP64), 1..8 slices, or -1 (per-block FP64)");
+      if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
+        return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
+      if (n_iter < 1 || n_iter > 60) return fail(TT_EINVAL, "Lanczos takes 1 to 60 steps");
+      const ttg::Program &p = *plan->program;
+      if (vector_operand < 0 || vector_operand >= p.n_inputs) return fail(TT_ERANGE, "no such operand");
+      if (p.input_spaces[static_cast<size_t>(vector_operand)] != p.output_space)
+        return fail(TT_EINVAL, "the action has to map the vector's space to itself");
+      if (start == nullptr || result == nullptr || scratch == nullptr) return fail(TT_EINVAL, "a missing arena");
+      ttg::ExecArgs args;
+      args.complex = dtype == TT_DTYPE_COMPLEX128;
+      args.precision = precision;
+      args.inputs = inputs;
+      args.prepared = prepared;
+      args.workspace = workspace;
+      args.stream = static_cast<cudaStream_t>(stream);
+      cudaError_t e = plan->tables->ensure(p);
+      if (e == cudaSuccess)
+      {
+        const int64_t n = p.output_space->size * (args.complex ? 2 : 1);
+        double *slot = ttg::lanczos_energy_slot(static_cast<double *>(scratch), n, n_iter);
+        e = ttg::lanczos(p, *plan->tables, args, vector_operand, static_cast<const double *>(start), n, n_iter, tol,
+                         static_cast<double *>(scratch), static_cast<double *>(result), energy_dev ? energy_dev : slot,
+                         size_dev ? size_dev : reinterpret_cast<int32_t *>(slot + 1));
+      }
+      if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+      return TT_OK;
+    }
+  } // namespace
+
   int32_t tt_lanczos(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                      const void *const *prepared, int32_t vector_operand, const void *start, int32_t n_iter,
                      double tol, void *workspace, void *scratch, void *result, double *energy, int32_t *size,
                      void *stream)
   {
-    if (!plan) return fail(TT_EINVAL, "no plan");
-    if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128) return fail(TT_EINVAL, "unknown dtype");
-    if (precision < TT_PRECISION_PER_BLOCK || precision > 8)
-      return fail(TT_EINVAL, "precision is 0 (FP64), 1..8 slices, or -1 (per-block FP64)");
-    if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
-      return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
-    if (n_iter < 1 || n_iter > 60) return fail(TT_EINVAL, "Lanczos takes 1 to 60 steps");
+    const int32_t status = run_lanczos(plan, dtype, precision, inputs, prepared, vector_operand, start, n_iter, tol,
+                                       workspace, scratch, result, nullptr, nullptr, stream);
+    if (status != TT_OK) return status;
+    // the energy and the size from their place in the scratch, after the stream's work
     const ttg::Program &p = *plan->program;
-    if (vector_operand < 0 || vector_operand >= p.n_inputs) return fail(TT_ERANGE, "no such operand");
-    if (p.input_spaces[static_cast<size_t>(vector_operand)] != p.output_space)
-      return fail(TT_EINVAL, "the action has to map the vector's space to itself");
-    if (start == nullptr || result == nullptr || scratch == nullptr) return fail(TT_EINVAL, "a missing arena");
-    ttg::ExecArgs args;
-    args.complex = dtype == TT_DTYPE_COMPLEX128;
-    args.precision = precision;
-    args.inputs = inputs;
-    args.prepared = prepared;
-    args.workspace = workspace;
-    args.stream = static_cast<cudaStream_t>(stream);
-    cudaError_t e = plan->tables->ensure(p);
-    if (e == cudaSuccess)
-    {
-      const int64_t n = p.output_space->size * (args.complex ? 2 : 1);
-      e = ttg::lanczos(p, *plan->tables, args, vector_operand, static_cast<const double *>(start), n, n_iter, tol,
-                       static_cast<double *>(scratch), static_cast<double *>(result), energy, size);
-    }
+    const int64_t n = p.output_space->size * (dtype == TT_DTYPE_COMPLEX128 ? 2 : 1);
+    double found[2];
+    const double *slot = ttg::lanczos_energy_slot(static_cast<double *>(scratch), n, n_iter);
+    cudaError_t e = cudaMemcpyAsync(found, slot, sizeof(found), cudaMemcpyDeviceToHost, static_cast<cudaStream_t>(stream));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    *energy = found[0];
+    std::memcpy(size, &found[1], sizeof(int32_t));
     return TT_OK;
+  }
+
+  int32_t tt_lanczos_async(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                           const void *const *prepared, int32_t vector_operand, const void *start, int32_t n_iter,
+                           double tol, void *workspace, void *scratch, void *result, double *energy, int32_t *size,
+                           void *stream)
+  {
+    if (energy == nullptr || size == nullptr)
+      return fail(TT_EINVAL, "tt_lanczos_async writes its energy and size to device memory");
+    return run_lanczos(plan, dtype, precision, inputs, prepared, vector_operand, start, n_iter, tol, workspace, scratch,
+                       result, energy, size, stream);
   }
 
   int32_t tt_svd_workspace(int32_t count, const int64_t *shapes, int64_t *offsets, int64_t *total)

@@ -199,11 +199,14 @@ namespace ttg
 
   // The Lanczos loop of a window (lanczos.cu): `base` carries the plan's operands (the vector
   // operand's pointer is replaced by each basis vector), prepared arenas and workspace; scratch holds
-  // lanczos_scratch_doubles() doubles; the normalised Ritz vector goes to `result`.
+  // lanczos_scratch_doubles() doubles; the normalised Ritz vector goes to `result`, the lowest Ritz
+  // value to *energy_dev and the Krylov size to *size_dev (device memory), all on base.stream with no
+  // host wait.  lanczos_energy_slot() is a place for both in the scratch (the energy, then the size).
   int64_t lanczos_scratch_doubles(int64_t n_doubles, int32_t n_iter);
   cudaError_t lanczos(const Program &p, DeviceTables &t, const ExecArgs &base, int32_t vector_operand,
                       const double *start, int64_t n_doubles, int32_t n_iter, double tol, double *scratch,
-                      double *result, double *energy, int32_t *size_out);
+                      double *result, double *energy_dev, int32_t *size_dev);
+  double *lanczos_energy_slot(double *scratch, int64_t n_doubles, int32_t n_iter);
 
   constexpr int kDotParts = 120;
   // out[2j], out[2j+1] = re, im of <a_j, b> for j < count; partial holds 2*kDotParts*count doubles.

@@ -2,9 +2,10 @@
 // device work: every Krylov step executes the window's compiled einsum on the current basis vector,
 // projects the image against the whole basis three times (the first projection holds alpha and
 // replaces the three-term step; then the reference's two full reorthogonalisation passes), takes
-// its norm and scales it into the next basis vector, with no host synchronisation.  The host reads
-// the tridiagonal once at the end, applies the reference's early stop (a beta below `tol` ends the
-// space), solves the small eigenproblem and the device forms the normalised Ritz vector.
+// its norm and scales it into the next basis vector, with no host synchronisation.  The device
+// then applies the reference's early stop (a beta below `tol` ends the space), solves the small
+// eigenproblem and forms the normalised Ritz vector: the whole call is stream-ordered work with no
+// host wait, and its energy and Krylov size stay in device memory until the caller reads them.
 //
 // Per step that is the plan's launches plus ten small ones issued from C++, so the CPU stays ahead
 // of the GPU; the same loop driven from Python spends more time launching than the GPU computing.
@@ -21,11 +22,15 @@ namespace ttg
 {
   namespace
   {
-    // table[j] = basis + j * n_doubles
-    __global__ void rows_kernel(const double **table, const double *basis, int64_t n_doubles, int32_t count)
+    // table[j] = basis + j * n_doubles for j < count, then the image, the start vector and the result
+    __global__ void rows_kernel(const double **table, const double *basis, int64_t n_doubles, int32_t count,
+                                const double *image, const double *start, const double *result)
     {
       const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
       if (j < count) table[j] = basis + j * n_doubles;
+      if (j == count) table[j] = image;
+      if (j == count + 1) table[j] = start;
+      if (j == count + 2) table[j] = result;
     }
 
     // dst = src / sqrt(norm2[0]) (norm2 the real part of <src, src>); beta_out (optional) = sqrt
@@ -72,63 +77,118 @@ namespace ttg
 
     __global__ void save_kernel(double *dst, const double *src) { *dst = *src; }
 
-    // out = sum_j c_j basis_j with real c_j
-    __global__ void combine_kernel(double *out, const double *basis, int64_t n_doubles, int32_t count, const double *c)
+    // out = sum_j c_j basis_j with real c_j, j < *count
+    __global__ void combine_kernel(double *out, const double *basis, int64_t n_doubles, const int32_t *count, const double *c)
     {
+      const int32_t used = *count;
       for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n_doubles;
            i += static_cast<int64_t>(gridDim.x) * blockDim.x)
       {
         double v = 0.0;
-        for (int32_t j = 0; j < count; ++j) v = fma(c[j], basis[j * n_doubles + i], v);
+        for (int32_t j = 0; j < used; ++j) v = fma(c[j], basis[j * n_doubles + i], v);
         out[i] = v;
       }
     }
 
-    int grid_of(int64_t n_doubles) { return static_cast<int>(std::clamp<int64_t>((n_doubles + 255) / 256, 1, device_sms() * 8)); }
-
-    // Eigenpairs of a small symmetric matrix by cyclic Jacobi rotations (C. G. J. Jacobi, 1846; the
-    // rotation as in Golub & Van Loan, "Matrix Computations", the symmetric Schur decomposition):
-    // `a` (n x n, row-major) is overwritten, `v` receives the eigenvectors as columns.
-    void jacobi_eigen(std::vector<double> &a, std::vector<double> &v, int n)
+    // The Krylov space's lowest Ritz pair on the device, one warp: the size of the space (the steps
+    // before the first beta below `tol`, as the reference stops), the tridiagonal's eigenpairs by
+    // cyclic Jacobi rotations (C. G. J. Jacobi, 1846; the rotation as in Golub & Van Loan, "Matrix
+    // Computations", the symmetric Schur decomposition; each rotation's parameters by one lane, its
+    // row and column updates over the lanes), the lowest eigenvalue and its eigenvector.  Products
+    // and sums are rounded one by one (no fused multiply-add), as the host arithmetic of x86 does.
+    __global__ void ritz_kernel(const double *tri, int32_t n_iter, double tol, double *ritz, double *energy,
+                                int32_t *size_out)
     {
-      v.assign(static_cast<size_t>(n) * n, 0.0);
-      for (int i = 0; i < n; ++i) v[static_cast<size_t>(i) * n + i] = 1.0;
+      extern __shared__ double work[];
+      __shared__ double rot[2];
+      __shared__ int32_t shared_size;
+      const int lane = threadIdx.x;
+      if (lane == 0)
+      {
+        int32_t size = n_iter;
+        for (int32_t k = 0; k < n_iter; ++k)
+          if (tri[n_iter + k] < tol)
+          {
+            size = k + 1;
+            break;
+          }
+        shared_size = size;
+      }
+      __syncwarp();
+      const int n = shared_size;
+      double *a = work, *v = work + n * n;
+      for (int i = lane; i < n * n; i += 32)
+      {
+        const int r = i / n, c = i % n;
+        a[i] = r == c ? tri[r] : (c == r + 1 ? tri[n_iter + r] : (r == c + 1 ? tri[n_iter + c] : 0.0));
+        v[i] = r == c ? 1.0 : 0.0;
+      }
+      __syncwarp();
       for (int sweep = 0; sweep < 100; ++sweep)
       {
-        double off = 0.0;
-        for (int p = 0; p < n; ++p)
-          for (int q = p + 1; q < n; ++q) off += a[static_cast<size_t>(p) * n + q] * a[static_cast<size_t>(p) * n + q];
-        if (off == 0.0) break;
+        if (lane == 0)
+        {
+          double off = 0.0;
+          for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) off = __dadd_rn(off, __dmul_rn(a[p * n + q], a[p * n + q]));
+          rot[0] = off;
+        }
+        __syncwarp();
+        if (rot[0] == 0.0) break;
         for (int p = 0; p < n; ++p)
           for (int q = p + 1; q < n; ++q)
           {
-            const double apq = a[static_cast<size_t>(p) * n + q];
+            const double apq = a[p * n + q];
+            __syncwarp();
             if (apq == 0.0) continue;
-            const double app = a[static_cast<size_t>(p) * n + p], aqq = a[static_cast<size_t>(q) * n + q];
-            const double tau = (aqq - app) / (2.0 * apq);
-            const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
-            const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
-            for (int k = 0; k < n; ++k)
+            if (lane == 0)
             {
-              const double akp = a[static_cast<size_t>(k) * n + p], akq = a[static_cast<size_t>(k) * n + q];
-              a[static_cast<size_t>(k) * n + p] = c * akp - s * akq;
-              a[static_cast<size_t>(k) * n + q] = s * akp + c * akq;
+              const double app = a[p * n + p], aqq = a[q * n + q];
+              const double tau = __ddiv_rn(__dsub_rn(aqq, app), __dmul_rn(2.0, apq));
+              const double t = __ddiv_rn(tau >= 0 ? 1.0 : -1.0, __dadd_rn(fabs(tau), __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(tau, tau)))));
+              const double c = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(t, t))));
+              rot[0] = c;
+              rot[1] = __dmul_rn(t, c);
             }
-            for (int k = 0; k < n; ++k)
+            __syncwarp();
+            const double c = rot[0], s = rot[1];
+            for (int k = lane; k < n; k += 32)
             {
-              const double apk = a[static_cast<size_t>(p) * n + k], aqk = a[static_cast<size_t>(q) * n + k];
-              a[static_cast<size_t>(p) * n + k] = c * apk - s * aqk;
-              a[static_cast<size_t>(q) * n + k] = s * apk + c * aqk;
+              const double akp = a[k * n + p], akq = a[k * n + q];
+              a[k * n + p] = __dsub_rn(__dmul_rn(c, akp), __dmul_rn(s, akq));
+              a[k * n + q] = __dadd_rn(__dmul_rn(s, akp), __dmul_rn(c, akq));
             }
-            for (int k = 0; k < n; ++k)
+            __syncwarp();
+            for (int k = lane; k < n; k += 32)
             {
-              const double vkp = v[static_cast<size_t>(k) * n + p], vkq = v[static_cast<size_t>(k) * n + q];
-              v[static_cast<size_t>(k) * n + p] = c * vkp - s * vkq;
-              v[static_cast<size_t>(k) * n + q] = s * vkp + c * vkq;
+              const double apk = a[p * n + k], aqk = a[q * n + k];
+              a[p * n + k] = __dsub_rn(__dmul_rn(c, apk), __dmul_rn(s, aqk));
+              a[q * n + k] = __dadd_rn(__dmul_rn(s, apk), __dmul_rn(c, aqk));
             }
+            for (int k = lane; k < n; k += 32)
+            {
+              const double vkp = v[k * n + p], vkq = v[k * n + q];
+              v[k * n + p] = __dsub_rn(__dmul_rn(c, vkp), __dmul_rn(s, vkq));
+              v[k * n + q] = __dadd_rn(__dmul_rn(s, vkp), __dmul_rn(c, vkq));
+            }
+            __syncwarp();
           }
       }
+      if (lane == 0)
+      {
+        int lowest = 0;
+        for (int k = 1; k < n; ++k)
+          if (a[k * n + k] < a[lowest * n + lowest]) lowest = k;
+        *energy = a[lowest * n + lowest];
+        *size_out = n;
+        shared_size = lowest;
+      }
+      __syncwarp();
+      for (int k = lane; k < n; k += 32) ritz[k] = v[k * n + shared_size];
     }
+
+    int grid_of(int64_t n_doubles) { return static_cast<int>(std::clamp<int64_t>((n_doubles + 255) / 256, 1, device_sms() * 8)); }
+
   } // namespace
 
   namespace
@@ -139,14 +199,15 @@ namespace ttg
   int64_t lanczos_scratch_doubles(int64_t n_doubles, int32_t n_iter)
   {
     const int64_t rows = n_iter + 1;
-    // basis, image, dot partials, coefficients, alpha and beta, Ritz coefficients, pointer table
+    // basis, image, dot partials, coefficients, alpha and beta, Ritz coefficients with the energy and
+    // the size after them, pointer table
     return up32(rows * n_doubles) + up32(n_doubles) + up32(2 * kDotParts * rows) + up32(2 * rows) + up32(2 * rows) +
-           up32(rows) + up32(rows + 3);
+           up32(rows + 2) + up32(rows + 3);
   }
 
   cudaError_t lanczos(const Program &p, DeviceTables &t, const ExecArgs &base, int32_t vector_operand,
                       const double *start, int64_t n_doubles, int32_t n_iter, double tol, double *scratch,
-                      double *result, double *energy, int32_t *size_out)
+                      double *result, double *energy_dev, int32_t *size_dev)
   {
     const bool complex = base.complex;
     const int64_t rows = n_iter + 1;
@@ -156,16 +217,14 @@ namespace ttg
     double *coeffs = partial + up32(2 * kDotParts * rows);
     double *tri = coeffs + up32(2 * rows);  // alpha[0..n_iter), beta[n_iter..2 n_iter)
     double *ritz = tri + up32(2 * rows);
-    const double **table = reinterpret_cast<const double **>(ritz + up32(rows));
+    const double **table = reinterpret_cast<const double **>(ritz + up32(rows + 2));
     // table[j] = basis row j (j < rows), then the image, the start vector and the result
     const double *const *image_slot = table + rows, *const *start_slot = table + rows + 1,
                         *const *result_slot = table + rows + 2;
     cudaStream_t stream = base.stream;
     const int grid = grid_of(n_doubles);
     cudaError_t e;
-    rows_kernel<<<1, 64, 0, stream>>>(table, basis, n_doubles, static_cast<int32_t>(rows));
-    const double *extra[3] = {image, start, result};
-    if ((e = cudaMemcpyAsync(table + rows, extra, sizeof(extra), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+    rows_kernel<<<1, 128, 0, stream>>>(table, basis, n_doubles, static_cast<int32_t>(rows), image, start, result);
     // basis[0] = start / |start|
     if ((e = arena_dots(start_slot, 1, start, n_doubles, complex, partial, coeffs, stream)) != cudaSuccess) return e;
     scale_kernel<<<grid, 256, 0, stream>>>(basis, start, n_doubles, coeffs, nullptr);
@@ -191,37 +250,24 @@ namespace ttg
       scale_kernel<<<grid, 256, 0, stream>>>(row + n_doubles, image, n_doubles, coeffs, tri + n_iter + k);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    std::vector<double> host(static_cast<size_t>(2 * n_iter));
-    if ((e = cudaMemcpyAsync(host.data(), tri, host.size() * 8, cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
-    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
-    // the reference stops at the first beta below tol; the steps computed after it are dropped
-    int size = n_iter;
-    for (int k = 0; k < n_iter; ++k)
-      if (host[static_cast<size_t>(n_iter + k)] < tol)
-      {
-        size = k + 1;
-        break;
-      }
-    std::vector<double> m(static_cast<size_t>(size) * size, 0.0), v;
-    for (int k = 0; k < size; ++k) m[static_cast<size_t>(k) * size + k] = host[static_cast<size_t>(k)];
-    for (int k = 0; k + 1 < size; ++k)
-      m[static_cast<size_t>(k) * size + k + 1] = m[static_cast<size_t>(k + 1) * size + k] = host[static_cast<size_t>(n_iter + k)];
-    jacobi_eigen(m, v, size);
-    int lowest = 0;
-    for (int k = 1; k < size; ++k)
-      if (m[static_cast<size_t>(k) * size + k] < m[static_cast<size_t>(lowest) * size + lowest]) lowest = k;
-    *energy = m[static_cast<size_t>(lowest) * size + lowest];
-    *size_out = size;
-    std::vector<double> c(static_cast<size_t>(size));
-    for (int k = 0; k < size; ++k) c[static_cast<size_t>(k)] = v[static_cast<size_t>(k) * size + lowest];
-    if ((e = cudaMemcpyAsync(ritz, c.data(), c.size() * 8, cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
-    // the Ritz vector, normalised (complex arenas: real coefficients act on both parts alike)
-    combine_kernel<<<grid, 256, 0, stream>>>(result, basis, n_doubles, size, ritz);
+    // the lowest Ritz pair of the tridiagonal (the steps after the first beta below tol dropped, as
+    // the reference stops there), then the normalised Ritz vector; complex arenas take the real
+    // coefficients on both parts alike
+    const int smem = static_cast<int>(2 * n_iter * n_iter * sizeof(double));
+    if (smem > 48 * 1024 && (e = cudaFuncSetAttribute(ritz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
+      return e;
+    ritz_kernel<<<1, 32, smem, stream>>>(tri, n_iter, tol, ritz, energy_dev, size_dev);
+    combine_kernel<<<grid, 256, 0, stream>>>(result, basis, n_doubles, size_dev, ritz);
     if ((e = arena_dots(result_slot, 1, result, n_doubles, complex, partial, coeffs, stream)) != cudaSuccess) return e;
     scale_kernel<<<grid, 256, 0, stream>>>(result, result, n_doubles, coeffs, nullptr);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    // the host vectors above are read by copies already issued; wait for them before they go
-    return cudaStreamSynchronize(stream);
+    return cudaGetLastError();
+  }
+
+  double *lanczos_energy_slot(double *scratch, int64_t n_doubles, int32_t n_iter)
+  {
+    const int64_t rows = n_iter + 1;
+    return scratch + up32(rows * n_doubles) + up32(n_doubles) + up32(2 * kDotParts * rows) + up32(2 * rows) +
+           up32(2 * rows) + rows;
   }
 
 } // namespace ttg

@@ -84,17 +84,19 @@ def lanczos(action: Callable[[Tensor], Tensor], start: Tensor, n_iter: int = 5,
 
 
 def lanczos_einsum(spec: str, tensors, vector: int, start: Tensor, n_iter: int = 5, tol: float = 1e-12,
-                   outcharge = None) -> tuple[float, Tensor]:
+                   outcharge = None, wait: bool = True):
     '''
     `lanczos(lambda v: einsum(spec, *tensors with v as operand `vector`), start, n_iter, tol)` with
     the whole Krylov loop on the device (tt_lanczos): the einsum's compiled plan runs on each basis
-    vector, the projections and norms stay on the GPU, and the host reads the tridiagonal once.  The
-    operands other than the vector are prepared once for every step (the head and tail of a DMRG
+    vector, the projections and norms stay on the GPU, and so does the tridiagonal's eigensolve.
+    The operands other than the vector are prepared once for every step (the head and tail of a DMRG
     window).  Same result as `lanczos` up to round-off; block products in the current precision.
+    With `wait` False nothing waits for the device (tt_lanczos_async): the energy comes back as a
+    0-d device tensor, and the zero-norm check of the start vector is left to the caller.
     '''
     if n_iter < 1:
         raise ValueError(f'Lanczos needs at least one step, not {n_iter}.')
-    if norm(start) == 0.0:
+    if wait and norm(start) == 0.0:
         raise ValueError('Lanczos needs a starting vector of non-zero norm.')
     from tentorch_gb300 import linalg
     from tentorch_gb300._lib import check, f64, i32, i64, lib, pointers
@@ -114,10 +116,14 @@ def lanczos_einsum(spec: str, tensors, vector: int, start: Tensor, n_iter: int =
     check(lib.tt_lanczos_scratch(start._space.size, n_iter, linalg._DTYPE[data.dtype], ctypes.byref(doubles)))
     scratch = torch.empty(doubles.value, dtype = torch.float64, device = device)
     result = torch.empty_like(data)
+    args = (plan.handle, linalg._DTYPE[data.dtype], linalg.get_precision(), pointers(t._data.data_ptr() for t in operands),
+            pointers((p.data_ptr() if p is not None else None) for p in prepared), vector, data.data_ptr(), n_iter, tol,
+            ws.data_ptr() if ws is not None else None, scratch.data_ptr(), result.data_ptr())
+    if not wait:
+        found = torch.empty(2, dtype = torch.float64, device = device)  # the energy, then the size (int32)
+        check(lib.tt_lanczos_async(*args, ctypes.cast(found.data_ptr(), ctypes.POINTER(f64)),
+                                   ctypes.cast(found.data_ptr() + 8, ctypes.POINTER(i32)), stream))
+        return found[0], Tensor._wrap(start._space, result)
     energy, size = f64(), i32()
-    check(lib.tt_lanczos(plan.handle, linalg._DTYPE[data.dtype], linalg.get_precision(),
-                         pointers(t._data.data_ptr() for t in operands),
-                         pointers((p.data_ptr() if p is not None else None) for p in prepared), vector, data.data_ptr(),
-                         n_iter, tol, ws.data_ptr() if ws is not None else None, scratch.data_ptr(), result.data_ptr(),
-                         ctypes.byref(energy), ctypes.byref(size), stream))
+    check(lib.tt_lanczos(*args, ctypes.byref(energy), ctypes.byref(size), stream))
     return float(energy.value), Tensor._wrap(start._space, result)

@@ -364,11 +364,11 @@ class DMRG:
     def update(self, direction: Literal['left', 'right']) -> tuple[float, float]:
         '''tentorch/algorithms/dmrg.py:96-129'''
         energy, lost = self._update(direction)
-        return energy, float(lost)
+        return float(energy), float(lost)
 
-    def _update(self, direction: Literal['left', 'right']) -> tuple[float, torch.Tensor]:
-        '''One window, with the discarded weight left on the device and the centre normalised there:
-        the window's only host waits are the Krylov loop's and the split's reads of its values.'''
+    def _update(self, direction: Literal['left', 'right']) -> tuple[torch.Tensor, torch.Tensor]:
+        '''One window, with its energy and discarded weight left on the device and the centre
+        normalised there: the window's only host wait is the split's read of its singular values.'''
         at = self.center
         first, second = self.state.tensors[at], self.state.tensors[at + 1]
         two = contract(first, second, domain_legs(first), [0])
@@ -379,7 +379,8 @@ class DMRG:
         # the reference's action, einsum('EPaqj,JRSFb,AQsb->EPrf', head, tail, vector), with the
         # Krylov loop on the device
         with precision(self.precision):
-            energy, vector = lanczos_einsum('EPaqj,JRSFb,AQsb->EPrf', [head, tail, two], 2, two, self.n_iter)
+            energy, vector = lanczos_einsum('EPaqj,JRSFb,AQsb->EPrf', [head, tail, two], 2, two, self.n_iter,
+                                            wait = False)
         self.matvecs += self.n_iter
         factor = 2 if direction == 'right' else 1
         left, values, right = svd(vector, self.max_bond_dim, self.svd_tol, factor)
@@ -413,9 +414,9 @@ class DMRG:
             lost.append(weight)
             if at > 0:
                 self.right[at + 1] = self._advance_right(self.right[at + 2], at + 1)
-        # the largest weight any window discarded, read once per sweep
+        # the energy of the last window and the largest weight any window discarded, read once per sweep
         discarded = float(torch.stack(lost).max()) if lost else 0.0
-        return energy, max(discarded, 0.0)
+        return float(energy), max(discarded, 0.0)
 
     def energy(self) -> complex:
         '''tentorch/algorithms/dmrg.py:163-179'''
