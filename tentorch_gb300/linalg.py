@@ -403,6 +403,14 @@ def is_close(first: Tensor, second: Tensor, rtol: float = 1e-10, atol: float = 1
 # ---------------------------------------------------------------------------------------------
 
 
+# The cuSOLVER method of the per-block SVDs on a CUDA device.  'gesvd' (QR iteration) leaves the
+# factors orthonormal to ~4e-15; torch's default for these block sizes (Jacobi, gesvdj) only to
+# ~1e-13, which moves a DMRG sweep energy at L = 64, bond 256 by ~1.4e-10.  None picks torch's
+# default, which is what the reference's at::linalg_svd (tentorch/linalg/graded/svd.cpp:59) runs
+# on a CUDA device.
+PER_BLOCK_SVD_DRIVER: Optional[str] = 'gesvd'
+
+
 def _factor_blocks(arranged: Tensor):
     """The thin SVD of every non-empty block.  float64 blocks on the GPU go through one launch of
     the engine's Jacobi SVD (tt_svd_blocks), complex blocks, blocks beyond its size and the
@@ -415,8 +423,9 @@ def _factor_blocks(arranged: Tensor):
                all(min(space.shapes[i]) <= 1024 for i, _ in present))
     if not batched:
         factors = []
+        driver = PER_BLOCK_SVD_DRIVER if arranged.device.type == 'cuda' else None
         for i, key in present:
-            u, sv, vh = torch.linalg.svd(arranged._view(i), full_matrices = False)
+            u, sv, vh = torch.linalg.svd(arranged._view(i), full_matrices = False, driver = driver)
             factors.append([key, u, sv, vh, 0, 0])
         host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
         return factors, host, None

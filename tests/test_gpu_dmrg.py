@@ -151,3 +151,36 @@ def test_device_lanczos_matches_the_python_loop(dtype):
         with tg.precision(8):
             e_split, _ = lanczos_einsum(spec, [head, tail, two], 2, two, 5)
         assert abs(e_split - e_dev) < 1e-10
+
+
+def test_sixty_four_sites_bond_256_meet_the_reference_sweeps():
+    '''The headline chain (U(1) Heisenberg, L = 64, bond 256, n_iter = 10, seed 0) against the
+    reference's own float64 run of the same seed (tests/golden/dmrg_chi256.json): from the fourth
+    sweep on, when every bond is at 256, the grouped FP64 sweeps meet the reference's energies
+    within 1e-10, and one sweep from the same fourth-sweep state in each other form does too: the
+    six-slice split matvec and the per-block form (one cuBLAS product per block pair, one cuSOLVER
+    SVD per block).  The first sweeps start from a random state whose truncations (the +-q pairing
+    of the bond) pick among nearly equal values, so they follow their own path until the bond fills
+    (their energies are not compared); the bond dimensions also differ at a few bonds, where
+    singular values sit at the 1e-14 cut and round to either side in two SVD implementations.'''
+    from tentorch_gb300.linalg import PER_BLOCK
+    golden = load_json('dmrg_chi256.json')
+    driver = _driver(64, 256, golden['seed'], 0, golden['n_iter'])
+    energies = []
+    for _ in range(4):
+        energies.append(driver.sweep()[0])
+    start = ([t.clone() for t in driver.state.tensors], driver.state.center)
+    for _ in range(2):
+        energies.append(driver.sweep()[0])
+    want = [s['energy'] for s in golden['sweeps']]
+    for at in (3, 4, 5):
+        assert abs(energies[at] - want[at]) < ENERGY_TOL, (at + 1, energies[at], want[at])
+    assert max(driver.state.bond_dims) == 256
+    assert abs(driver.energy().real - golden['energy']) < ENERGY_TOL
+    for form in (6, PER_BLOCK):
+        driver.state.tensors = [t.clone() for t in start[0]]
+        driver.state.center = start[1]
+        driver.precision = form
+        with tg.precision(PER_BLOCK if form == PER_BLOCK else 0):
+            energy, _ = driver.sweep()
+        assert abs(energy - want[4]) < ENERGY_TOL, (form, energy, want[4])
