@@ -280,7 +280,13 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     split precision, environments included, is the driver's `all_products` option; at this bond it
     is slower than the matvec alone in split precision and, at 6 slices, outside the 1e-10 bar.)"""
     from tentorch_gb300 import networks as nw
+    from tentorch_gb300 import linalg as la
     from tentorch_gb300.linalg import PER_BLOCK, cached_plans, clear_plans
+    # the reference's own float64 run of this chain and seed (sweep energies, per sweep)
+    golden_path = os.path.join(HERE, 'tests', 'golden', 'dmrg_chi256.json')
+    golden = None
+    if length == 64 and chi == 256 and n_iter == 10 and os.path.exists(golden_path):
+        golden = [s['energy'] for s in json.load(open(golden_path))['sweeps']]
     tg.set_precision(0)
     driver = nw.DMRG(nw.Model(length, cat = tg.u1), max_bond_dim = chi, n_iter = n_iter, dtype = torch.float64,
                      device = device, generator = torch.Generator().manual_seed(SEED), precision = 0)
@@ -290,10 +296,13 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     warm_s = time.perf_counter() - start
     snapshot = ([t.clone() for t in driver.state.tensors], driver.state.center)
     out = {}
-    for name, form in (('fp64_grouped', 0), ('split', precision), ('fp64_per_block', PER_BLOCK)):
+    forms = (('fp64_grouped', 0, 'gesvd'), ('split', precision, 'gesvd'), ('fp64_per_block', PER_BLOCK, 'gesvd'),
+             ('fp64_per_block_default_svd', PER_BLOCK, None))
+    for name, form, svd_driver in forms:
         driver.state.tensors = [t.clone() for t in snapshot[0]]
         driver.state.center = snapshot[1]
         driver.precision = form
+        la.PER_BLOCK_SVD_DRIVER = svd_driver
         tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
         clear_plans()
         mv0 = driver.matvecs
@@ -306,7 +315,16 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
         # the energy of the state the sweep left, evaluated in FP64
         check = driver.energy().real
         out[name] = {'s_per_sweep': elapsed, 'energy': energy, 'energy_fp64_check': check,
-                     'discarded': lost, 'matvecs': driver.matvecs - mv0, 'max_bond': max(driver.state.bond_dims)}
+                     'discarded': lost, 'matvecs': driver.matvecs - mv0, 'max_bond': max(driver.state.bond_dims),
+                     'svd': 'engine Jacobi (batched)' if form != PER_BLOCK else f'torch.linalg.svd per block, driver {svd_driver}'}
+        if golden is not None:
+            out[name]['delta_e_vs_reference'] = abs(energy - golden[warm])
+        if svd_driver is None:
+            # the per-block form as the reference runs on a CUDA device (torch's default cuSOLVER
+            # method): one sweep, for the record
+            la.PER_BLOCK_SVD_DRIVER = 'gesvd'
+            tg.set_precision(0)
+            continue
         # the next sweep of the same run, its plans cached by the first where the shapes recur
         # (as in a long run); it compiles only the shapes that the truncations changed
         tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
@@ -318,6 +336,9 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
         out[name]['s_per_sweep_continued'] = time.perf_counter() - t0
         out[name]['continued_energy'] = energy2
         out[name]['continued_plans_compiled'] = cached_plans() - plans0
+        if golden is not None and warm + 1 < len(golden):
+            out[name]['continued_delta_e_vs_reference'] = abs(energy2 - golden[warm + 1])
+        la.PER_BLOCK_SVD_DRIVER = 'gesvd'
         tg.set_precision(0)
     tg.set_precision(0)
     clear_plans()
@@ -327,7 +348,12 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
         out[name]['delta_e_vs_own_fp64_check'] = abs(out[name]['energy'] - out[name]['energy_fp64_check'])
     return {'length': length, 'chi': chi, 'n_iter': n_iter, 'warm_fp64_sweeps': warm, 'warm_s': warm_s,
             'forms': out,
+            'reference_energy': golden[warm] if golden is not None else None,
+            'reference': 'the reference run in float64 from the same seed (tests/golden/dmrg_chi256.json), sweep '
+                         f'{warm + 1} and the next',
             'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
+            'speedup_split_vs_per_block_default_svd': out['fp64_per_block_default_svd']['s_per_sweep'] /
+                                                      out['split']['s_per_sweep'],
             'speedup_split_vs_fp64_grouped': out['fp64_grouped']['s_per_sweep'] / out['split']['s_per_sweep'],
             'speedup_split_vs_per_block_continued': out['fp64_per_block']['s_per_sweep_continued'] /
                                                     out['split']['s_per_sweep_continued'],
@@ -557,12 +583,26 @@ def run_recoupling(args):
     each, float64; Fibonacci legs (vacuum 16, tau 16), complex128; seeded N(0, 1) blocks.  Times each
     form the engine has for it (grouped FP64, split (float64 only), per-block cuBLAS) and the
     largest relative difference between the forms.  Prints one line of its own."""
+    import numpy as np
     import torch
     import tentorch_gb300 as tg
     from tentorch_gb300.linalg import PER_BLOCK
+    from oracle import engine as orc
     device = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
     torch.cuda.set_device(device)
     out = {'workload': 'recoupling_einsum_ABcd_DCef', 'equation': 'ABcd,DCef->ABef'}
+
+    def orc_einsum_of(tensors):
+        ocat = {id(tg.su2): orc.su2, id(tg.fibonacci): orc.fibonacci}[id(tensors[0].cat)]
+        cast = np.complex128 if tensors[0].dtype == torch.complex128 else np.float64
+        legs = lambda ls: [orc.Leg(ocat, l.sectors, l.multiplicities) for l in ls]
+        ops = []
+        for t in tensors:
+            o = orc.Tensor(ocat, legs(t.codomain), legs(t.domain), tuple(t.qtotal), cast)
+            for key in o.blocks:
+                o.blocks[key][...] = t.block(*key).cpu().numpy()
+            ops.append(o)
+        return orc.einsum('ABcd,DCef->ABef', *ops).blocks
     for name, cat, leg, dtype in (('su2', tg.su2, tg.Leg(tg.su2, [(j,) for j in range(9)], [8] * 9), torch.float64),
                                   ('fibonacci', tg.fibonacci, tg.Leg(tg.fibonacci, [(0,), (1,)], [16, 16]),
                                    torch.complex128)):
@@ -591,10 +631,14 @@ def run_recoupling(args):
             ms = 1e3 * (time.perf_counter() - start) / steps
             flops = plan.flops * (4 if dtype == torch.complex128 else 1)
             results[form_name] = {'ms': ms, 'tflops': flops / (ms / 1e3) / 1e12}
-        ref = images['fp64_grouped'].data
-        scale = float(ref.abs().max())
+        # every form against the oracle (the CPU restatement of the reference's einsum) on the same
+        # inputs, relative to the largest entry
+        want = orc_einsum_of(tensors)
+        scale = max(float(np.abs(b).max()) for b in want.values())
         for form_name in results:
-            results[form_name]['max_rel_diff_vs_fp64_grouped'] = float((images[form_name].data - ref).abs().max()) / scale
+            got = images[form_name]
+            worst = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.items())
+            results[form_name]['max_rel_err_vs_oracle'] = worst / scale
         out[name] = {'dtype': str(dtype).replace('torch.', ''), 'blocks': tensors[0].nblocks(),
                      'entries_per_tensor': tensors[0].data.numel(), 'gemm_flop': plan.flops, 'forms': results}
     print(json.dumps(out), flush = True)
@@ -618,6 +662,10 @@ def run_windows(args):
     windows = [matvec_operands(tg, torch, device, chi, SEED + i) for i, chi in enumerate(chis)]
     flops = sum(tg.linalg.plan_of(MATVEC, *win).flops for win in windows)
     out = {'workload': 'batched_windows_u1_matvec', 'windows': len(windows), 'chis': chis, 'gemm_flop_per_step': flops}
+    # a few windows (bonds 512, 64, 32, 128) checked against the oracle in every form
+    from oracle import engine as orc
+    checked = (0, 3, 5, 12)
+    wanted = {i: orc.einsum(MATVEC, *(to_oracle(orc, t) for t in windows[i])).blocks for i in checked}
     stream = torch.cuda.current_stream(device)
     for name, form in (('split', args.precision), ('fp64_grouped', 0)):
         with tg.precision(form):
@@ -670,9 +718,32 @@ def run_windows(args):
                 graph.replay()
             torch.cuda.synchronize(device)
             graph_ms = 1e3 * (time.perf_counter() - start) / steps
+            # all windows through one call: in FP64 one persistent launch for every window's products
+            def batched():
+                for win in windows:
+                    increment_version(win[2].data)
+                return tg.linalg.einsum_batch(MATVEC, windows)
+            for _ in range(3):
+                batched()
+            torch.cuda.synchronize(device)
+            start = time.perf_counter()
+            for _ in range(steps):
+                batched()
+            torch.cuda.synchronize(device)
+            batch_ms = 1e3 * (time.perf_counter() - start) / steps
+            batch_launches = tg.linalg.last_batch_launches
+            worst = 0.0
+            images = batched()
+            for i in checked:
+                scale = max(float(np.abs(b).max()) for b in wanted[i].values())
+                for got in (tg.einsum(MATVEC, *windows[i]), images[i]):
+                    worst = max(worst, max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in wanted[i].items()) / scale)
         out[name] = {'eager_ms_per_step': eager_ms, 'four_streams_ms_per_step': streams_ms, 'graph_ms_per_step': graph_ms,
+                     'one_call_ms_per_step': batch_ms, 'one_call_launches': batch_launches,
                      'matvecs_per_s_graph': len(windows) / (graph_ms / 1e3),
-                     'gflops_graph': flops / (graph_ms / 1e3) / 1e9}
+                     'matvecs_per_s_one_call': len(windows) / (batch_ms / 1e3),
+                     'gflops_graph': flops / (graph_ms / 1e3) / 1e9,
+                     'max_rel_err_vs_oracle': {'windows': list(checked), 'value': worst}}
     print(json.dumps(out), flush = True)
 
 
