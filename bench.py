@@ -153,6 +153,18 @@ def cpu_matvecs(chi, count):
     return count / elapsed, elapsed, count
 
 
+def cpu_matvecs_one_thread(chi, count):
+    '''The same sample with one BLAS thread, in a child process (the thread count of numpy's BLAS is
+    fixed when it loads); (matvecs/s, seconds, count), or None when the child fails.'''
+    env = dict(os.environ, OMP_NUM_THREADS = '1', OPENBLAS_NUM_THREADS = '1', MKL_NUM_THREADS = '1')
+    code = f'import sys, json; sys.path.insert(0, {HERE!r}); import bench; print(json.dumps(bench.cpu_matvecs({chi}, {count})))'
+    try:
+        done = subprocess.run([sys.executable, '-c', code], env = env, capture_output = True, text = True, timeout = 600)
+        return tuple(json.loads(done.stdout.strip().splitlines()[-1]))
+    except Exception:
+        return None
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -524,6 +536,7 @@ def run_gpu(args, rank, world):
 
     if rank == 0:
         cpu_value, cpu_elapsed, cpu_n = cpu_matvecs(args.chi, args.cpu_sample)
+        one = cpu_matvecs_one_thread(args.chi, max(1, args.cpu_sample // 2))
         line = {'metric': METRIC, 'value': value, 'unit': 'matvecs/s', 'n_gpus': world, 'steps': args.steps,
                 'warmup': args.warmup, 'ms_per_step': ms_per_step, 'higher_is_better': True, 'scaling': 'weak',
                 'vs_baseline': None, 'dtype': 'f64' if args.precision == 0 else f'bf16x{args.precision}-split/f64',
@@ -540,6 +553,11 @@ def run_gpu(args, rank, world):
                 'cpu_baseline': {'value': cpu_value, 'unit': 'matvecs/s', 'cores': os.cpu_count(), 'kind': 'port',
                                  'sample': f'{cpu_n} matvecs at chi={args.chi} of the oracle port of tentorch einsum '
                                            f'(numpy; {cpu_elapsed:.1f} s)'},
+                'cpu_baseline_one_thread': ({'value': one[0], 'unit': 'matvecs/s', 'cores': 1, 'kind': 'port',
+                                             'sample': f'{one[2]} matvecs, one BLAS thread ({one[1]:.1f} s)'}
+                                            if one else None),
+                'e2e_vs_cpu': 'the e2e rate against cpu_baseline compares with the numpy port of the reference '
+                              "(oracle/engine.py), not with the reference's compiled engine",
                 'e2e': {'value': world * 1e3 / e2e_ms, 'unit': 'matvecs/s', 'h2d_bytes_per_step': h2d,
                         'd2h_bytes_per_step': d2h,
                         'path': 'pinned host theta -> H2D -> tentorch_gb300.einsum (C ABI) -> D2H of the image'},
