@@ -20,7 +20,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <numeric>
@@ -428,11 +427,9 @@ namespace ttg
 
     // The DMMA tile machinery of gemm_dmma_kernel (gemm.cu) over the items of both products: K in
     // steps of 32 through two shared stages per worker, a 16 x 16 quarter of the 32 x 32 tile per
-    // warp, `Chains` accumulators per fragment taking the 8-wide K steps in turn (2 * Chains DMMAs of
-    // a warp in flight).  The first product's operands and the second's B side are read-only during
+    // warp.  The first product's operands and the second's B side are read-only during
     // the launch and staged with cp.async; the second's A side (X', written during the launch by
     // other SMs) is read with L2 loads, so that no SM reads a stale copy of a line from its L1.
-    template <int Chains>
     __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1) chain_dmma_kernel(const __grid_constant__ ChainLaunch L)
     {
       dependent_entry();
@@ -460,7 +457,7 @@ namespace ttg
         if (second) wait_first(a, L.error, worker, lt);
         const double *A = second ? a.moved : a.a1;
         const double *B = second ? a.b2 : a.b1;
-        double acc[Chains][2][4] = {};
+        double acc[2][4] = {};
         const bool live_i = it.m0 + wm * 16 < blk.m;
         const bool live_j[2] = {it.n0 + wn * 16 < blk.n, it.n0 + wn * 16 + 8 < blk.n};
         int32_t kbase = 0;
@@ -534,32 +531,21 @@ namespace ttg
               if (steps == BK)
               {
 #pragma unroll
-                for (int kb = 0; kb < BK; kb += 8) step_k(kb, acc[(kb / 8) % Chains]);
+                for (int kb = 0; kb < BK; kb += 8) step_k(kb, acc);
               }
               else
-                for (int kb = 0; kb < steps; kb += 8 * Chains)
-                {
-#pragma unroll
-                  for (int c = 0; c < Chains; ++c)
-                    if (kb + 8 * c < steps) step_k(kb + 8 * c, acc[c]);
-                }
+                for (int kb = 0; kb < steps; kb += 8) step_k(kb, acc);
             }
             worker_sync(worker);
           }
         }
-#pragma unroll
-        for (int c = 1; c < Chains; ++c)
-#pragma unroll
-          for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int h = 0; h < 4; ++h) acc[0][j][h] += acc[c][j][h];
         if (it.slot >= 0)
         {
           double *out = a.partial + static_cast<int64_t>(it.slot) * BM * BN;
 #pragma unroll
           for (int j = 0; j < 2; ++j)
 #pragma unroll
-            for (int h = 0; h < 4; ++h) out[(wm * 16 + (h >> 1) * 8 + fr) * BN + wn * 16 + j * 8 + fk * 2 + (h & 1)] = acc[0][j][h];
+            for (int h = 0; h < 4; ++h) out[(wm * 16 + (h >> 1) * 8 + fr) * BN + wn * 16 + j * 8 + fk * 2 + (h & 1)] = acc[j][h];
           finish_chain_partial(a, worker, lt, flags + worker, it.reduce);
           continue;
         }
@@ -569,7 +555,7 @@ namespace ttg
           for (int h = 0; h < 4; ++h)
           {
             const int gm = it.m0 + wm * 16 + (h >> 1) * 8 + fr, gn = it.n0 + wn * 16 + j * 8 + fk * 2 + (h & 1);
-            if (gm < blk.m && gn < blk.n) store_entry(a, it.stage, blk, gm, gn, acc[0][j][h]);
+            if (gm < blk.m && gn < blk.n) store_entry(a, it.stage, blk, gm, gn, acc[j][h]);
           }
         store_pad(a, it.stage, blk, it.m0, it.n0, lt);
         if (!second) signal_done(a, worker, lt);
@@ -618,19 +604,10 @@ namespace ttg
       const int bytes = std::max<int>(kF64Workers * 2 * 2 * kDmmaStepK * 36 * 8, kChainPinBytes);
       static std::once_flag once;
       cudaError_t e = cudaSuccess;
-      static const int chains = []
-      {
-        const char *v = std::getenv("TTG_CHAINS");
-        return v && v[0] == '2' ? 2 : 1;
-      }();
-      std::call_once(once, [&] {
-        e = cudaFuncSetAttribute(chain_dmma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(chain_dmma_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-      });
+      std::call_once(once, [&] { e = cudaFuncSetAttribute(chain_dmma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
       if (e != cudaSuccess) return e;
       const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kF64Workers));
-      if (chains == 2) return launch_dependent(chain_dmma_kernel<2>, n_ctas, workers * kWorkerThreads, bytes, stream, launch);
-      return launch_dependent(chain_dmma_kernel<1>, n_ctas, workers * kWorkerThreads, bytes, stream, launch);
+      return launch_dependent(chain_dmma_kernel, n_ctas, workers * kWorkerThreads, bytes, stream, launch);
     }
 
     // The deal of a batch's items, per list of programs.

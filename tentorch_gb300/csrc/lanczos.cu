@@ -90,17 +90,36 @@ namespace ttg
       }
     }
 
+    // The number of eigenvalues of the symmetric tridiagonal (diagonal a, off-diagonal b) below x: the
+    // negative pivots of the LDL^T factorisation of T - x I (Sturm's sequence); a zero pivot is taken
+    // as a tiny negative one.
+    __device__ int below(const double *a, const double *b, int n, double x, double pivmin)
+    {
+      int count = 0;
+      double d = a[0] - x;
+      for (int i = 0;; ++i)
+      {
+        if (fabs(d) < pivmin) d = -pivmin;
+        if (d < 0.0) ++count;
+        if (i + 1 == n) break;
+        d = (a[i + 1] - x) - b[i] * b[i] / d;
+      }
+      return count;
+    }
+
     // The Krylov space's lowest Ritz pair on the device, one warp: the size of the space (the steps
-    // before the first beta below `tol`, as the reference stops), the tridiagonal's eigenpairs by
-    // cyclic Jacobi rotations (C. G. J. Jacobi, 1846; the rotation as in Golub & Van Loan, "Matrix
-    // Computations", the symmetric Schur decomposition; each rotation's parameters by one lane, its
-    // row and column updates over the lanes), the lowest eigenvalue and its eigenvector.  Products
-    // and sums are rounded one by one (no fused multiply-add), as the host arithmetic of x86 does.
+    // before the first beta below `tol`, as the reference stops), the tridiagonal's lowest eigenvalue
+    // by multisection of its Sturm count (each round the 32 lanes count below 32 points of the
+    // bracket, which shrinks it 33-fold, from Gershgorin's bounds down to a few units in the last
+    // place) and its eigenvector by inverse iteration (Gaussian elimination with partial pivoting
+    // of T - lambda I, three solves from a vector of ones, normalised; W. Kahan, "Accurate
+    // eigenvalues of a symmetric tri-diagonal matrix", 1966, and J. H. Wilkinson, "The Algebraic
+    // Eigenvalue Problem", 1965, for inverse iteration).
     __global__ void ritz_kernel(const double *tri, int32_t n_iter, double tol, double *ritz, double *energy,
                                 int32_t *size_out)
     {
       extern __shared__ double work[];
-      __shared__ double rot[2];
+      __shared__ double bracket[2];
       __shared__ int32_t shared_size;
       const int lane = threadIdx.x;
       if (lane == 0)
@@ -116,79 +135,119 @@ namespace ttg
       }
       __syncwarp();
       const int n = shared_size;
-      double *a = work, *v = work + n * n;
-      for (int i = lane; i < n * n; i += 32)
+      double *a = work, *b = work + n, *v = work + 2 * n;
+      for (int i = lane; i < n; i += 32)
       {
-        const int r = i / n, c = i % n;
-        a[i] = r == c ? tri[r] : (c == r + 1 ? tri[n_iter + r] : (r == c + 1 ? tri[n_iter + c] : 0.0));
-        v[i] = r == c ? 1.0 : 0.0;
+        a[i] = tri[i];
+        b[i] = i + 1 < n ? tri[n_iter + i] : 0.0;
       }
       __syncwarp();
-      for (int sweep = 0; sweep < 100; ++sweep)
-      {
-        if (lane == 0)
-        {
-          double off = 0.0;
-          for (int p = 0; p < n; ++p)
-            for (int q = p + 1; q < n; ++q) off = __dadd_rn(off, __dmul_rn(a[p * n + q], a[p * n + q]));
-          rot[0] = off;
-        }
-        __syncwarp();
-        if (rot[0] == 0.0) break;
-        for (int p = 0; p < n; ++p)
-          for (int q = p + 1; q < n; ++q)
-          {
-            const double apq = a[p * n + q];
-            __syncwarp();
-            if (apq == 0.0) continue;
-            if (lane == 0)
-            {
-              const double app = a[p * n + p], aqq = a[q * n + q];
-              const double tau = __ddiv_rn(__dsub_rn(aqq, app), __dmul_rn(2.0, apq));
-              const double t = __ddiv_rn(tau >= 0 ? 1.0 : -1.0, __dadd_rn(fabs(tau), __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(tau, tau)))));
-              const double c = __ddiv_rn(1.0, __dsqrt_rn(__dadd_rn(1.0, __dmul_rn(t, t))));
-              rot[0] = c;
-              rot[1] = __dmul_rn(t, c);
-            }
-            __syncwarp();
-            const double c = rot[0], s = rot[1];
-            for (int k = lane; k < n; k += 32)
-            {
-              const double akp = a[k * n + p], akq = a[k * n + q];
-              a[k * n + p] = __dsub_rn(__dmul_rn(c, akp), __dmul_rn(s, akq));
-              a[k * n + q] = __dadd_rn(__dmul_rn(s, akp), __dmul_rn(c, akq));
-            }
-            __syncwarp();
-            for (int k = lane; k < n; k += 32)
-            {
-              const double apk = a[p * n + k], aqk = a[q * n + k];
-              a[p * n + k] = __dsub_rn(__dmul_rn(c, apk), __dmul_rn(s, aqk));
-              a[q * n + k] = __dadd_rn(__dmul_rn(s, apk), __dmul_rn(c, aqk));
-            }
-            for (int k = lane; k < n; k += 32)
-            {
-              const double vkp = v[k * n + p], vkq = v[k * n + q];
-              v[k * n + p] = __dsub_rn(__dmul_rn(c, vkp), __dmul_rn(s, vkq));
-              v[k * n + q] = __dadd_rn(__dmul_rn(s, vkp), __dmul_rn(c, vkq));
-            }
-            __syncwarp();
-          }
-      }
       if (lane == 0)
       {
-        int lowest = 0;
-        for (int k = 1; k < n; ++k)
-          if (a[k * n + k] < a[lowest * n + lowest]) lowest = k;
-        *energy = a[lowest * n + lowest];
-        *size_out = n;
-        shared_size = lowest;
+        double lo = a[0], hi = a[0], scale = 0.0;
+        for (int i = 0; i < n; ++i)
+        {
+          const double r = (i > 0 ? fabs(b[i - 1]) : 0.0) + (i + 1 < n ? fabs(b[i]) : 0.0);
+          lo = fmin(lo, a[i] - r);
+          hi = fmax(hi, a[i] + r);
+          scale = fmax(scale, fabs(a[i]) + r);
+        }
+        bracket[0] = lo;
+        bracket[1] = hi;
+        work[3 * n] = fmax(scale, 1.0) * 1e-290;  // pivmin
       }
       __syncwarp();
-      for (int k = lane; k < n; k += 32) ritz[k] = v[k * n + shared_size];
+      const double pivmin = work[3 * n];
+      for (int round = 0; round < 64; ++round)
+      {
+        const double lo = bracket[0], hi = bracket[1];
+        if (!(hi - lo > 4.0 * 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi))) || !(hi > lo)) break;
+        const double x = lo + (hi - lo) * static_cast<double>(lane + 1) / 33.0;
+        const bool any = below(a, b, n, x, pivmin) >= 1;
+        const unsigned hits = __ballot_sync(0xffffffffu, any);
+        __syncwarp();
+        if (lane == 0)
+        {
+          // the first point with an eigenvalue below it closes the bracket of the lowest one
+          const int first = hits ? __ffs(hits) - 1 : 32;
+          const double step = (hi - lo) / 33.0;
+          bracket[0] = first == 0 ? lo : lo + step * first;
+          bracket[1] = first == 32 ? hi : lo + step * (first + 1);
+        }
+        __syncwarp();
+      }
+      const double lambda = 0.5 * (bracket[0] + bracket[1]);
+      if (lane == 0)
+      {
+        // inverse iteration: (T - lambda I) y = v by elimination with partial pivoting (the
+        // tridiagonal's upper factor has two superdiagonals)
+        double *d = work + 3 * n + 1, *du = d + n, *du2 = du + n, *dl = du2 + n;
+        for (int i = 0; i < n; ++i) v[i] = 1.0;
+        for (int it = 0; it < 3; ++it)
+        {
+          for (int i = 0; i < n; ++i)
+          {
+            d[i] = a[i] - lambda;
+            du[i] = i + 1 < n ? b[i] : 0.0;
+            du2[i] = 0.0;
+            dl[i] = i + 1 < n ? b[i] : 0.0;
+          }
+          for (int i = 0; i + 1 < n; ++i)
+          {
+            if (fabs(d[i]) >= fabs(dl[i]))
+            {
+              const double piv = d[i] != 0.0 ? d[i] : pivmin;
+              const double f = dl[i] / piv;
+              d[i] = piv;
+              d[i + 1] -= f * du[i];
+              v[i + 1] -= f * v[i];
+            }
+            else
+            {
+              // swap rows i and i + 1
+              const double f = d[i] / dl[i];
+              d[i] = dl[i];
+              const double t = d[i + 1];
+              d[i + 1] = du[i] - f * t;
+              du[i] = t;
+              du2[i] = i + 2 < n ? du[i + 1] : 0.0;
+              if (i + 2 < n) du[i + 1] = -f * du2[i];
+              const double vt = v[i];
+              v[i] = v[i + 1];
+              v[i + 1] = vt - f * v[i + 1];
+            }
+          }
+          if (d[n - 1] == 0.0) d[n - 1] = pivmin;
+          for (int i = n - 1; i >= 0; --i)
+          {
+            double x = v[i];
+            if (i + 1 < n) x -= du[i] * v[i + 1];
+            if (i + 2 < n) x -= du2[i] * v[i + 2];
+            v[i] = x / d[i];
+          }
+          // scaled by the largest component first (a shift at an eigenvalue makes the solve huge),
+          // then normalised with that component positive
+          int big = 0;
+          for (int i = 1; i < n; ++i)
+            if (fabs(v[i]) > fabs(v[big])) big = i;
+          const double top = v[big];
+          double norm2 = 0.0;
+          for (int i = 0; i < n; ++i)
+          {
+            v[i] /= top;
+            norm2 += v[i] * v[i];
+          }
+          const double inv = 1.0 / sqrt(norm2);
+          for (int i = 0; i < n; ++i) v[i] *= inv;
+        }
+        *energy = lambda;
+        *size_out = n;
+      }
+      __syncwarp();
+      for (int k = lane; k < n; k += 32) ritz[k] = v[k];
     }
 
     int grid_of(int64_t n_doubles) { return static_cast<int>(std::clamp<int64_t>((n_doubles + 255) / 256, 1, device_sms() * 8)); }
-
   } // namespace
 
   namespace
@@ -253,7 +312,7 @@ namespace ttg
     // the lowest Ritz pair of the tridiagonal (the steps after the first beta below tol dropped, as
     // the reference stops there), then the normalised Ritz vector; complex arenas take the real
     // coefficients on both parts alike
-    const int smem = static_cast<int>(2 * n_iter * n_iter * sizeof(double));
+    const int smem = static_cast<int>((7 * n_iter + 1) * sizeof(double));
     if (smem > 48 * 1024 && (e = cudaFuncSetAttribute(ritz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
       return e;
     ritz_kernel<<<1, 32, smem, stream>>>(tri, n_iter, tol, ritz, energy_dev, size_dev);
