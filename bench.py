@@ -265,7 +265,7 @@ def ncu_traffic(kernel):
 
 
 KIND_NAMES = {0: 'memset', 1: 'gather_kernel', 2: 'runs_kernel', 3: None, 4: 'add_f64_kernel', 5: 'memcpy',
-              6: 'tiles_kernel', 7: 'chain_dmma_kernel'}
+              6: 'tiles_kernel', 7: 'chain_fp64_kernel'}
 
 
 def gemm_kernel_name(precision):
@@ -483,9 +483,9 @@ def run_gpu(args, rank, world):
     by_kind, launches_per_step = op_profile(args.precision)
     gemm_ms = by_kind.get(gemm_kernel_name(args.precision), 0.0)
     fp64_kinds, _ = op_profile(0)
-    # the FP64 products of the matvec: one launch with the leg move between them (chain_dmma_kernel),
+    # the FP64 products of the matvec: one launch with the leg move between them (chain_fp64_kernel),
     # or the two grouped launches when the chain does not run as one
-    fp64_kernel = 'chain_dmma_kernel' if 'chain_dmma_kernel' in fp64_kinds else 'gemm_dmma_kernel'
+    fp64_kernel = 'chain_fp64_kernel' if 'chain_fp64_kernel' in fp64_kinds else 'gemm_dmma_kernel'
     dmma_ms = fp64_kinds.get(fp64_kernel, 0.0)
     fp64_peak = fp64_peak_tflops(torch, device)
     fp64_achieved = plan.flops / (dmma_ms / 1e3) / 1e12 if dmma_ms > 0 else 0.0

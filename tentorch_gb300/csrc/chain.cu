@@ -76,58 +76,95 @@ namespace ttg
 
   namespace
   {
-    constexpr int kChainTile = 32;  // the DMMA tile (kF64TileM x kF64TileN)
+    constexpr int kChainTile = 32;  // the tile of an item (kF64TileM x kF64TileN)
+    // Four workers of 128 threads per SM, each with one warp on every quarter of the SM: while one
+    // worker claims, waits for its operands or sums a partial tile, the others keep the quarters'
+    // FP64 units busy.
+    constexpr int kChainWorkers = 4, kChainThreads = 128;
+    constexpr int kPer = 8;                           // a thread's slots of a tile
+    constexpr int kSlots = kChainThreads * kPer;      // a worker's slots
 
-    // The work estimate the FP64 schedules deal by (gemm.cu schedule_gemm): 16 x 8 fragments
-    // touching the block times K, plus a quarter tile over 16 of K per staged step and per item.
+    // The work estimate of an item, in multiply-adds: its live entries in warps of 32 times K, plus
+    // the equivalent of a quarter tile over 16 of K per staged step and per item.
     double item_work(double rows, double cols, double k)
     {
-      const double frag = std::ceil(rows / 16.0) * 16.0 * std::ceil(cols / 8.0) * 8.0;
-      return frag * k + 0.25 * kChainTile * kChainTile * 16.0 * (std::ceil(k / kDmmaStepK) + 1.0);
+      const double lanes = std::ceil(rows * cols / 32.0) * 32.0;
+      return lanes * k + 0.25 * kChainTile * kChainTile * 16.0 * (std::ceil(k / kDmmaStepK) + 1.0);
     }
 
-    // The items of both products (cut as their separate launches cut them, first product first),
-    // their work, and one list per SM dealt largest first onto the least loaded, the first product
-    // before the second; false when the counters do not fit the ticket region.
+    // The items of one product: the grouped FP64 schedule's 32 x 32 tiles over K ranges (gemm.cu
+    // schedule_gemm: about six items per SM, a tile cut along K into partial tiles when it is
+    // larger), with their tile extents in ChainItem::pad and ChainReduce::pad0 (rows | cols << 8)
+    // and their work for the deal.
+    struct ChainCut
+    {
+      std::vector<ChainItem> items;
+      std::vector<double> work;
+      std::vector<ChainReduce> reduces;
+      int64_t slots = 0;
+    };
+    void cut_product(const Program &p, const Op &op, int32_t stage, ChainCut &cut)
+    {
+      const GemmSchedule s = schedule_gemm(p, op, kChainTile, kChainTile, true);
+      const int32_t slot0 = static_cast<int32_t>(cut.slots), reduce0 = static_cast<int32_t>(cut.reduces.size());
+      constexpr int32_t extents = kChainTile | kChainTile << 8;
+      for (const GemmReduce &r : s.reduces)
+        cut.reduces.push_back(ChainReduce{stage, r.block, r.m0, r.n0, r.slot0 + slot0, r.nslots, extents, 0});
+      for (const GemmItem &g : s.items)
+      {
+        const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(g.block)];
+        ChainItem it{stage, g.block, g.m0, g.n0, g.k0, g.k1, -1, -1, 0, extents};
+        if (g.slot >= 0)
+        {
+          it.slot = g.slot + slot0;
+          it.reduce = g.reduce + reduce0;
+        }
+        cut.items.push_back(it);
+        cut.work.push_back(item_work(std::min(kChainTile, blk.m - g.m0), std::min(kChainTile, blk.n - g.n0), g.k1 - g.k0));
+      }
+      cut.slots += s.slots;
+    }
+  } // namespace
+
+  int64_t chain_partial_slots(const Program &p)
+  {
+    if (p.chain_first < 0) return 0;
+    ChainCut cut;
+    cut_product(p, p.ops[static_cast<size_t>(p.chain_first)], 0, cut);
+    cut_product(p, p.ops[static_cast<size_t>(p.chain_second)], 1, cut);
+    return cut.slots;
+  }
+
+  namespace
+  {
+    // The items of both products, their work, and one list per SM dealt largest first onto the
+    // least loaded, the first product before the second; false when the counters do not fit the
+    // ticket region.
     bool build_chain(const Program &p, DeviceTables::ChainTables &ct, TableStaging &staging,
                      std::vector<ChainItem> &items, std::vector<int32_t> &cta_begin, std::vector<ChainReduce> &reduces)
     {
-      const Op &first = p.ops[static_cast<size_t>(p.chain_first)];
-      const Op &second = p.ops[static_cast<size_t>(p.chain_second)];
-      const GemmSchedule s1 = schedule_gemm(p, first, kChainTile, kChainTile, true);
-      const GemmSchedule s2 = schedule_gemm(p, second, kChainTile, kChainTile, true);
-      const int64_t n_reduces = static_cast<int64_t>(s1.reduces.size() + s2.reduces.size());
+      ChainCut cut;
+      cut_product(p, p.ops[static_cast<size_t>(p.chain_first)], 0, cut);
+      const size_t first_items = cut.items.size(), first_reduces = cut.reduces.size();
+      cut_product(p, p.ops[static_cast<size_t>(p.chain_second)], 1, cut);
+      // the workspace holds the partial tiles the plan was sized for
+      if (cut.slots > p.chain_slots) return false;
+      const int64_t n_reduces = static_cast<int64_t>(cut.reduces.size());
       // tickets of both products, then the first product's done count, the exit count, the error flag
       if (n_reduces + 3 > kTicketInts) return false;
-      reduces.clear();
-      for (const GemmReduce &r : s1.reduces) reduces.push_back(ChainReduce{0, r.block, r.m0, r.n0, r.slot0, r.nslots, 0, 0});
-      for (const GemmReduce &r : s2.reduces)
-        reduces.push_back(ChainReduce{1, r.block, r.m0, r.n0, static_cast<int32_t>(r.slot0 + s1.slots), r.nslots, 0, 0});
-      int64_t first_tiles = static_cast<int64_t>(s1.reduces.size());
+      reduces = cut.reduces;
+      int64_t first_tiles = static_cast<int64_t>(first_reduces);
       struct Sized
       {
         ChainItem item;
         double work;
       };
       std::vector<Sized> stage[2];
-      const auto sized = [&](const GemmItem &g, int32_t which) -> Sized
+      for (size_t i = 0; i < cut.items.size(); ++i)
       {
-        const GemmBlock &blk = p.gemm_blocks[static_cast<size_t>(g.block)];
-        ChainItem it{which, g.block, g.m0, g.n0, g.k0, g.k1, -1, -1, 0, 0};
-        if (g.slot >= 0)
-        {
-          it.slot = static_cast<int32_t>(g.slot + (which ? s1.slots : 0));
-          it.reduce = g.reduce + (which ? static_cast<int32_t>(s1.reduces.size()) : 0);
-        }
-        const double rows = std::min(kChainTile, blk.m - g.m0), cols = std::min(kChainTile, blk.n - g.n0);
-        return Sized{it, item_work(rows, cols, static_cast<double>(g.k1 - g.k0))};
-      };
-      for (const GemmItem &g : s1.items)
-      {
-        stage[0].push_back(sized(g, 0));
-        if (g.slot < 0) ++first_tiles;
+        stage[i < first_items ? 0 : 1].push_back(Sized{cut.items[i], cut.work[i]});
+        if (i < first_items && cut.items[i].slot < 0) ++first_tiles;
       }
-      for (const GemmItem &g : s2.items) stage[1].push_back(sized(g, 1));
       ct.host_items.clear();
       ct.host_work.clear();
       for (const std::vector<Sized> &st : stage)
@@ -170,7 +207,7 @@ namespace ttg
       ct.n_items = static_cast<int64_t>(items.size());
       ct.n_reduces = n_reduces;
       ct.first_tiles = first_tiles;
-      ct.slots = s1.slots + s2.slots;
+      ct.slots = cut.slots;
       staging.add(items, reinterpret_cast<void **>(const_cast<ChainItem **>(&ct.items)));
       staging.add(cta_begin, reinterpret_cast<void **>(const_cast<int32_t **>(&ct.cta_begin)));
       staging.add(reduces, reinterpret_cast<void **>(const_cast<ChainReduce **>(&ct.reduces)));
@@ -312,6 +349,20 @@ namespace ttg
 
     constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // two seconds
 
+    __device__ __forceinline__ void chain_sync(int worker)
+    {
+      asm volatile("bar.sync %0, %1;\n" ::"r"(worker + 1), "r"(kChainThreads) : "memory");
+    }
+    // The next entry of the CTA's own list for a worker.
+    __device__ __forceinline__ int64_t chain_claim(int worker, int lt, int *slot, int *taken)
+    {
+      if (lt == 0) *slot = atomicAdd(taken, 1);
+      chain_sync(worker);
+      const int64_t idx = *slot;
+      chain_sync(worker);
+      return idx;
+    }
+
     __device__ __forceinline__ unsigned long long global_ns()
     {
       unsigned long long t;
@@ -339,21 +390,32 @@ namespace ttg
         a.c[at] = v;
     }
 
-    // A second-product tile that covers the end of its block writes the block's alignment pad.
-    __device__ __forceinline__ void store_pad(const ChainWindow &a, int stage, const DevBlock &blk, int m0, int n0, int lt)
+    // A second-product tile that covers the end of its block (tile extents rows | cols << 8) writes
+    // the block's alignment pad.
+    __device__ __forceinline__ void store_pad(const ChainWindow &a, int stage, const DevBlock &blk, int m0, int n0, int extents, int lt)
     {
       const int64_t entries = static_cast<int64_t>(blk.m) * blk.n;
-      if (stage == 1 && lt == 0 && m0 + kChainTile >= blk.m && n0 + kChainTile >= blk.n && (entries & 1))
+      if (stage == 1 && lt == 0 && m0 + (extents & 0xff) >= blk.m && n0 + (extents >> 8) >= blk.n && (entries & 1))
         a.c[blk.c + entries] = 0.0;
     }
 
-    // A first-product tile is complete in the moved layout: count it done.  Every thread's fence
-    // orders its stores before the count.
-    __device__ __forceinline__ void signal_done(const ChainWindow &a, int worker, int lt)
+    // First-product tiles complete in the moved layout are counted per worker and program in
+    // shared memory (`pending`, the worker's row) and published once, before the worker's first
+    // wait and at its end: every thread's fence orders its stores before the counts (a
+    // second-product item waits for all of its program's first-product tiles, so publishing each
+    // tile as it completes would gain nothing).
+    __device__ __forceinline__ void publish_done(const ChainLaunch &L, int *pending, int worker, int lt)
     {
       __threadfence();
-      worker_sync(worker);
-      if (lt == 0) atomicAdd(a.done, 1);
+      chain_sync(worker);
+      if (lt == 0)
+        for (int w = 0; w < L.windows; ++w)
+          if (pending[w] != 0)
+          {
+            atomicAdd(L.w[w].done, pending[w]);
+            pending[w] = 0;
+          }
+      chain_sync(worker);
     }
 
     // A second-product item waits until every first-product tile of its program is done (one thread
@@ -374,22 +436,22 @@ namespace ttg
           __nanosleep(128);
         }
       }
-      worker_sync(worker);
+      chain_sync(worker);
       __threadfence();
     }
 
     // After a worker wrote a partial tile: the worker holding the tile's last ticket sums the
-    // partials in slot order (deterministic) and stores the tile; first-product tiles then signal.
-    __device__ void finish_chain_partial(const ChainWindow &a, int worker, int lt, int *flag, int reduce)
+    // partials in slot order (deterministic) and stores the tile; first-product tiles are counted.
+    __device__ void finish_chain_partial(const ChainWindow &a, int window, int *pending, int worker, int lt, int *flag, int reduce)
     {
-      constexpr int BM = kChainTile, BN = kChainTile, PER = BM * BN / kWorkerThreads;
+      constexpr int BM = kChainTile, BN = kChainTile, PER = BM * BN / kChainThreads;
       __threadfence();
-      worker_sync(worker);
+      chain_sync(worker);
       const ChainReduce r = a.reduces[reduce];
       if (lt == 0) *flag = atomicAdd(a.tickets + reduce, 1) == r.nslots - 1;
-      worker_sync(worker);
+      chain_sync(worker);
       const bool last = *flag;
-      worker_sync(worker);
+      chain_sync(worker);
       if (!last) return;
       if (lt == 0) a.tickets[reduce] = 0;
       __threadfence();
@@ -405,7 +467,7 @@ namespace ttg
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-          for (int k = 0; k < PER; ++k) v[u][k] = __ldcg(base + static_cast<int64_t>(s + u) * BM * BN + k * kWorkerThreads);
+          for (int k = 0; k < PER; ++k) v[u][k] = __ldcg(base + static_cast<int64_t>(s + u) * BM * BN + k * kChainThreads);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
@@ -413,153 +475,397 @@ namespace ttg
       }
       for (; s < r.nslots; ++s)
 #pragma unroll
-        for (int k = 0; k < PER; ++k) sum[k] += __ldcg(base + static_cast<int64_t>(s) * BM * BN + k * kWorkerThreads);
+        for (int k = 0; k < PER; ++k) sum[k] += __ldcg(base + static_cast<int64_t>(s) * BM * BN + k * kChainThreads);
 #pragma unroll
       for (int k = 0; k < PER; ++k)
       {
-        const int e = lt + k * kWorkerThreads;
-        const int gm = r.m0 + e / BN, gn = r.n0 + e % BN;
-        if (gm < blk.m && gn < blk.n) store_entry(a, r.stage, blk, gm, gn, sum[k]);
+        const int e = lt + k * kChainThreads, tr = e / BN, tc = e % BN;
+        const int gm = r.m0 + tr, gn = r.n0 + tc;
+        if (tr < (r.pad0 & 0xff) && tc < (r.pad0 >> 8) && gm < blk.m && gn < blk.n) store_entry(a, r.stage, blk, gm, gn, sum[k]);
       }
-      store_pad(a, r.stage, blk, r.m0, r.n0, lt);
-      if (r.stage == 0) signal_done(a, worker, lt);
+      store_pad(a, r.stage, blk, r.m0, r.n0, r.pad0, lt);
+      if (r.stage == 0 && lt == 0) ++pending[window];
     }
 
-    // The DMMA tile machinery of gemm_dmma_kernel (gemm.cu) over the items of both products: K in
-    // steps of 32 through two shared stages per worker, a 16 x 16 quarter of the 32 x 32 tile per
-    // warp.  The first product's operands and the second's B side are read-only during
-    // the launch and staged with cp.async; the second's A side (X', written during the launch by
-    // other SMs) is read with L2 loads, so that no SM reads a stale copy of a line from its L1.
-    __global__ void __launch_bounds__(kF64Workers * kWorkerThreads, 1) chain_dmma_kernel(const __grid_constant__ ChainLaunch L)
+    // A worker's place in an item: the block pair of its next K step, that step's first K within
+    // the pair and the end of the item's range in the pair.
+    struct Cursor
+    {
+      int32_t pi, kbase;  // the pair (index within the block) and its first K in the block's sum
+      int32_t k0, hi, K;  // the step's first K within the pair, the range's end there, the pair's K
+      int64_t a_off, b_off;
+    };
+
+    // The first step at or after pair c.pi (whose first K in the block's sum is c.kbase) that lies
+    // in the item's range; false when there is none.
+    __device__ __forceinline__ bool seek(const ChainWindow &a, const ChainItem &it, const DevBlock &blk, Cursor &c)
+    {
+      for (; c.pi < blk.pair_count; ++c.pi)
+      {
+        const DevPair pr = a.pairs[blk.pair_begin + c.pi];
+        const int32_t lo = max(it.k0 - c.kbase, 0), hi = min(it.k1 - c.kbase, pr.k);
+        if (lo < hi)
+        {
+          c.k0 = lo;
+          c.hi = hi;
+          c.K = pr.k;
+          c.a_off = pr.a;
+          c.b_off = pr.b;
+          return true;
+        }
+        c.kbase += pr.k;
+      }
+      return false;
+    }
+    __device__ __forceinline__ bool first_step(const ChainWindow &a, const ChainItem &it, const DevBlock &blk, Cursor &c)
+    {
+      c.pi = 0;
+      c.kbase = 0;
+      return seek(a, it, blk, c);
+    }
+    __device__ __forceinline__ bool next_step(const ChainWindow &a, const ChainItem &it, const DevBlock &blk, Cursor &c)
+    {
+      c.k0 += kDmmaStepK;
+      if (c.k0 < c.hi) return true;
+      c.kbase += c.K;
+      ++c.pi;
+      return seek(a, it, blk, c);
+    }
+
+    constexpr int kStageP = 36;                                      // shared row pitch (doubles)
+    constexpr int kXPer = kChainTile * kDmmaStepK / kChainThreads;  // a thread's X' entries of a step
+
+    // One K step's operands into a shared stage: the first product's both sides and the second's B
+    // side by cp.async (one group, committed by the caller); the second's A side (X', written during
+    // the launch by other SMs) by L2 loads into `xa`, which put_x stores once the stage is free.
+    __device__ __forceinline__ void load_step(const ChainWindow &a, const ChainItem &it, const DevBlock &blk, const Cursor &c,
+                                              double *as, double *bs, int lt, double (&xa)[kXPer])
+    {
+      constexpr int BM = kChainTile, BN = kChainTile, BK = kDmmaStepK, P = kStageP;
+      const bool second = it.stage == 1;
+      const double *pa = (second ? a.moved : a.a1) + c.a_off;
+      const double *pb = (second ? a.b2 : a.b1) + c.b_off;
+      const int th = it.pad & 0xff, tw = it.pad >> 8;
+      if (second)
+      {
+#pragma unroll
+        for (int j = 0; j < kXPer; ++j)
+        {
+          const int i = lt + j * kChainThreads, r = i / BK, kk = i % BK;
+          const int gm = it.m0 + r, gk = c.k0 + kk;
+          xa[j] = (r < th && gm < blk.m && gk < c.hi) ? __ldcg(pa + static_cast<int64_t>(gm) * c.K + gk) : 0.0;
+        }
+      }
+      else
+        for (int i = lt; i < th * BK; i += kChainThreads)
+        {
+          const int r = i / BK, kk = i % BK;
+          const int gm = it.m0 + r, gk = c.k0 + kk;
+          const bool in = gm < blk.m && gk < c.hi;
+          copy8(as + kk * P + r, in ? pa + static_cast<int64_t>(gm) * c.K + gk : pa, in);
+        }
+      for (int i = lt; i < BK * tw; i += kChainThreads)
+      {
+        const int kk = i / tw, cc = i - kk * tw;
+        const int gk = c.k0 + kk, gn = it.n0 + cc;
+        const bool in = gk < c.hi && gn < blk.n;
+        copy8(bs + kk * P + cc, in ? pb + static_cast<int64_t>(gk) * blk.n + gn : pb, in);
+      }
+    }
+    __device__ __forceinline__ void put_x(double *as, int lt, const double (&xa)[kXPer])
+    {
+#pragma unroll
+      for (int j = 0; j < kXPer; ++j)
+      {
+        const int i = lt + j * kChainThreads;
+        as[(i % kDmmaStepK) * kStageP + i / kDmmaStepK] = xa[j];
+      }
+    }
+
+    // An item's tile as the worker computes it.  Its live entries (rows x cols of the block) times
+    // R phases of K (R a power of two, the most that fit the worker's 2048 slots, at most the 32 K of
+    // a step) are the slots: slot v = entry * R + phase sums the products at K = phase, phase + R, ...
+    // of every step, so that a small tile still gives each thread up to eight independent chains
+    // (the FP64 unit of an SM quarter serves every warp on it in turn: a lone chain of dependent
+    // multiply-adds waits behind all of them).  Thread lt holds slots lt, lt + 256, ... (at most
+    // kPer, packed row | column << 8 | phase << 16); the phases of an entry are summed in order at
+    // the end of the item.
+    struct Layout
+    {
+      int mine, cols, live, shift;
+      int at[kPer];
+    };
+    __device__ __forceinline__ void layout_of(const ChainItem &it, const DevBlock &blk, int lt, Layout &l)
+    {
+      const int rows = min(it.pad & 0xff, blk.m - it.m0), cols = min(it.pad >> 8, blk.n - it.n0);
+      const int live = rows * cols;
+      int shift = 0;
+      while (shift < 5 && (live << (shift + 1)) <= kSlots) ++shift;
+      const int slots = live << shift;
+      l.cols = cols;
+      l.live = live;
+      l.shift = shift;
+      l.mine = slots > lt ? (slots - lt + kChainThreads - 1) / kChainThreads : 0;
+#pragma unroll
+      for (int i = 0; i < kPer; ++i)
+      {
+        const int v = min(lt + i * kChainThreads, max(slots - 1, 0));
+        const int e = v >> shift, r = e / cols;
+        l.at[i] = r | (e - r * cols) << 8 | (v & ((1 << shift) - 1)) << 16;
+      }
+    }
+
+    // The items of both products, each a 32 x 32 tile over a K range: K in steps of 32 through two
+    // shared stages per worker, the next step's operands (the next item's first step at the end of
+    // an item) in flight while a step is computed, and the tile's live entries computed by FP64
+    // fused multiply-adds, eight per thread.  GB300's FP64 pipe is shared by DMMA and DFMA and
+    // measured faster for DFMA (1.05 against 1.17 TFLOP/s on register operands, 1.05 against 1.20
+    // fed from shared memory), and an entry costs one lane: a 16 x 8 DMMA fragment would spend its
+    // whole width on the ragged edges of the small blocks of a two-site matvec (1.16 times the
+    // products' multiply-adds at bond 256).  The first product's operands and the second's B side
+    // are read-only during the launch and staged with cp.async; the second's A side (X', written
+    // during the launch by other SMs) is read with L2 loads, so that no SM reads a stale copy of a
+    // line from its L1.  A second-product item is waited for (its program's first-product tiles all
+    // done) only once the worker's current item is finished when that item is a first-product one.
+    __global__ void __launch_bounds__(kChainWorkers * kChainThreads, 1) chain_fp64_kernel(const __grid_constant__ ChainLaunch L)
     {
       dependent_entry();
-      constexpr int BM = kChainTile, BN = kChainTile, BK = kDmmaStepK, P = 36;
+      constexpr int BK = kDmmaStepK, P = kStageP, BN = kChainTile, BM = kChainTile;
       extern __shared__ __align__(16) unsigned char smem_raw[];
-      const int worker = threadIdx.x / kWorkerThreads, lt = threadIdx.x % kWorkerThreads;
-      double *stage_base = reinterpret_cast<double *>(smem_raw) + static_cast<size_t>(worker) * 2 * 2 * BK * P;
-      __shared__ int flags[kF64Workers];
-      __shared__ int next[kF64Workers];
+      const int worker = threadIdx.x / kChainThreads, lt = threadIdx.x % kChainThreads;
+      double *stage_base = reinterpret_cast<double *>(smem_raw) + static_cast<size_t>(worker) * (2 * 2 * BK * P + kSlots);
+      __shared__ int flags[kChainWorkers];
+      __shared__ int next[kChainWorkers];
       __shared__ int taken;
       __shared__ int last_out;
-      const int warp = lt >> 5, lane = lt & 31;
-      const int wm = warp >> 1, wn = warp & 1;
-      const int fr = lane >> 2, fk = lane & 3;
+      // first-product tiles done and not yet published, per worker and program
+      __shared__ int pending_all[kChainWorkers * kChainBatch];
+      int *pending = pending_all + worker * kChainBatch;
       if (threadIdx.x == 0) taken = 0;
+      for (int w = threadIdx.x; w < kChainWorkers * kChainBatch; w += blockDim.x) pending_all[w] = 0;
       __syncthreads();
       const int64_t list_begin = L.cta_begin[blockIdx.x], list_end = L.cta_begin[blockIdx.x + 1];
-      for (int64_t idx = list_begin + local_claim(worker, lt, next + worker, &taken); idx < list_end;
-           idx = list_begin + local_claim(worker, lt, next + worker, &taken))
+      const auto stage_a = [&](int buf) { return stage_base + buf * 2 * BK * P; };
+      // the phase sums of a finished item (kSlots doubles after the worker's two stages)
+      double *scratch = stage_base + 2 * 2 * BK * P;
+      const auto stage_b = [&](int buf) { return stage_base + buf * 2 * BK * P + BK * P; };
+
+      // the epilogue of a finished item (`val` holds its slots, then its entries): the phases of
+      // each entry summed (through `scratch` when there are several),
+      // then its entries stored (through the move for the first product, and counted) or its
+      // partial tile written and, by the tile's last finisher, summed
+      const auto finish = [&](const ChainItem &it, const DevBlock &blk, const Layout &l, double (&val)[kPer], double *scratch)
       {
-        const ChainItem it = L.items[idx];
         const ChainWindow &a = L.w[it.window];
-        const bool second = it.stage == 1;
-        const DevBlock blk = a.blocks[it.block];
-        if (second) wait_first(a, L.error, worker, lt);
-        const double *A = second ? a.moved : a.a1;
-        const double *B = second ? a.b2 : a.b1;
-        double acc[2][4] = {};
-        const bool live_i = it.m0 + wm * 16 < blk.m;
-        const bool live_j[2] = {it.n0 + wn * 16 < blk.n, it.n0 + wn * 16 + 8 < blk.n};
-        int32_t kbase = 0;
-        for (int32_t pi = 0; pi < blk.pair_count; ++pi)
+        if (l.shift != 0)
         {
-          const DevPair pr = a.pairs[blk.pair_begin + pi];
-          const int K = pr.k;
-          const int lo = max(it.k0 - kbase, 0), hi = min(it.k1 - kbase, K);
-          kbase += K;
-          if (lo >= hi) continue;
-          const double *pa = A + pr.a;
-          const double *pb = B + pr.b;
-          const auto load = [&](int stage, int k0)
+#pragma unroll
+          for (int i = 0; i < kPer; ++i)
+            if (i < l.mine) scratch[lt + i * kChainThreads] = val[i];
+          chain_sync(worker);
+          const int phases = 1 << l.shift;
+#pragma unroll
+          for (int j = 0; j < kPer; ++j)
           {
-            double *as = stage_base + stage * 2 * BK * P, *bs = as + BK * P;
-            if (second)
-            {
-              // X': plain L2 loads into shared memory
-              for (int i = lt; i < BM * BK; i += kWorkerThreads)
-              {
-                const int r = i / BK, kk = i % BK;
-                const int gm = it.m0 + r, gk = k0 + kk;
-                as[kk * P + r] = (gm < blk.m && gk < hi) ? __ldcg(pa + static_cast<int64_t>(gm) * K + gk) : 0.0;
-              }
-            }
-            else
-              for (int i = lt; i < BM * BK; i += kWorkerThreads)
-              {
-                const int r = i / BK, kk = i % BK;
-                const int gm = it.m0 + r, gk = k0 + kk;
-                const bool in = gm < blk.m && gk < hi;
-                copy8(as + kk * P + r, in ? pa + static_cast<int64_t>(gm) * K + gk : pa, in);
-              }
-            for (int i = lt; i < BK * BN; i += kWorkerThreads)
-            {
-              const int kk = i / BN, cc = i % BN;
-              const int gk = k0 + kk, gn = it.n0 + cc;
-              const bool in = gk < hi && gn < blk.n;
-              copy8(bs + kk * P + cc, in ? pb + static_cast<int64_t>(gk) * blk.n + gn : pb, in);
-            }
-            copy_commit();
-          };
-          load(0, lo);
-          int stage = 0;
-          for (int k0 = lo; k0 < hi; k0 += BK, stage ^= 1)
-          {
-            if (k0 + BK < hi)
-              load(stage ^ 1, k0 + BK);
-            else
-              copy_commit();  // an empty group keeps the count of the wait below
-            copy_wait_one();
-            worker_sync(worker);
-            const double(*as)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P);
-            const double(*bs)[P] = reinterpret_cast<const double(*)[P]>(stage_base + stage * 2 * BK * P + BK * P);
-            const int steps = min(BK, hi - k0);
-            const auto step_k = [&](int kb, double (&into)[2][4])
-            {
-              double af[4], bf[2][2];
-#pragma unroll
-              for (int h = 0; h < 4; ++h) af[h] = as[kb + fk + (h >> 1) * 4][wm * 16 + (h & 1) * 8 + fr];
-#pragma unroll
-              for (int j = 0; j < 2; ++j)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) bf[j][h] = bs[kb + fk + h * 4][wn * 16 + j * 8 + fr];
-#pragma unroll
-              for (int j = 0; j < 2; ++j)
-                if (live_j[j]) dmma16(into[j], af, bf[j]);
-            };
-            if (live_i && live_j[0])
-            {
-              if (steps == BK)
-              {
-#pragma unroll
-                for (int kb = 0; kb < BK; kb += 8) step_k(kb, acc);
-              }
-              else
-                for (int kb = 0; kb < steps; kb += 8) step_k(kb, acc);
-            }
-            worker_sync(worker);
+            const int e = lt + j * kChainThreads;
+            double sum = 0.0;
+            if (e < l.live)
+              for (int q = 0; q < phases; ++q) sum += scratch[(e << l.shift) + q];
+            val[j] = sum;
           }
+          chain_sync(worker);  // the scratch is written again after this
         }
+        const int entries = l.live > lt ? (l.live - lt + kChainThreads - 1) / kChainThreads : 0;
         if (it.slot >= 0)
         {
           double *out = a.partial + static_cast<int64_t>(it.slot) * BM * BN;
 #pragma unroll
-          for (int j = 0; j < 2; ++j)
-#pragma unroll
-            for (int h = 0; h < 4; ++h) out[(wm * 16 + (h >> 1) * 8 + fr) * BN + wn * 16 + j * 8 + fk * 2 + (h & 1)] = acc[j][h];
-          finish_chain_partial(a, worker, lt, flags + worker, it.reduce);
-          continue;
+          for (int j = 0; j < kPer; ++j)
+            if (j < entries)
+            {
+              const int e = lt + j * kChainThreads, r = e / l.cols;
+              out[r * BN + (e - r * l.cols)] = val[j];
+            }
+          finish_chain_partial(a, it.window, pending, worker, lt, flags + worker, it.reduce);
+          return;
         }
 #pragma unroll
-        for (int j = 0; j < 2; ++j)
-#pragma unroll
-          for (int h = 0; h < 4; ++h)
+        for (int j = 0; j < kPer; ++j)
+          if (j < entries)
           {
-            const int gm = it.m0 + wm * 16 + (h >> 1) * 8 + fr, gn = it.n0 + wn * 16 + j * 8 + fk * 2 + (h & 1);
-            if (gm < blk.m && gn < blk.n) store_entry(a, it.stage, blk, gm, gn, acc[j][h]);
+            const int e = lt + j * kChainThreads, r = e / l.cols;
+            store_entry(a, it.stage, blk, it.m0 + r, it.n0 + (e - r * l.cols), val[j]);
           }
-        store_pad(a, it.stage, blk, it.m0, it.n0, lt);
-        if (!second) signal_done(a, worker, lt);
+        store_pad(a, it.stage, blk, it.m0, it.n0, it.pad, lt);
+        if (it.stage == 0 && lt == 0) ++pending[it.window];
+      };
+
+      // claim the worker's next item, wait for it when it is a second-product one, and place its
+      // first step; items with no K (a block that no pair feeds) are stored as zeros on the way
+      ChainItem it{};
+      DevBlock blk{};
+      Cursor cur{};
+      double xa[kXPer];
+      // set once the worker's first-product counts are published (the CTA's list holds all its
+      // first-product items first)
+      bool published = false;
+      const auto open = [&]() -> bool
+      {
+        for (;;)
+        {
+          const int64_t idx = list_begin + chain_claim(worker, lt, next + worker, &taken);
+          if (idx >= list_end) return false;
+          it = L.items[idx];
+          blk = L.w[it.window].blocks[it.block];
+          if (it.stage == 1)
+          {
+            if (!published) publish_done(L, pending, worker, lt);
+            published = true;
+            wait_first(L.w[it.window], L.error, worker, lt);
+          }
+          if (first_step(L.w[it.window], it, blk, cur)) return true;
+          Layout l;
+          layout_of(it, blk, lt, l);
+          l.shift = 0;  // nothing to sum
+          double zero[kPer];
+#pragma unroll
+          for (int i = 0; i < kPer; ++i) zero[i] = 0.0;
+          finish(it, blk, l, zero, nullptr);
+        }
+      };
+
+      int buf = 0;
+      bool have = open();
+      if (have)
+      {
+        load_step(L.w[it.window], it, blk, cur, stage_a(0), stage_b(0), lt, xa);
+        if (it.stage == 1) put_x(stage_a(0), lt, xa);
       }
+      copy_commit();
+      while (have)
+      {
+        Layout l;
+        layout_of(it, blk, lt, l);
+        double acc[kPer];
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) acc[i] = 0.0;
+        // the steps of the item; `follow` is set when the next item's first step was prefetched
+        bool follow = false, have_next = false;
+        ChainItem nit{};
+        DevBlock nblk{};
+        Cursor ncur{};
+        for (;;)
+        {
+          Cursor step = cur;
+          const bool more = next_step(L.w[it.window], it, blk, step);
+          bool pending_x = false;
+          if (more)
+          {
+            load_step(L.w[it.window], it, blk, step, stage_a(buf ^ 1), stage_b(buf ^ 1), lt, xa);
+            pending_x = it.stage == 1;
+          }
+          else
+          {
+            // the item's last step: claim the next item now and prefetch its first step unless it
+            // would wait on first-product tiles while this worker still holds one
+            const int64_t idx = list_begin + chain_claim(worker, lt, next + worker, &taken);
+            have_next = idx < list_end;
+            if (have_next)
+            {
+              nit = L.items[idx];
+              nblk = L.w[nit.window].blocks[nit.block];
+              if ((nit.stage == 0 || it.stage == 1))
+              {
+                if (nit.stage == 1)
+                {
+                  if (!published) publish_done(L, pending, worker, lt);
+                  published = true;
+                  wait_first(L.w[nit.window], L.error, worker, lt);
+                }
+                if (first_step(L.w[nit.window], nit, nblk, ncur))
+                {
+                  load_step(L.w[nit.window], nit, nblk, ncur, stage_a(buf ^ 1), stage_b(buf ^ 1), lt, xa);
+                  pending_x = nit.stage == 1;
+                  follow = true;
+                }
+              }
+            }
+          }
+          copy_commit();  // an empty group when nothing was issued keeps the count of the wait below
+          copy_wait_one();
+          chain_sync(worker);
+          {
+            const double(*as)[P] = reinterpret_cast<const double(*)[P]>(stage_a(buf));
+            const double(*bs)[P] = reinterpret_cast<const double(*)[P]>(stage_b(buf));
+            const int steps = min(BK, cur.hi - cur.k0);
+            if (l.shift == 0 && l.mine == kPer && l.cols == BN)
+            {
+              // a full tile: the thread's entries share one column
+              const int c = (l.at[0] >> 8) & 0xff;
+#pragma unroll 4
+              for (int kk = 0; kk < steps; ++kk)
+              {
+                const double b = bs[kk][c];
+#pragma unroll
+                for (int i = 0; i < kPer; ++i) acc[i] = fma(as[kk][l.at[i] & 0xff], b, acc[i]);
+              }
+            }
+            else
+            {
+              const int phases = 1 << l.shift;
+              for (int kb = 0; kb < steps; kb += phases)
+              {
+#pragma unroll
+                for (int i = 0; i < kPer; ++i)
+                {
+                  const int kk = kb + (l.at[i] >> 16);
+                  if (i < l.mine && kk < steps) acc[i] = fma(as[kk][l.at[i] & 0xff], bs[kk][(l.at[i] >> 8) & 0xff], acc[i]);
+                }
+              }
+            }
+          }
+          chain_sync(worker);
+          if (pending_x) put_x(stage_a(buf ^ 1), lt, xa);
+          buf ^= 1;
+          if (!more) break;
+          cur = step;
+        }
+        finish(it, blk, l, acc, scratch);
+        if (!have_next) break;
+        if (follow)
+        {
+          it = nit;
+          blk = nblk;
+          cur = ncur;
+          continue;
+        }
+        // the claimed item was not prefetched (a second-product item after a first-product one,
+        // or one with no K): wait for it now, then go on from it
+        it = nit;
+        blk = nblk;
+        if (it.stage == 1)
+        {
+          if (!published) publish_done(L, pending, worker, lt);
+          published = true;
+          wait_first(L.w[it.window], L.error, worker, lt);
+        }
+        if (!first_step(L.w[it.window], it, blk, cur))
+        {
+          Layout z;
+          layout_of(it, blk, lt, z);
+          z.shift = 0;  // nothing to sum
+          double zero[kPer];
+#pragma unroll
+          for (int i = 0; i < kPer; ++i) zero[i] = 0.0;
+          finish(it, blk, z, zero, nullptr);
+          have = open();
+          if (!have) break;
+        }
+        load_step(L.w[it.window], it, blk, cur, stage_a(buf), stage_b(buf), lt, xa);
+        if (it.stage == 1) put_x(stage_a(buf), lt, xa);
+        copy_commit();
+      }
+      if (!published) publish_done(L, pending, worker, lt);
       // the last CTA to leave resets the done counts and the exit count for the next launch
       __syncthreads();
       if (threadIdx.x == 0)
@@ -601,13 +907,13 @@ namespace ttg
 
     cudaError_t launch_chain(const ChainLaunch &launch, int32_t n_ctas, int64_t longest, cudaStream_t stream)
     {
-      const int bytes = std::max<int>(kF64Workers * 2 * 2 * kDmmaStepK * 36 * 8, kChainPinBytes);
+      const int bytes = std::max<int>(kChainWorkers * (2 * 2 * kDmmaStepK * kStageP + kSlots) * 8, kChainPinBytes);
       static std::once_flag once;
       cudaError_t e = cudaSuccess;
-      std::call_once(once, [&] { e = cudaFuncSetAttribute(chain_dmma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
+      std::call_once(once, [&] { e = cudaFuncSetAttribute(chain_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes); });
       if (e != cudaSuccess) return e;
-      const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kF64Workers));
-      return launch_dependent(chain_dmma_kernel, n_ctas, workers * kWorkerThreads, bytes, stream, launch);
+      const int workers = static_cast<int>(std::clamp<int64_t>(longest, 1, kChainWorkers));
+      return launch_dependent(chain_fp64_kernel, n_ctas, workers * kChainThreads, bytes, stream, launch);
     }
 
     // The deal of a batch's items, per list of programs.

@@ -350,8 +350,11 @@ namespace ttg
       need = std::max(need, (f64_bytes(plans->f64[i]) + 7) / 8);
       // a chain's one launch holds the partial tiles of both its products at once
       if (static_cast<int32_t>(i) == p.chain_second)
-        need = std::max(need, (up256((plans->f64[static_cast<size_t>(p.chain_first)].slots + plans->f64[i].slots) *
-                                     kF64TileM * kF64TileN * 8) + 7) / 8);
+      {
+        // its items are cut for the FMA kernel (chain.cu)
+        p.chain_slots = chain_partial_slots(p);
+        need = std::max(need, (up256(p.chain_slots * kF64TileM * kF64TileN * 8) + 7) / 8);
+      }
       const SplitSchedule sizes = schedule_split(p, op, false);
       need = std::max(need, (split_bytes(sizes, kMaxSlices) + 7) / 8);
       // the slices of a prepared operand's value go into its arena

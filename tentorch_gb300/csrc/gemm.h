@@ -93,6 +93,9 @@ namespace ttg
   // The FP64 schedule of a GEMM op; with full = false only its sizes (items, partial slots,
   // reductions), for sizing the scratch: the items are dealt on the op's first FP64 launch.
   GemmSchedule schedule_gemm(const Program &p, const Op &op, int bm, int bn, bool full = true);
+  // The partial tiles (32 x 32 doubles each) the one launch of a program's product chain may hold
+  // (chain.cu; 0 without a chain).
+  int64_t chain_partial_slots(const Program &p);
 
   // Scratch doubles a program's GEMM ops need at most (FP64 partials, or slices + exponents +
   // partials for split precision), laid out per op from offset 0.

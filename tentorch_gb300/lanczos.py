@@ -109,8 +109,15 @@ def lanczos_einsum(spec: str, tensors, vector: int, start: Tensor, n_iter: int =
     data = start._data
     device = data.device
     stream = torch.cuda.current_stream(device).cuda_stream
+    capturing = torch.cuda.is_current_stream_capturing()
+    if capturing:
+        linalg._note_capture()
     ws = linalg._workspace(plan, device, data.dtype, stream)
-    prepared = [None if i == vector else linalg._prepared_arena(plan, i, t, ws, stream, force = True)
+    # under a CUDA graph capture the operands are prepared inside the graph (each replay reads the
+    # head and tail from their buffers) and the prepared copies are not cached
+    prepared = [None if i == vector else
+                (linalg._prepare_now(plan, i, t, ws, stream) if capturing else
+                 linalg._prepared_arena(plan, i, t, ws, stream, force = True))
                 for i, t in enumerate(operands)]
     doubles = i64()
     check(lib.tt_lanczos_scratch(start._space.size, n_iter, linalg._DTYPE[data.dtype], ctypes.byref(doubles)))

@@ -216,6 +216,18 @@ def _prepared_arena(plan: Plan, operand: int, tensor: Tensor, ws, stream, force:
     return arena
 
 
+def _prepare_now(plan: Plan, operand: int, tensor: Tensor, ws, stream) -> Optional[torch.Tensor]:
+    '''The operand prepared into a new arena, not cached (the form a CUDA graph captures).'''
+    size = plan.prepared_size(operand)
+    if size <= 0:
+        return None
+    data = tensor._data
+    arena = torch.empty(size, dtype = data.dtype, device = data.device)
+    check(lib.tt_plan_prepare(plan.handle, _DTYPE[data.dtype], operand, data.data_ptr(), arena.data_ptr(),
+                              ws.data_ptr() if ws is not None else None, stream))
+    return arena
+
+
 def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool = True) -> Tensor:
     """Execute a plan on the operands' device and return the output tensor."""
     _check_device(tensors)
@@ -224,11 +236,11 @@ def run(plan: Plan, tensors, out: Optional[Tensor] = None, reuse_prepared: bool 
     if out is None:
         out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = data0.dtype, device = device))
     stream = torch.cuda.current_stream(device).cuda_stream
-    ws = _workspace(plan, device, data0.dtype, stream)
     # a captured CUDA graph reads every operand from its own buffer at each replay, never a prepared copy
     if torch.cuda.is_current_stream_capturing():
         _note_capture()
         reuse_prepared = False
+    ws = _workspace(plan, device, data0.dtype, stream)
     prepared = [(_prepared_arena(plan, i, t, ws, stream) if reuse_prepared else None) for i, t in enumerate(tensors)]
     inputs = pointers(t._data.data_ptr() for t in tensors)
     prep = pointers((p.data_ptr() if p is not None else None) for p in prepared)
@@ -312,7 +324,9 @@ def einsum_batch(spec: str, operand_lists, outcharge = None) -> list:
     the two-site matvecs of many windows (different bond dimensions allowed) run as ONE persistent
     launch with their work items dealt together over the SMs; in split precision, or for equations
     that are not a product chain, one window after another.  At most 64 windows per launch (longer
-    lists are cut into launches of 64).  Operands are prepared per window as `einsum` prepares them.'''
+    lists are cut into launches of 64).  Operands are prepared per window as `einsum` prepares them;
+    under a CUDA graph capture every operand is read from its buffer (a warm-up call outside the
+    capture compiles the plans and deals the batch first).'''
     global last_batch_launches
     operand_lists = [list(ops) for ops in operand_lists]
     if len(operand_lists) > 64:
@@ -322,6 +336,10 @@ def einsum_batch(spec: str, operand_lists, outcharge = None) -> list:
     first = operand_lists[0][0]
     device, dtype = first._data.device, first._data.dtype
     stream = torch.cuda.current_stream(device).cuda_stream
+    # a captured CUDA graph reads every operand from its own buffer at each replay
+    capturing = torch.cuda.is_current_stream_capturing()
+    if capturing:
+        _note_capture()
     handles, outs, keep, inputs, prepared, workspaces = [], [], [], [], [], []
     for w, ops in enumerate(operand_lists):
         _check_device(ops)
@@ -332,7 +350,7 @@ def einsum_batch(spec: str, operand_lists, outcharge = None) -> list:
             if pool is not None and _captured:
                 _superseded.append(pool)
             pool = _batch_pools[key] = torch.zeros(max(plan.workspace, 1 << 16), dtype = dtype, device = device)
-        prep = [_prepared_arena(plan, i, t, pool, stream) for i, t in enumerate(ops)]
+        prep = [None if capturing else _prepared_arena(plan, i, t, pool, stream) for i, t in enumerate(ops)]
         out = Tensor._wrap(plan.out_space, torch.empty(plan.out_space.size, dtype = dtype, device = device))
         handles.append(plan.handle.value)
         outs.append(out)
