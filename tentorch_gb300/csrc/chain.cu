@@ -150,8 +150,9 @@ namespace ttg
       // the workspace holds the partial tiles the plan was sized for
       if (cut.slots > p.chain_slots) return false;
       const int64_t n_reduces = static_cast<int64_t>(cut.reduces.size());
-      // tickets of both products, then the first product's done count, the exit count, the error flag
-      if (n_reduces + 3 > kTicketInts) return false;
+      // tickets of both products, then the first product's done count, the exit count, the error
+      // flag and the count of CTAs that zeroed the partial-tile accumulators
+      if (n_reduces + 4 > kTicketInts) return false;
       reduces = cut.reduces;
       int64_t first_tiles = static_cast<int64_t>(first_reduces);
       struct Sized
@@ -334,6 +335,7 @@ namespace ttg
       int *tickets;         // one per reduce (left zero by the last finisher of the tile)
       int *done;            // first-product tiles done so far (reset by the last CTA out)
       int32_t first_tiles;  // first-product tiles (items that cover their tile, and reductions)
+      int32_t accumulators; // partial-tile accumulators (32 x 32 doubles each, one per cut tile)
     };
     // A launch: the dealt items of every program (ChainItem::window names its program) and the
     // programs themselves, passed by value (a kernel parameter of a few KiB).
@@ -343,6 +345,7 @@ namespace ttg
       const int32_t *cta_begin;
       int *exit_count;  // CTAs done (reset by the last)
       int *error;       // set when a wait gave up
+      int *zeroed;      // CTAs that zeroed their share of the accumulators (reset by the last out)
       int32_t windows;
       ChainWindow w[kChainBatch];
     };
@@ -418,15 +421,15 @@ namespace ttg
       chain_sync(worker);
     }
 
-    // A second-product item waits until every first-product tile of its program is done (one thread
-    // polls with acquire loads, the worker's barrier releases the rest); after two seconds it raises
-    // the error flag and goes on.
-    __device__ __forceinline__ void wait_first(const ChainWindow &a, int *error, int worker, int lt)
+    // A worker waits until a counter reaches its target (one thread polls with acquire loads, the
+    // worker's barrier releases the rest); after two seconds it raises the error flag and goes on.
+    // A second-product item waits until every first-product tile of its program is done.
+    __device__ __forceinline__ void wait_count(const int *count, int target, int *error, int worker, int lt)
     {
       if (lt == 0)
       {
         const unsigned long long start = global_ns();
-        while (load_acquire(a.done) < a.first_tiles)
+        while (load_acquire(count) < target)
         {
           if (global_ns() - start > kWaitLimitNs)
           {
@@ -439,15 +442,39 @@ namespace ttg
       chain_sync(worker);
       __threadfence();
     }
+    __device__ __forceinline__ void wait_first(const ChainWindow &a, int *error, int worker, int lt)
+    {
+      wait_count(a.done, a.first_tiles, error, worker, lt);
+    }
 
-    // After a worker wrote a partial tile: the worker holding the tile's last ticket sums the
-    // partials in slot order (deterministic) and stores the tile; first-product tiles are counted.
+    // After a worker added its partial tile into the tile's accumulator (zeroed at the start of
+    // the launch): the worker holding the tile's last ticket reads the sum and stores the tile
+    // (first-product tiles through the move, counted).  The partial tiles are summed by FP64
+    // atomic additions in L2, in the order their items finish: a tile's value is the same up to
+    // the rounding of that order (a few units in the last place over its K chunks), while a sum
+    // of separate partial tiles by the last finisher would cost it a round trip to L2 per group of
+    // partials at the end of the product.  The move's targets of the tile's entries are read
+    // before the ticket, to overlap that latency.
     __device__ void finish_chain_partial(const ChainWindow &a, int window, int *pending, int worker, int lt, int *flag, int reduce)
     {
-      constexpr int BM = kChainTile, BN = kChainTile, PER = BM * BN / kChainThreads;
+      constexpr int BN = kChainTile, PER = kChainTile * kChainTile / kChainThreads;
+      const ChainReduce r = a.reduces[reduce];
+      const DevBlock blk = a.blocks[r.block];
+      int64_t at[PER];
+#pragma unroll
+      for (int k = 0; k < PER; ++k)
+      {
+        const int e = lt + k * kChainThreads, tr = e / BN, tc = e % BN;
+        const int gm = r.m0 + tr, gn = r.n0 + tc;
+        at[k] = -1;
+        if (tr < (r.pad0 & 0xff) && tc < (r.pad0 >> 8) && gm < blk.m && gn < blk.n)
+        {
+          at[k] = blk.c + static_cast<int64_t>(gm) * blk.n + gn;
+          if (r.stage == 0) at[k] = __ldg(a.relabel + at[k]);
+        }
+      }
       __threadfence();
       chain_sync(worker);
-      const ChainReduce r = a.reduces[reduce];
       if (lt == 0) *flag = atomicAdd(a.tickets + reduce, 1) == r.nslots - 1;
       chain_sync(worker);
       const bool last = *flag;
@@ -455,34 +482,13 @@ namespace ttg
       if (!last) return;
       if (lt == 0) a.tickets[reduce] = 0;
       __threadfence();
-      const DevBlock blk = a.blocks[r.block];
-      double sum[PER];
+      double *sum = a.partial + static_cast<int64_t>(reduce) * kChainTile * kChainTile + lt;
+      double v[PER];
 #pragma unroll
-      for (int k = 0; k < PER; ++k) sum[k] = 0.0;
-      const double *base = a.partial + static_cast<int64_t>(r.slot0) * BM * BN + lt;
-      int s = 0;
-      for (; s + 4 <= r.nslots; s += 4)
-      {
-        double v[4][PER];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int k = 0; k < PER; ++k) v[u][k] = __ldcg(base + static_cast<int64_t>(s + u) * BM * BN + k * kChainThreads);
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int k = 0; k < PER; ++k) sum[k] += v[u][k];
-      }
-      for (; s < r.nslots; ++s)
-#pragma unroll
-        for (int k = 0; k < PER; ++k) sum[k] += __ldcg(base + static_cast<int64_t>(s) * BM * BN + k * kChainThreads);
+      for (int k = 0; k < PER; ++k) v[k] = __ldcg(sum + k * kChainThreads);
 #pragma unroll
       for (int k = 0; k < PER; ++k)
-      {
-        const int e = lt + k * kChainThreads, tr = e / BN, tc = e % BN;
-        const int gm = r.m0 + tr, gn = r.n0 + tc;
-        if (tr < (r.pad0 & 0xff) && tc < (r.pad0 >> 8) && gm < blk.m && gn < blk.n) store_entry(a, r.stage, blk, gm, gn, sum[k]);
-      }
+        if (at[k] >= 0) (r.stage == 0 ? a.moved : a.c)[at[k]] = v[k];
       store_pad(a, r.stage, blk, r.m0, r.n0, r.pad0, lt);
       if (r.stage == 0 && lt == 0) ++pending[window];
     }
@@ -643,11 +649,22 @@ namespace ttg
       int *pending = pending_all + worker * kChainBatch;
       if (threadIdx.x == 0) taken = 0;
       for (int w = threadIdx.x; w < kChainWorkers * kChainBatch; w += blockDim.x) pending_all[w] = 0;
+      // the partial-tile accumulators (in the workspace's scratch, which other launches also use)
+      // zeroed by all CTAs together before any item adds into them
+      for (int w = 0; w < L.windows; ++w)
+      {
+        const int64_t n = static_cast<int64_t>(L.w[w].accumulators) * kChainTile * kChainTile;
+        for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+          __stcg(L.w[w].partial + i, 0.0);
+      }
+      __threadfence();
       __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(L.zeroed, 1);
       const int64_t list_begin = L.cta_begin[blockIdx.x], list_end = L.cta_begin[blockIdx.x + 1];
       const auto stage_a = [&](int buf) { return stage_base + buf * 2 * BK * P; };
       // the phase sums of a finished item (kSlots doubles after the worker's two stages)
       double *scratch = stage_base + 2 * 2 * BK * P;
+      bool zero_seen = false;  // set once the partial-tile accumulators are known to be zeroed
       const auto stage_b = [&](int buf) { return stage_base + buf * 2 * BK * P + BK * P; };
 
       // the epilogue of a finished item (`val` holds its slots, then its entries): the phases of
@@ -678,13 +695,19 @@ namespace ttg
         const int entries = l.live > lt ? (l.live - lt + kChainThreads - 1) / kChainThreads : 0;
         if (it.slot >= 0)
         {
-          double *out = a.partial + static_cast<int64_t>(it.slot) * BM * BN;
+          // added into the tile's accumulator, once every CTA has zeroed its share
+          if (!zero_seen)
+          {
+            wait_count(L.zeroed, static_cast<int>(gridDim.x), L.error, worker, lt);
+            zero_seen = true;
+          }
+          double *out = a.partial + static_cast<int64_t>(it.reduce) * BM * BN;
 #pragma unroll
           for (int j = 0; j < kPer; ++j)
             if (j < entries)
             {
               const int e = lt + j * kChainThreads, r = e / l.cols;
-              out[r * BN + (e - r * l.cols)] = val[j];
+              atomicAdd(out + r * BN + (e - r * l.cols), val[j]);
             }
           finish_chain_partial(a, it.window, pending, worker, lt, flags + worker, it.reduce);
           return;
@@ -878,7 +901,11 @@ namespace ttg
       {
         __threadfence();
         for (int w = threadIdx.x; w < L.windows; w += blockDim.x) *L.w[w].done = 0;
-        if (threadIdx.x == 0) *L.exit_count = 0;
+        if (threadIdx.x == 0)
+        {
+          *L.exit_count = 0;
+          *L.zeroed = 0;
+        }
       }
     }
 
@@ -902,6 +929,7 @@ namespace ttg
       w.tickets = static_cast<int *>(workspace);
       w.done = w.tickets + ct.n_reduces;
       w.first_tiles = static_cast<int32_t>(ct.first_tiles);
+      w.accumulators = static_cast<int32_t>(ct.n_reduces);
       return w;
     }
 
@@ -965,6 +993,7 @@ namespace ttg
     launch.w[0] = window_of(p, t, A1, B1, moved, B2, C, workspace);
     launch.exit_count = launch.w[0].done + 1;
     launch.error = launch.exit_count + 1;
+    launch.zeroed = launch.error + 1;
     e = launch_chain(launch, ct.n_ctas, ct.longest, stream);
     if (e == cudaSuccess) *used = true;
     return e;
@@ -1060,6 +1089,7 @@ namespace ttg
     // the launch's exit count and error flag after the first program's done count
     launch.exit_count = launch.w[0].done + 1;
     launch.error = launch.exit_count + 1;
+    launch.zeroed = launch.error + 1;
     const cudaError_t e = launch_chain(launch, deal.n_ctas, deal.longest, stream);
     if (e == cudaSuccess) *used = true;
     return e;
