@@ -184,6 +184,13 @@ namespace ttg
       std::vector<std::vector<ChainItem>> per_cta(static_cast<size_t>(ctas));
       for (std::vector<Sized> &st : stage)
       {
+        // the second product starts on every SM when the first is done everywhere: its items are
+        // balanced on their own
+        if (&st == &stage[1])
+        {
+          for (auto &h : heap) h.first = 0.0;
+          std::make_heap(heap.begin(), heap.end(), later);
+        }
         std::stable_sort(st.begin(), st.end(), [](const Sized &a, const Sized &b) { return a.work > b.work; });
         for (const Sized &one : st)
         {
