@@ -424,6 +424,15 @@ def run_gpu(args, rank, world):
             got = tg.einsum(MATVEC, head, tail, theta)
         parity[name] = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.blocks.items()) / scale
 
+    # the autotuner picks each grouped form's launch forms for this histogram (cached; the timed
+    # steps run the choice)
+    tuned = {}
+    for name, form in (('split', args.precision), ('fp64_grouped', 0)):
+        with tg.precision(form):
+            forms, tune_ms = tg.linalg.autotune(MATVEC, head, tail, vectors[0])
+        tuned[name] = {'forms': forms, 'ms': tune_ms}
+    tuned['histogram_key'] = f'{tg.linalg.histogram_key(plan):016x}'
+
     for form in (args.precision, 0, PER_BLOCK):
         tg.set_precision(form)
         for i in range(args.warmup):
@@ -549,6 +558,8 @@ def run_gpu(args, rank, world):
                 'parity_vs_oracle': parity,
                 'roofline': roofline,
                 'roofline_fp64_grouped': roofline_fp64,
+                'autotune': dict(tuned, meaning = 'forms bits: 1 product chain as separate launches, '
+                                                  '2 split products off the tensor cores; ms: median of the choice'),
                 'dmrg': dmrg,
                 'cpu_baseline': {'value': cpu_value, 'unit': 'matvecs/s', 'cores': os.cpu_count(), 'kind': 'port',
                                  'sample': f'{cpu_n} matvecs at chi={args.chi} of the oracle port of tentorch einsum '

@@ -159,6 +159,30 @@ int32_t tt_plan_execute_batch(int32_t count, const tt_plan *const *plans, int32_
 int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                               const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
                               float *op_ms, int32_t *op_kind);
+/* ---- autotuning (replaces a fixed choice of kernel forms; SURVEY item "tt_autotune_lookup") --- */
+
+/* The forms a plan's block products run in, as bits: TT_FORM_SEPARATE runs a product chain (two
+ * products with the leg move between them, the two-site matvec) as separate launches instead of
+ * one; TT_FORM_NO_TENSOR_CORES keeps split-precision products of large blocks on the mma.sync
+ * kernel instead of the tcgen05 one.  Executions use the forms cached for the plan's block-size
+ * histogram (0 when none is cached). */
+#define TT_FORM_SEPARATE 1
+#define TT_FORM_NO_TENSOR_CORES 2
+/* The 64-bit key of the plan's block-size histogram: per block product the multiply-adds of its
+ * block pairs binned by (log2 m, log2 n, log2 K), and whether it has a product chain. */
+int32_t tt_plan_histogram(const tt_plan *plan, uint64_t *key);
+/* Time every form that applies to the plan on these operands (arguments as tt_plan_execute; two
+ * untimed and five timed executions of each on `stream`, synchronously), cache the fastest under
+ * the plan's histogram for this dtype and precision, and return it (*forms) with its median time in
+ * milliseconds (*ms).  Not capturable: a setup step, like the first execution of a plan. */
+int32_t tt_autotune(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                    const void *const *prepared, void *output, void *workspace, void *stream, int32_t *forms, float *ms);
+/* The forms cached for a histogram key, dtype and precision: *found 0 when there are none. */
+int32_t tt_autotune_lookup(uint64_t key, int32_t dtype, int32_t precision, int32_t *forms, int32_t *found);
+/* Cache forms for a key (a saved tuning table restored), or forget every cached choice. */
+int32_t tt_autotune_store(uint64_t key, int32_t dtype, int32_t precision, int32_t forms);
+int32_t tt_autotune_clear(void);
+
 /* Run operand `operand`'s preparation only, writing its prepared arena (for float64 also the
  * slices of it that split-precision products read).  The arena stays valid while the operand's
  * arena is unchanged; a changed operand needs a new preparation. */

@@ -66,6 +66,11 @@ _declare('tt_svd_workspace', i32, P(i64), P(i64), P(i64))
 _declare('tt_lanczos_scratch', i64, i32, i32, P(i64))
 _declare('tt_lanczos', vp, i32, i32, P(vp), P(vp), i32, vp, i32, f64, vp, vp, vp, P(f64), P(i32), vp)
 _declare('tt_lanczos_async', vp, i32, i32, P(vp), P(vp), i32, vp, i32, f64, vp, vp, vp, P(f64), P(i32), vp)
+_declare('tt_plan_histogram', vp, P(ctypes.c_uint64))
+_declare('tt_autotune', vp, i32, i32, P(vp), P(vp), vp, vp, vp, P(i32), P(ctypes.c_float))
+_declare('tt_autotune_lookup', ctypes.c_uint64, i32, i32, P(i32), P(i32))
+_declare('tt_autotune_store', ctypes.c_uint64, i32, i32, i32)
+_declare('tt_autotune_clear')
 _declare('tt_svd_blocks', i32, i64, vp, vp, vp, vp, vp, vp, vp, vp)
 _declare('tt_svd_keep', i32, vp, vp, vp, vp, vp, vp, vp, vp)
 
@@ -98,4 +103,5 @@ EXPORTED = ['tt_last_error', 'tt_version', 'tt_category', 'tt_outcomes', 'tt_dua
             'tt_R_symbol', 'tt_leg', 'tt_leg_blocks', 'tt_reachable_charges', 'tt_fusion_trees', 'tt_space',
             'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_conj', 'tt_plan_contract', 'tt_plan_einsum',
             'tt_plan_info', 'tt_plan_describe', 'tt_plan_cache_clear', 'tt_plan_gather', 'tt_plan_prepared_size', 'tt_plan_execute', 'tt_plan_execute_timed', 'tt_plan_prepare', 'tt_step_plan', 'tt_chain', 'tt_svd_workspace', 'tt_lanczos_scratch', 'tt_lanczos', 'tt_svd_blocks', 'tt_svd_keep',
-            'tt_dots', 'tt_dots_noalloc', 'tt_plan_execute_batch', 'tt_lanczos_async']
+            'tt_dots', 'tt_dots_noalloc', 'tt_plan_execute_batch', 'tt_lanczos_async', 'tt_plan_histogram', 'tt_autotune',
+            'tt_autotune_lookup', 'tt_autotune_store', 'tt_autotune_clear']

@@ -605,6 +605,59 @@ extern "C"
     return TT_OK;
   }
 
+  int32_t tt_plan_histogram(const tt_plan *plan, uint64_t *key)
+  {
+    if (!plan || !key) return fail(TT_EINVAL, "no plan");
+    *key = plan->program->tune_key;
+    return TT_OK;
+  }
+
+  int32_t tt_autotune(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
+                      const void *const *prepared, void *output, void *workspace, void *stream, int32_t *forms, float *ms)
+  {
+    if (!plan || !forms || !ms) return fail(TT_EINVAL, "no plan");
+    if (dtype != TT_DTYPE_FLOAT64 && dtype != TT_DTYPE_COMPLEX128) return fail(TT_EINVAL, "unknown dtype");
+    if (precision < TT_PRECISION_PER_BLOCK || precision > 8)
+      return fail(TT_EINVAL, "precision is 0 (FP64), 1..8 slices, or -1 (per-block FP64)");
+    if (precision > 0 && dtype != TT_DTYPE_FLOAT64)
+      return fail(TT_EINVAL, "split precision is implemented for float64 arenas");
+    const ttg::Program &p = *plan->program;
+    if (cudaError_t e = plan->tables->ensure(p); e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    ttg::ExecArgs args;
+    args.complex = dtype == TT_DTYPE_COMPLEX128;
+    args.precision = precision;
+    args.inputs = inputs;
+    args.prepared = prepared;
+    args.output = output;
+    args.workspace = workspace;
+    args.stream = static_cast<cudaStream_t>(stream);
+    const cudaError_t e = ttg::autotune(p, *plan->tables, args, forms, ms);
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+
+  int32_t tt_autotune_lookup(uint64_t key, int32_t dtype, int32_t precision, int32_t *forms, int32_t *found)
+  {
+    if (!forms || !found) return fail(TT_EINVAL, "no output");
+    const int32_t f = ttg::tuned_forms(key, dtype == TT_DTYPE_COMPLEX128, precision);
+    *found = f >= 0 ? 1 : 0;
+    *forms = f >= 0 ? f : 0;
+    return TT_OK;
+  }
+
+  int32_t tt_autotune_store(uint64_t key, int32_t dtype, int32_t precision, int32_t forms)
+  {
+    if (forms < 0 || forms > (TT_FORM_SEPARATE | TT_FORM_NO_TENSOR_CORES)) return fail(TT_EINVAL, "unknown forms");
+    ttg::store_forms(key, dtype == TT_DTYPE_COMPLEX128, precision, forms);
+    return TT_OK;
+  }
+
+  int32_t tt_autotune_clear(void)
+  {
+    ttg::clear_forms();
+    return TT_OK;
+  }
+
   int32_t tt_plan_prepare(const tt_plan *plan, int32_t dtype, int32_t operand, const void *input, void *prepared,
                           void *workspace, void *stream)
   {

@@ -127,7 +127,23 @@ namespace ttg
     bool *chain_ran = nullptr;             // when set: whether the product chain ran as one launch
                                            // (its events are those of the chain's first op)
     bool phases_only = false;              // run only the prepare phases that have to run
+    int32_t forms = -1;                    // kForm* bits; -1: the autotuner's choice for the plan's
+                                           // histogram (autotune.cpp), 0 when it has none
   };
+
+  // The forms a plan's products can run in (autotune.cpp).
+  constexpr int32_t kFormSeparate = 1;       // a product chain as separate launches
+  constexpr int32_t kFormNoTensorCores = 2;  // split products of large blocks on mma.sync, not tcgen05
+  // The cached forms for a key, or -1.
+  int32_t tuned_forms(uint64_t key, bool complex, int32_t precision);
+  void store_forms(uint64_t key, bool complex, int32_t precision, int32_t forms);
+  void clear_forms();
+  // The forms worth timing for a plan, the plain one first.
+  std::vector<int32_t> candidate_forms(const Program &p, bool complex, int32_t precision);
+  // Times every candidate form on `base`'s operands (two untimed and five timed executions each, on
+  // base.stream, waited for), keeps the fastest in the cache under the plan's key, and returns it
+  // with its median time.
+  cudaError_t autotune(const Program &p, DeviceTables &t, const ExecArgs &base, int32_t *best, float *best_ms);
 
   cudaError_t execute(const Program &p, DeviceTables &t, const ExecArgs &args);
   // Where every buffer of the program lives for these arguments (inputs, output, prepared arenas,
@@ -143,7 +159,8 @@ namespace ttg
   // place after the program's chain move instead (C then being the move's destination).
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, int *tickets,
-                                const void *const *prepared, cudaStream_t stream, const int32_t *relabel = nullptr);
+                                const void *const *prepared, cudaStream_t stream, const int32_t *relabel = nullptr,
+                                bool tensor_cores = true);
   // The device table of the program's chain move (chain.cu): per entry of the first product's
   // result its place after the move, or -1; built on first use, null when the move does not write
   // every entry the second product reads.

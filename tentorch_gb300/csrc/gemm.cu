@@ -1141,7 +1141,7 @@ namespace ttg
 
   cudaError_t launch_gemm_split(const Program &p, const Op &op, DeviceTables &t, size_t op_index, const double *A,
                                 const double *B, double *C, int32_t slices, void *scratch, int *ticket_region,
-                                const void *const *prepared, cudaStream_t stream, const int32_t *relabel)
+                                const void *const *prepared, cudaStream_t stream, const int32_t *relabel, bool tensor_cores)
   {
     cudaError_t e = ensure_split(p, op, t, op_index);
     if (e != cudaSuccess) return e;
@@ -1192,7 +1192,7 @@ namespace ttg
       const char *v = std::getenv("TENTORCH_GB300_TCGEN05");
       return !(v && v[0] == '0');
     }();
-    if (tc_enabled && !relabel && split_tc_suits(p, op, slices))
+    if (tc_enabled && tensor_cores && !relabel && split_tc_suits(p, op, slices))
       return launch_split_tc(p, op, t, op_index, slices, sa, sb, exps_a, exps_b, sched.slice_a, sched.slice_b, sched.pairs,
                              C, ticket_region + kTicketInts - 1, stream);
     const auto *blocks = reinterpret_cast<const DevBlock *>(t.blocks);

@@ -96,6 +96,8 @@ namespace ttg
   // The partial tiles (32 x 32 doubles each) the one launch of a program's product chain may hold
   // (chain.cu; 0 without a chain).
   int64_t chain_partial_slots(const Program &p);
+  // The key of a plan's block-size histogram (autotune.cpp).
+  uint64_t tune_key(const Program &p);
 
   // Scratch doubles a program's GEMM ops need at most (FP64 partials, or slices + exponents +
   // partials for split precision), laid out per op from offset 0.

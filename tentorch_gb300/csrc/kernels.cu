@@ -311,6 +311,10 @@ namespace ttg
       if (args.phases_only && op.phase < 0) return false;
       return !(op.phase >= 0 && args.prepared && args.prepared[op.phase]);
     };
+    // the forms the caller asked for, else those the autotuner chose for this histogram
+    int32_t forms = args.forms;
+    if (forms < 0) forms = std::max(tuned_forms(p.tune_key, args.complex, args.precision), 0);
+    const bool tensor_cores = (forms & kFormNoTensorCores) == 0;
     const auto run_op = [&](size_t i) -> cudaError_t
     {
       const Op &op = p.ops[i];
@@ -388,7 +392,7 @@ namespace ttg
         else if (args.precision > 0 && !args.complex)
           e = launch_gemm_split(p, op, t, i, reinterpret_cast<const double *>(src), reinterpret_cast<const double *>(src2),
                                 reinterpret_cast<double *>(dst), args.precision, scratch, tickets, args.prepared,
-                                args.stream);
+                                args.stream, nullptr, tensor_cores);
         else
           e = launch_gemm_f64(p, t, i, src, src2, dst, args.complex, scratch, tickets, args.stream);
         break;
@@ -406,8 +410,8 @@ namespace ttg
       const char *v = std::getenv("TENTORCH_GB300_CHAIN");
       return !(v && v[0] == '0');
     }();
-    const bool chain = chain_enabled && p.chain_first >= 0 && args.only_phase < 0 && !args.phases_only && !args.complex &&
-                       args.precision >= 0;
+    const bool chain = chain_enabled && (forms & kFormSeparate) == 0 && p.chain_first >= 0 && args.only_phase < 0 &&
+                       !args.phases_only && !args.complex && args.precision >= 0;
     std::vector<char> done(p.ops.size(), 0);
     if (args.chain_ran) *args.chain_ran = false;
     for (size_t i = 0; i < p.ops.size(); ++i)

@@ -846,6 +846,7 @@ namespace ttg
       p.scratch_offset = p.workspace;
       detect_chain(p);
       p.workspace += plan_gemms(p);
+      p.tune_key = tune_key(p);
       validate(p);
     }
 

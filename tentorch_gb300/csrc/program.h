@@ -140,6 +140,7 @@ namespace ttg
     // the move and the second product belong to prepare phases.
     int32_t chain_first = -1, chain_move = -1, chain_second = -1;
     int64_t chain_slots = 0;  // partial tiles the chain's one launch may hold (its scratch is sized for them)
+    uint64_t tune_key = 0;    // its block-size histogram's key (autotune.cpp)
     // per operand: the buffer holding its prepared value (the input itself when no op prepares it)
     std::vector<int32_t> prepared;
     // descriptor tables

@@ -368,6 +368,57 @@ def einsum_batch(spec: str, operand_lists, outcharge = None) -> list:
     return outs
 
 
+# the forms a plan's block products run in (tt_autotune): bits of the integer autotune returns
+FORM_SEPARATE = 1          # a product chain (the two-site matvec) as separate launches
+FORM_NO_TENSOR_CORES = 2   # split products of large blocks on mma.sync instead of tcgen05
+
+
+def histogram_key(plan: Plan) -> int:
+    '''The 64-bit key of a plan's block-size histogram (the autotuner's cache key).'''
+    key = ctypes.c_uint64()
+    check(lib.tt_plan_histogram(plan.handle, ctypes.byref(key)))
+    return key.value
+
+
+def autotune(spec: str, *operands: Tensor, outcharge = None) -> tuple:
+    '''Time every form the einsum's block products can run in on these operands, in the current
+    precision, and cache the fastest under the plan's block-size histogram: every later execution
+    of a plan with the same histogram (any operands of these shapes, or of others that bin alike)
+    runs it.  Returns (forms, milliseconds).  Synchronous; call it outside CUDA graph captures.'''
+    _check_device(operands)
+    plan = plan_of(spec, *operands, outcharge = outcharge)
+    data0 = operands[0]._data
+    device = data0.device
+    stream = torch.cuda.current_stream(device).cuda_stream
+    ws = _workspace(plan, device, data0.dtype, stream)
+    prepared = [_prepared_arena(plan, i, t, ws, stream, force = True) for i, t in enumerate(operands)]
+    out = torch.empty(plan.out_space.size, dtype = data0.dtype, device = device)
+    forms, ms = i32(), ctypes.c_float()
+    check(lib.tt_autotune(plan.handle, _DTYPE[data0.dtype], _precision, pointers(t._data.data_ptr() for t in operands),
+                          pointers((p.data_ptr() if p is not None else None) for p in prepared), out.data_ptr(),
+                          ws.data_ptr() if ws is not None else None, stream, ctypes.byref(forms), ctypes.byref(ms)))
+    return forms.value, ms.value
+
+
+def tuned_forms(plan: Plan, dtype = torch.float64, precision: Optional[int] = None) -> Optional[int]:
+    '''The forms cached for the plan's histogram (tt_autotune_lookup), or None.'''
+    forms, found = i32(), i32()
+    check(lib.tt_autotune_lookup(histogram_key(plan), _DTYPE[dtype], _precision if precision is None else precision,
+                                 ctypes.byref(forms), ctypes.byref(found)))
+    return forms.value if found.value else None
+
+
+def store_forms(plan: Plan, forms: int, dtype = torch.float64, precision: Optional[int] = None) -> None:
+    '''Cache forms for the plan's histogram by hand (tt_autotune_store): a saved tuning restored.'''
+    check(lib.tt_autotune_store(histogram_key(plan), _DTYPE[dtype], _precision if precision is None else precision,
+                                int(forms)))
+
+
+def clear_tuning() -> None:
+    '''Forget every cached form choice (tt_autotune_clear).'''
+    check(lib.tt_autotune_clear())
+
+
 def plan_of(spec: str, *tensors: Tensor, outcharge = None) -> Plan:
     '''The compiled plan an einsum of these operands runs (for timing and the roofline).'''
     has = outcharge is not None

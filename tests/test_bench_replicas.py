@@ -39,7 +39,8 @@ def _rank(rank, world, port, results):
 
 def test_two_replicas_report_the_slowest_rank_and_the_whole_job():
     world = 2
-    with mp.Manager() as manager:
+    # the manager process started with spawn, like the ranks (no fork of a threaded process)
+    with mp.get_context('spawn').Manager() as manager:
         results = manager.dict()
         mp.spawn(_rank, args = (world, _free_port(), results), nprocs = world, join = True)
         for rank in range(world):

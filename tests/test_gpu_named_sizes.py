@@ -125,3 +125,22 @@ def test_batched_windows_run_as_one_launch():
         assert la.last_batch_launches == len(windows)
         for got, want in zip(outs, wants):
             assert max_relative(got, want) < split_bound(6)
+
+
+def test_tensor_core_form_is_an_autotuned_choice(su2_case):
+    '''At the benchmark size the split products can run on tcgen05 or on mma.sync: the autotuner
+    times both (tt_autotune) and caches the faster under the plan's histogram; either form meets
+    the oracle within the six-slice bound.'''
+    from tentorch_gb300 import linalg as la
+    a, b, want = su2_case
+    pa, pb = to_product(a, tg.su2), to_product(b, tg.su2)
+    la.clear_tuning()
+    with tg.precision(6):
+        plan = la.plan_of(SPEC, pa, pb)
+        chosen, ms = la.autotune(SPEC, pa, pb)
+        assert chosen in (0, la.FORM_NO_TENSOR_CORES) and ms > 0
+        assert la.tuned_forms(plan) == chosen
+        for forms in (0, la.FORM_NO_TENSOR_CORES):
+            la.store_forms(plan, forms)
+            assert max_relative(tg.einsum(SPEC, pa, pb), want) < split_bound(6)
+    la.clear_tuning()
