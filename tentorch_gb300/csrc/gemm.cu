@@ -703,6 +703,8 @@ namespace ttg
     // the power of two 2^e that bounds the line, then each entry as the integer round(x 2^(56-e))
     // cut into `slices` balanced 7-bit digits (|q_1| <= 128, |q_t| <= 64 after it), exact in bf16,
     // written to a row padded with zeros to a multiple of 32.  Loads are issued eight at a time.
+    constexpr int kLineHeld = 16;  // entries a lane holds of a line sliced in one pass (lines <= 512)
+
     __global__ void split_lines_kernel(const double *__restrict__ a, const double *__restrict__ b,
                                        uint16_t *__restrict__ slices_a, uint16_t *__restrict__ slices_b,
                                        int16_t *__restrict__ exps_a, int16_t *__restrict__ exps_b, int64_t stride_a,
@@ -721,6 +723,52 @@ namespace ttg
         uint16_t *dst = (left ? slices_a : slices_b) + line.dst;
         int16_t *exps = left ? exps_a : exps_b;
         const int64_t stride = left ? stride_a : stride_b;
+        const auto cut = [&](int i, long long r)
+        {
+          for (int t = 0; t < slices_n; ++t)
+          {
+            const int shift = 49 - 7 * t;  // digit t weighs 2^(49 - 7t) of the 2^56 scale
+            long long q;
+            if (shift > 0)
+            {
+              q = (r + (1ll << (shift - 1))) >> shift;  // nearest integer, halves up
+              r -= q << shift;
+            }
+            else
+              q = r;
+            // |q| <= 128: exact in bf16, converted through int32 and fp32
+            dst[t * stride + i] = __bfloat16_as_ushort(__float2bfloat16_rn(__int2float_rn(static_cast<int>(q))));
+          }
+        };
+        if (line.padded <= 32 * kLineHeld)
+        {
+          // the whole line in registers, all its loads in flight at once: one round trip to memory
+          // for the maximum and the digits together
+          double v[kLineHeld];
+          unsigned long long big = 0;
+#pragma unroll
+          for (int u = 0; u < kLineHeld; ++u)
+          {
+            const int i = u * 32 + lane;
+            v[u] = i < line.len ? src[static_cast<int64_t>(i) * line.src_stride] : 0.0;
+            const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(v[u])) & 0x7fffffffffffffffull;
+            big = bits > big ? bits : big;
+          }
+          for (int off = 16; off > 0; off >>= 1)
+          {
+            const unsigned long long o = __shfl_xor_sync(0xffffffffu, big, off);
+            big = o > big ? o : big;
+          }
+          const int e = frexp_exponent(big);
+          if (lane == 0) exps[line.exp] = static_cast<int16_t>(e);
+#pragma unroll
+          for (int u = 0; u < kLineHeld; ++u)
+          {
+            const int i = u * 32 + lane;
+            if (i < line.padded) cut(i, i < line.len ? scaled_integer(v[u], 56 - e) : 0ll);
+          }
+          continue;
+        }
         // the largest |entry| by its bits (positive doubles order as integers), then its frexp
         // exponent e: every |entry| < 2^e
         unsigned long long big = 0;
@@ -758,22 +806,7 @@ namespace ttg
           for (int u = 0; u < 4; ++u)
           {
             const int i = i0 + u * 32 + lane;
-            if (i >= line.padded) continue;
-            long long r = x[u];
-            for (int t = 0; t < slices_n; ++t)
-            {
-              const int shift = 49 - 7 * t;  // digit t weighs 2^(49 - 7t) of the 2^56 scale
-              long long q;
-              if (shift > 0)
-              {
-                q = (r + (1ll << (shift - 1))) >> shift;  // nearest integer, halves up
-                r -= q << shift;
-              }
-              else
-                q = r;
-              // |q| <= 128: exact in bf16, converted through int32 and fp32
-              dst[t * stride + i] = __bfloat16_as_ushort(__float2bfloat16_rn(__int2float_rn(static_cast<int>(q))));
-            }
+            if (i < line.padded) cut(i, x[u]);
           }
         }
       }
