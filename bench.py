@@ -14,7 +14,11 @@ inputs.  The DMRG section times one sweep of the L = 64, chi = 256, n_iter = 10 
 each form from one FP64 state, with the energy differences.  Prints ONE JSON line (rank 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision P] [--impl reference]
-                    [--dmrg-length L] [--workload matvec|svd]
+                    [--dmrg-length L] [--chi X] [--workload matvec|svd|recoupling|windows|dmrg]
+
+Other workloads print a line of their own: recoupling (the SU(2) and Fibonacci recoupling einsums
+at their named sizes), windows (64 batched windows of drawn bonds), svd (the split of a two-site
+tensor), dmrg (the DMRG sweeps of every form at --dmrg-length sites and bond --chi).
 
 --impl reference times the reference's CPU path for the same workload on the host cores: the
 oracle port of tentorch's einsum (oracle/engine.py), a bounded sample of matvecs.  With N > 1 (one
@@ -57,7 +61,7 @@ def parse():
     p.add_argument('--dmrg-iter', type = int, default = 10, help = 'Lanczos steps per window in the DMRG timing')
     p.add_argument('--dmrg-warm', type = int, default = 4,
                    help = 'FP64 sweeps before the timed sweeps (four bring every bond of the L = 64 chain to chi = 256)')
-    p.add_argument('--workload', default = 'matvec', choices = ['matvec', 'svd', 'recoupling', 'windows'],
+    p.add_argument('--workload', default = 'matvec', choices = ['matvec', 'svd', 'recoupling', 'windows', 'dmrg'],
                    help = 'matvec: the headline line; svd: the truncating split of a two-site tensor; recoupling: '
                           'the SU(2) / Fibonacci einsum; windows: 64 batched matvecs in a CUDA graph')
     return p.parse_args()
@@ -280,14 +284,15 @@ def launches_of(kind, precision):
     return 1 if kind in (1, 2, 4, 6, 7) else 0
 
 
-def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
+def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms = None):
     """The two-site DMRG of the U(1) Heisenberg chain (tentorch/algorithms/dmrg.py) timed per sweep
     in three forms from one FP64 state: `warm` FP64 sweeps grow the bond to chi, then each form
     runs one sweep from a copy of that state, with the plan caches cleared first so that every
     form compiles its plans inside its sweep, and then the next sweep of its run with the plans
     kept (`s_per_sweep_continued`: the steady state of a long run, where the shapes recur).  Forms: split (grouped kernels, the Lanczos matvec in
-    split precision), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one cuBLAS
-    call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
+    split precision), bf16x3_fp64_ritz (three slices, the window's energy the FP64 Rayleigh
+    quotient of the Ritz vector), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one
+    cuBLAS call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
     around the sweep, the device synchronised on both sides.  (Every block product of the sweep in
     split precision, environments included, is the driver's `all_products` option; at this bond it
     is slower than the matvec alone in split precision and, at 6 slices, outside the 1e-10 bar.)"""
@@ -308,12 +313,15 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
     warm_s = time.perf_counter() - start
     snapshot = ([t.clone() for t in driver.state.tensors], driver.state.center)
     out = {}
-    forms = (('fp64_grouped', 0, 'gesvd'), ('split', precision, 'gesvd'), ('fp64_per_block', PER_BLOCK, 'gesvd'),
-             ('fp64_per_block_default_svd', PER_BLOCK, None))
-    for name, form, svd_driver in forms:
+    if forms is None:
+        forms = (('fp64_grouped', 0, 'gesvd', False), ('split', precision, 'gesvd', False),
+                 ('bf16x3_fp64_ritz', 3, 'gesvd', True), ('fp64_per_block', PER_BLOCK, 'gesvd', False),
+                 ('fp64_per_block_default_svd', PER_BLOCK, None, False))
+    for name, form, svd_driver, refine in forms:
         driver.state.tensors = [t.clone() for t in snapshot[0]]
         driver.state.center = snapshot[1]
         driver.precision = form
+        driver.refine_energy = refine
         la.PER_BLOCK_SVD_DRIVER = svd_driver
         tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
         clear_plans()
@@ -328,7 +336,8 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
         check = driver.energy().real
         out[name] = {'s_per_sweep': elapsed, 'energy': energy, 'energy_fp64_check': check,
                      'discarded': lost, 'matvecs': driver.matvecs - mv0, 'max_bond': max(driver.state.bond_dims),
-                     'svd': 'engine Jacobi (batched)' if form != PER_BLOCK else f'torch.linalg.svd per block, driver {svd_driver}'}
+                     'svd': 'engine Jacobi (batched)' if form != PER_BLOCK else f'torch.linalg.svd per block, driver {svd_driver}',
+                     'refined_energy': refine}
         if golden is not None:
             out[name]['delta_e_vs_reference'] = abs(energy - golden[warm])
         if svd_driver is None:
@@ -352,6 +361,7 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
             out[name]['continued_delta_e_vs_reference'] = abs(energy2 - golden[warm + 1])
         la.PER_BLOCK_SVD_DRIVER = 'gesvd'
         tg.set_precision(0)
+    driver.refine_energy = False
     tg.set_precision(0)
     clear_plans()
     ref = out['fp64_grouped']['energy']
@@ -363,12 +373,15 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm):
             'reference_energy': golden[warm] if golden is not None else None,
             'reference': 'the reference run in float64 from the same seed (tests/golden/dmrg_chi256.json), sweep '
                          f'{warm + 1} and the next',
-            'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
-            'speedup_split_vs_per_block_default_svd': out['fp64_per_block_default_svd']['s_per_sweep'] /
-                                                      out['split']['s_per_sweep'],
+            **({'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
+                'speedup_split_vs_per_block_default_svd': out['fp64_per_block_default_svd']['s_per_sweep'] /
+                                                          out['split']['s_per_sweep'],
+                'speedup_split_vs_per_block_continued': out['fp64_per_block']['s_per_sweep_continued'] /
+                                                        out['split']['s_per_sweep_continued'],
+                'speedup_bf16x3_fp64_ritz_vs_per_block': out['fp64_per_block']['s_per_sweep'] /
+                                                         out['bf16x3_fp64_ritz']['s_per_sweep']}
+               if 'fp64_per_block' in out else {}),
             'speedup_split_vs_fp64_grouped': out['fp64_grouped']['s_per_sweep'] / out['split']['s_per_sweep'],
-            'speedup_split_vs_per_block_continued': out['fp64_per_block']['s_per_sweep_continued'] /
-                                                    out['split']['s_per_sweep_continued'],
             'start': f'{warm} FP64 sweeps from the seeded random MPS (N(0,1) float64 blocks in key order, seed {SEED})'}
 
 
@@ -761,14 +774,28 @@ def run_windows(args):
             torch.cuda.synchronize(device)
             batch_ms = 1e3 * (time.perf_counter() - start) / steps
             batch_launches = tg.linalg.last_batch_launches
+            # the one call captured in a CUDA graph (config 4 as named: one persistent launch in a
+            # captured graph; the graph reads every operand from its buffer, so the environments'
+            # phases run in every replay)
+            batch_graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(batch_graph):
+                batched_images = tg.linalg.einsum_batch(MATVEC, windows)
+            batch_graph.replay()
+            torch.cuda.synchronize(device)
+            start = time.perf_counter()
+            for _ in range(steps):
+                batch_graph.replay()
+            torch.cuda.synchronize(device)
+            batch_graph_ms = 1e3 * (time.perf_counter() - start) / steps
             worst = 0.0
             images = batched()
             for i in checked:
                 scale = max(float(np.abs(b).max()) for b in wanted[i].values())
-                for got in (tg.einsum(MATVEC, *windows[i]), images[i]):
+                for got in (tg.einsum(MATVEC, *windows[i]), images[i], batched_images[i]):
                     worst = max(worst, max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in wanted[i].items()) / scale)
         out[name] = {'eager_ms_per_step': eager_ms, 'four_streams_ms_per_step': streams_ms, 'graph_ms_per_step': graph_ms,
                      'one_call_ms_per_step': batch_ms, 'one_call_launches': batch_launches,
+                     'one_call_graph_ms_per_step': batch_graph_ms,
                      'matvecs_per_s_graph': len(windows) / (graph_ms / 1e3),
                      'matvecs_per_s_one_call': len(windows) / (batch_ms / 1e3),
                      'gflops_graph': flops / (graph_ms / 1e3) / 1e9,
@@ -776,8 +803,30 @@ def run_windows(args):
     print(json.dumps(out), flush = True)
 
 
+def run_dmrg(args):
+    """Config 5's other sizes: the U(1) Heisenberg DMRG at `--dmrg-length` sites and bond `--chi`
+    (n_iter `--dmrg-iter`), `--dmrg-warm` FP64 sweeps from the seeded MPS, then each form's sweeps
+    from that state (dmrg_sweeps; the per-block form only up to bond 512).  Every form's energy is
+    reported against the grouped FP64 run from the same state.  Prints one line of its own."""
+    import torch
+    import tentorch_gb300 as tg
+    from tentorch_gb300.linalg import PER_BLOCK
+    device = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(device)
+    forms = [('fp64_grouped', 0, 'gesvd', False), ('split', args.precision, 'gesvd', False),
+             ('bf16x3_fp64_ritz', 3, 'gesvd', True)]
+    if args.chi <= 512:
+        forms.append(('fp64_per_block', PER_BLOCK, 'gesvd', False))
+    result = dmrg_sweeps(tg, torch, device, args.precision, args.dmrg_length, args.chi, args.dmrg_iter,
+                         args.dmrg_warm, forms = tuple(forms))
+    print(json.dumps({'workload': 'dmrg_u1_heisenberg', **result}), flush = True)
+
+
 def main():
     args = parse()
+    if args.workload == 'dmrg':
+        run_dmrg(args)
+        return
     if args.workload == 'svd':
         run_splittings(args)
         return

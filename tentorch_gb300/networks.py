@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from tentorch_gb300.lanczos import lanczos, lanczos_einsum
-from tentorch_gb300.linalg import contract, einsum, inner, precision, qr, rq, svd
+from tentorch_gb300.linalg import contract, einsum, inner, inner_device, precision, qr, rq, svd
 from tentorch_gb300.symmetry import (AbelianGroup, FusionCategory, FusionTree, Leg, NoSymmetry, fusion_trees,
                                      reachable_charges, u1)
 from tentorch_gb300.tensor import BlockKey, Tensor, block_keys, domain_legs
@@ -313,17 +313,21 @@ class DMRG:
     (see `MPS.random`).  `precision` chooses the block products of the Lanczos matvec (0: FP64;
     k: k bf16 slices, see `tentorch_gb300.precision`); with `all_products` also those of the
     environments, head and tail and the two-site contraction.  The SVDs, the Lanczos vector algebra
-    and the tridiagonal eigensolve stay FP64 either way.'''
+    and the tridiagonal eigensolve stay FP64 either way.  With `refine_energy` a window's energy is
+    the FP64 Rayleigh quotient <v|H v> / <v|v> of the Ritz vector v the split-precision Lanczos found
+    (one FP64 matvec per window): its error is second order in the vector's, so a coarse split
+    (three slices, ~2^-21 per matvec) still reports energies near FP64.'''
 
     def __init__(self, model: Model, max_bond_dim: int = 50, svd_tol: float = 1e-14, n_iter: int = 5, seed: int = 0,
                  dtype = None, device = None, generator: Optional[torch.Generator] = None, precision: int = 0,
-                 all_products: bool = False) -> None:
+                 all_products: bool = False, refine_energy: bool = False) -> None:
         self.model = model
         self.max_bond_dim = max_bond_dim
         self.svd_tol = svd_tol
         self.n_iter = n_iter
         self.precision = precision
         self.all_products = all_products
+        self.refine_energy = refine_energy
         self.operator = heisenberg(model.cat, model.length, model.coupling, dtype = dtype, device = device)
         physical = model.physical if model.physical is not None else self.operator.physical
         self.state = MPS.random(model.cat, physical, model.length, model.sector, seed = seed, dtype = dtype,
@@ -382,6 +386,12 @@ class DMRG:
             energy, vector = lanczos_einsum('EPaqj,JRSFb,AQsb->EPrf', [head, tail, two], 2, two, self.n_iter,
                                             wait = False)
         self.matvecs += self.n_iter
+        if self.refine_energy and self.precision != 0:
+            # the Ritz vector's Rayleigh quotient in FP64, on the device
+            with precision(0):
+                image = einsum('EPaqj,JRSFb,AQsb->EPrf', head, tail, vector)
+            energy = (inner_device(vector, image) / inner_device(vector, vector)).real
+            self.matvecs += 1
         factor = 2 if direction == 'right' else 1
         left, values, right = svd(vector, self.max_bond_dim, self.svd_tol, factor)
         self.state.tensors[at], self.state.tensors[at + 1] = left, right.place([0, 1])
