@@ -370,6 +370,7 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
         out[name]['delta_e_vs_own_fp64_check'] = abs(out[name]['energy'] - out[name]['energy_fp64_check'])
     return {'length': length, 'chi': chi, 'n_iter': n_iter, 'warm_fp64_sweeps': warm, 'warm_s': warm_s,
             'forms': out,
+            'svd_per_block_redos': la.svd_fallbacks,
             'reference_energy': golden[warm] if golden is not None else None,
             'reference': 'the reference run in float64 from the same seed (tests/golden/dmrg_chi256.json), sweep '
                          f'{warm + 1} and the next',

@@ -480,6 +480,21 @@ def is_close(first: Tensor, second: Tensor, rtol: float = 1e-10, atol: float = 1
 PER_BLOCK_SVD_DRIVER: Optional[str] = 'gesvd'
 
 
+# splits whose Jacobi SVD left a block unsettled and were redone per block with cuSOLVER
+svd_fallbacks = 0
+
+
+def _factor_blocks_per_block(arranged: Tensor, present):
+    '''The thin SVD of each present block by at::linalg_svd, one block at a time (svd.cpp:57-62).'''
+    factors = []
+    driver = PER_BLOCK_SVD_DRIVER if arranged.device.type == 'cuda' else None
+    for i, key in present:
+        u, sv, vh = torch.linalg.svd(arranged._view(i), full_matrices = False, driver = driver)
+        factors.append([key, u, sv, vh, 0, 0])
+    host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
+    return factors, host, None
+
+
 def _factor_blocks(arranged: Tensor):
     """The thin SVD of every non-empty block.  float64 blocks on the GPU go through one launch of
     the engine's Jacobi SVD (tt_svd_blocks), complex blocks, blocks beyond its size and the
@@ -491,13 +506,7 @@ def _factor_blocks(arranged: Tensor):
     batched = (arranged.dtype == torch.float64 and arranged.device.type == 'cuda' and _precision != PER_BLOCK and
                all(min(space.shapes[i]) <= 1024 for i, _ in present))
     if not batched:
-        factors = []
-        driver = PER_BLOCK_SVD_DRIVER if arranged.device.type == 'cuda' else None
-        for i, key in present:
-            u, sv, vh = torch.linalg.svd(arranged._view(i), full_matrices = False, driver = driver)
-            factors.append([key, u, sv, vh, 0, 0])
-        host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
-        return factors, host, None
+        return _factor_blocks_per_block(arranged, present)
     dims, count = ints64(x for i, _ in present for x in space.shapes[i])
     places, total = (i64 * max(len(present), 1))(), i64()
     check(lib.tt_svd_workspace(len(present), dims, places, ctypes.byref(total)))
@@ -528,7 +537,11 @@ def _factor_blocks(arranged: Tensor):
     info_host = info[:max(len(present), 1)].to('cpu', non_blocking = True)
     host = sv[:s_at].cpu().tolist()
     if present and int(info_host.min()) < 0:
-        raise RuntimeError('the Jacobi SVD of a block did not converge')
+        # a block the Jacobi sweeps did not settle within their cap: this split's blocks go through
+        # cuSOLVER one by one instead (QR iteration, gesvd), as the per-block form runs them
+        global svd_fallbacks
+        svd_fallbacks += 1
+        return _factor_blocks_per_block(arranged, present)
     factors = [[key, (u_off, rows, k), (s_off, k), (vh_off, k, cols), 0, 0]
                for key, rows, cols, k, u_off, s_off, vh_off in shapes]
     return factors, host, (u, sv, vh)
