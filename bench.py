@@ -375,13 +375,14 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
             'reference': 'the reference run in float64 from the same seed (tests/golden/dmrg_chi256.json), sweep '
                          f'{warm + 1} and the next',
             **({'speedup_split_vs_per_block': out['fp64_per_block']['s_per_sweep'] / out['split']['s_per_sweep'],
-                'speedup_split_vs_per_block_default_svd': out['fp64_per_block_default_svd']['s_per_sweep'] /
-                                                          out['split']['s_per_sweep'],
                 'speedup_split_vs_per_block_continued': out['fp64_per_block']['s_per_sweep_continued'] /
                                                         out['split']['s_per_sweep_continued'],
                 'speedup_bf16x3_fp64_ritz_vs_per_block': out['fp64_per_block']['s_per_sweep'] /
                                                          out['bf16x3_fp64_ritz']['s_per_sweep']}
                if 'fp64_per_block' in out else {}),
+            **({'speedup_split_vs_per_block_default_svd': out['fp64_per_block_default_svd']['s_per_sweep'] /
+                                                          out['split']['s_per_sweep']}
+               if 'fp64_per_block_default_svd' in out else {}),
             'speedup_split_vs_fp64_grouped': out['fp64_grouped']['s_per_sweep'] / out['split']['s_per_sweep'],
             'start': f'{warm} FP64 sweeps from the seeded random MPS (N(0,1) float64 blocks in key order, seed {SEED})'}
 
