@@ -18,14 +18,17 @@ Recipe differences from the reference's ``tentorch/_ext/build.py:115-146``: ``-s
 force-included as a plain header instead of a precompiled one.  The reference tree is read only; all
 outputs go under ``oracle/_ref``.
 
-Usage: ``python oracle/build_ref.py`` (about two minutes on 8 cores).  It needs the reference
-checkout at ``REFERENCE`` (default ``/root/reference``), so it runs only where that exists.
+Usage: ``python oracle/build_ref.py --reference <checkout>`` or with ``TENTORCH_REFERENCE`` set
+(about two minutes on 8 cores).  It runs only where a reference checkout is named and present.
 '''
 import glob
 import os
 import sys
 
-REFERENCE = os.environ.get('TENTORCH_REFERENCE', '/root/reference')
+# the reference checkout: from --reference, or the TENTORCH_REFERENCE environment variable
+REFERENCE = os.environ.get('TENTORCH_REFERENCE', '')
+if '--reference' in sys.argv[:-1]:
+    REFERENCE = sys.argv[sys.argv.index('--reference') + 1]
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, '_ref')
 EXT_DIR = os.path.join(OUT, 'ext')
@@ -40,8 +43,8 @@ _UNITS = ('symmetry/cat/cat.cpp', 'symmetry/cat/group.cpp', 'symmetry/cat/abelia
 
 
 def available() -> bool:
-    '''Whether the reference sources are present on this machine.'''
-    return os.path.isdir(os.path.join(REFERENCE, 'tentorch', 'tensors'))
+    '''Whether a reference checkout is named and its sources are present.'''
+    return bool(REFERENCE) and os.path.isdir(os.path.join(REFERENCE, 'tentorch', 'tensors'))
 
 
 def built() -> bool:

@@ -4,7 +4,7 @@ from its own sources by `oracle/build_ref.py`, imported by `oracle/ref_import.py
 
 Run from the repository root, where the reference checkout exists:
 
-    TENTORCH_DEVICE=cpu python tests/golden/make_golden.py
+    TENTORCH_REFERENCE=<reference checkout> TENTORCH_DEVICE=cpu python tests/golden/make_golden.py
 
 Every fixture is produced by the reference's own code path, on the CPU, in float64 (and complex128
 for the Fibonacci category, whose R symbol is complex):
