@@ -211,9 +211,10 @@ namespace ttg
     s.lines_a = static_cast<int64_t>(s.lines.size());
     s.lines.insert(s.lines.end(), b_lines.begin(), b_lines.end());
     // items: one pair's K range each (a multiple of 32), about two per worker, never below a tile
-    // over 128 of K
+    // over 256 of K (one exact level chunk: smaller items cost more in folds and partial tiles than
+    // they gain in spread; at bond 512 the split matvec took 147 us with 128 and 123 us with 256)
     const double target =
-      std::max(op_work(p, op) / (p.ctas * kSplitWorkers * 2.0), static_cast<double>(kSplitTileM) * kSplitTileN * 128.0);
+      std::max(op_work(p, op) / (p.ctas * kSplitWorkers * 2.0), static_cast<double>(kSplitTileM) * kSplitTileN * kExactChunk);
     struct Sized
     {
       SplitItem item;
