@@ -662,8 +662,14 @@ def run_recoupling(args):
         if dtype == torch.float64:
             forms['split'] = args.precision
         results, images = {}, {}
+        tuned = {}
         for form_name, form in forms.items():
             with tg.precision(form):
+                if form >= 0:
+                    # the autotuner times the forms that apply (tcgen05 or mma.sync split products)
+                    # and the timed calls run its choice
+                    chosen, tune_ms = tg.linalg.autotune('ABcd,DCef->ABef', *tensors)
+                    tuned[form_name] = {'forms': chosen, 'ms': tune_ms}
                 for _ in range(max(1, args.warmup)):
                     images[form_name] = tg.einsum('ABcd,DCef->ABef', *tensors)
                 torch.cuda.synchronize(device)
@@ -684,7 +690,8 @@ def run_recoupling(args):
             worst = max(float(np.abs(got.block(*k).cpu().numpy() - b).max()) for k, b in want.items())
             results[form_name]['max_rel_err_vs_oracle'] = worst / scale
         out[name] = {'dtype': str(dtype).replace('torch.', ''), 'blocks': tensors[0].nblocks(),
-                     'entries_per_tensor': tensors[0].data.numel(), 'gemm_flop': plan.flops, 'forms': results}
+                     'entries_per_tensor': tensors[0].data.numel(), 'gemm_flop': plan.flops, 'forms': results,
+                     'autotune': tuned}
     print(json.dumps(out), flush = True)
 
 
