@@ -4,12 +4,17 @@
 // (tentorch/linalg/graded/einsum.cpp:351-376 folds it as two contractions with a recoupling between
 // them, tentorch/linalg/graded/contract.cpp:148-163 one product per block pair).
 //
-// The persistent FP64 kernel runs the work items of both products from one list per SM:
+// The persistent FP64 kernel runs the work items of both products from one list per SM (4 workers
+// of 128 threads claiming from it, FP64 FMA lanes, see the kernel):
 //   - a first-product tile writes its entries straight to their places after the move (a table of
 //     one int32 per entry of X, built on the device once per plan from the move's tile
-//     descriptors, replaces the move's own pass), then counts itself done;
-//   - a second-product item waits until every first-product tile is done, then runs like any other
-//     tile.
+//     descriptors, replaces the move's own pass), then counts itself done (per worker, published
+//     once before the worker's first wait);
+//   - a second-product item waits until every first-product tile of its program is done, then runs
+//     like any other tile;
+//   - a tile cut along K adds its chunks into a per-tile accumulator with FP64 atomics; the
+//     accumulators, in the workspace's scratch, are zeroed by all CTAs at the start of the launch,
+//     and no chunk adds before every CTA has zeroed its share.
 // Each SM's list holds its first-product items before its second-product items and every SM runs
 // its own list, so every wait ends once the first-product items of the running SMs are done; a wait
 // still gives up after two seconds and raises an error flag (no hang on a fault elsewhere).  The
