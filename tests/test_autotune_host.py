@@ -51,3 +51,21 @@ def test_unknown_forms_are_refused():
     plan = _matvec_plan(32)
     with pytest.raises(ValueError):
         la.store_forms(plan, 7, precision = 0)
+
+
+def test_the_matvec_plan_is_a_product_chain_and_a_plain_contraction_is_not():
+    '''The compiler finds the two-site matvec's chain (a product, the leg move of its result, the
+    product that reads the moved result: one FP64 launch on the GPU), and a single contraction has
+    none; the histogram key records the difference.'''
+    plan = _matvec_plan(64)
+    text = plan.describe()
+    assert text.splitlines()[0].startswith('chain ops ')
+    ops = [int(x) for x in text.splitlines()[0].split()[2:]]
+    kinds = {int(line.split()[1]): line.split()[2] for line in text.splitlines() if line.startswith('op ')}
+    assert [kinds[o] for o in ops] == ['gemm', 'tiles', 'gemm']
+    cat = tg.u1
+    leg = tg.Leg(cat, [(q,) for q in (-1, 0, 1)], [2, 3, 2])
+    a = tg.Tensor(cat, [leg], [leg], (0,), dtype = torch.float64, device = 'cpu')
+    single = la.plan_of('ab,bc->ac', a, a)
+    assert not single.describe().startswith('chain ops')
+    assert la.histogram_key(single) != la.histogram_key(plan)
