@@ -545,11 +545,39 @@ def run_gpu(args, rank, world):
         out = tg.einsum(MATVEC, head, tail, staging)
         host_out.copy_(out.data, non_blocking = True)
 
+    def e2e_link_step(i):
+        # the same transfers by kernels over the CPU-GPU link (tt_link_copy), no copy-engine call
+        tg.linalg.link_copy(staging.data, host_in[i % 4])
+        out = tg.einsum(MATVEC, head, tail, staging)
+        tg.linalg.link_copy(host_out, out.data)
+
     tg.set_precision(args.precision)
     for i in range(3):
         e2e_step(i)
     e2e_times = timed_loop(args.steps, args.precision, e2e_step)
-    e2e_ms = sum(e2e_times) / args.steps
+    copy_engine_ms = sum(e2e_times) / args.steps
+    e2e_path = 'pinned host theta -> H2D (copy engine) -> tentorch_gb300.einsum (C ABI) -> D2H (copy engine) of the image'
+    e2e_ms = copy_engine_ms
+    link_ms = None
+    try:
+        for i in range(3):
+            e2e_link_step(i)
+        torch.cuda.synchronize(device)
+        # the link path checked once against the copy-engine path on the same vector
+        e2e_step(0)
+        torch.cuda.synchronize(device)
+        engine_image = host_out.clone()
+        e2e_link_step(0)
+        torch.cuda.synchronize(device)
+        if not torch.equal(engine_image, host_out):
+            raise RuntimeError('the link transfer gave another image')
+        link_times = timed_loop(args.steps, args.precision, e2e_link_step)
+        link_ms = sum(link_times) / args.steps
+        e2e_ms = link_ms
+        e2e_path = ('pinned host theta -> kernel read over NVLink-C2C (tt_link_copy) -> tentorch_gb300.einsum (C ABI) '
+                    '-> kernel write of the image to pinned host memory (tt_link_copy)')
+    except (ValueError, RuntimeError) as error:
+        print(f'link transfers unavailable: {error}', file = sys.stderr)
     h2d = host_in[0].numel() * 8
     d2h = host_out.numel() * 8
 
@@ -585,8 +613,9 @@ def run_gpu(args, rank, world):
                 'e2e_vs_cpu': 'the e2e rate against cpu_baseline compares with the numpy port of the reference '
                               "(oracle/engine.py), not with the reference's compiled engine",
                 'e2e': {'value': world * 1e3 / e2e_ms, 'unit': 'matvecs/s', 'h2d_bytes_per_step': h2d,
-                        'd2h_bytes_per_step': d2h,
-                        'path': 'pinned host theta -> H2D -> tentorch_gb300.einsum (C ABI) -> D2H of the image'},
+                        'd2h_bytes_per_step': d2h, 'path': e2e_path,
+                        'copy_engine_value': world * 1e3 / copy_engine_ms,
+                        'link_value': world * 1e3 / link_ms if link_ms else None},
                 'clocks': clock_record,
                 'gpu_launches': launches_per_step * args.steps}
         print(json.dumps(line), flush = True)

@@ -272,6 +272,13 @@ int32_t tt_dots(int32_t dtype, int32_t count, const void *const *as, const void 
  * work overlaps on the GPU share the array and race.  Otherwise the same contract as tt_dots. */
 int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *out,
                         void *stream);
+/* Copy `bytes` between page-locked host memory and device memory with a kernel that reads or
+ * writes the host end directly over the coherent CPU-GPU link (GB300's NVLink-C2C), on `stream`:
+ * direction 0 host -> device (src host, dst device), 1 device -> host.  The host end must be
+ * mapped page-locked memory (cudaHostAlloc; TT_EINVAL otherwise, nothing copied).  The transfer a
+ * step of the end-to-end matvec makes (its vector in, its image out) without a copy-engine call.
+ * No counterpart in the reference (its tensors live on one device). */
+int32_t tt_link_copy(void *dst, const void *src, int64_t bytes, int32_t direction, void *stream);
 
 #ifdef __cplusplus
 }

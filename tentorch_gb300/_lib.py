@@ -71,6 +71,7 @@ _declare('tt_autotune', vp, i32, i32, P(vp), P(vp), vp, vp, vp, P(i32), P(ctypes
 _declare('tt_autotune_lookup', ctypes.c_uint64, i32, i32, P(i32), P(i32))
 _declare('tt_autotune_store', ctypes.c_uint64, i32, i32, i32)
 _declare('tt_autotune_clear')
+_declare('tt_link_copy', vp, vp, i64, i32, vp)
 _declare('tt_svd_blocks', i32, i64, vp, vp, vp, vp, vp, vp, vp, vp)
 _declare('tt_svd_keep', i32, vp, vp, vp, vp, vp, vp, vp, vp)
 
@@ -104,4 +105,4 @@ EXPORTED = ['tt_last_error', 'tt_version', 'tt_category', 'tt_outcomes', 'tt_dua
             'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_conj', 'tt_plan_contract', 'tt_plan_einsum',
             'tt_plan_info', 'tt_plan_describe', 'tt_plan_cache_clear', 'tt_plan_gather', 'tt_plan_prepared_size', 'tt_plan_execute', 'tt_plan_execute_timed', 'tt_plan_prepare', 'tt_step_plan', 'tt_chain', 'tt_svd_workspace', 'tt_lanczos_scratch', 'tt_lanczos', 'tt_svd_blocks', 'tt_svd_keep',
             'tt_dots', 'tt_dots_noalloc', 'tt_plan_execute_batch', 'tt_lanczos_async', 'tt_plan_histogram', 'tt_autotune',
-            'tt_autotune_lookup', 'tt_autotune_store', 'tt_autotune_clear']
+            'tt_autotune_lookup', 'tt_autotune_store', 'tt_autotune_clear', 'tt_link_copy']

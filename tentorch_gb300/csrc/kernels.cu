@@ -635,3 +635,55 @@ extern "C" int32_t tt_dots_noalloc(int32_t dtype, int32_t count, const void *con
   return TT_OK;
 }
 
+
+// ------------------------------------------------------------------------------------------
+// host <-> device transfers by a kernel over the coherent host link
+// ------------------------------------------------------------------------------------------
+
+namespace
+{
+  // 16-byte words while both ends are 16-byte aligned, then the rest one byte at a time.
+  __global__ void link_copy_kernel(unsigned char *__restrict__ dst, const unsigned char *__restrict__ src, int64_t bytes)
+  {
+    const int64_t thread = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t threads = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const bool aligned = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0;
+    const int64_t words = aligned ? bytes / 16 : 0;
+    for (int64_t i = thread; i < words; i += threads)
+      reinterpret_cast<uint4 *>(dst)[i] = reinterpret_cast<const uint4 *>(src)[i];
+    for (int64_t i = words * 16 + thread; i < bytes; i += threads) dst[i] = src[i];
+  }
+
+  // The device address of page-locked host memory allocated mapped (cudaHostAlloc; every
+  // allocation is mapped where the device has unified addressing), or an error when it is not.
+  cudaError_t mapped(const void *host, void **device)
+  {
+    cudaPointerAttributes attributes{};
+    cudaError_t e = cudaPointerGetAttributes(&attributes, host);
+    if (e != cudaSuccess) return e;
+    if (attributes.type != cudaMemoryTypeHost || attributes.devicePointer == nullptr) return cudaErrorInvalidValue;
+    return cudaHostGetDevicePointer(device, const_cast<void *>(host), 0);
+  }
+}
+
+extern "C" int32_t tt_link_copy(void *dst, const void *src, int64_t bytes, int32_t direction, void *stream)
+{
+  if (bytes < 0 || (bytes > 0 && (!dst || !src))) return ttg::report(TT_EINVAL, "tt_link_copy needs both ends");
+  if (direction != 0 && direction != 1) return ttg::report(TT_EINVAL, "direction is 0 (host to device) or 1 (device to host)");
+  if (bytes == 0) return TT_OK;
+  void *host = direction == 0 ? const_cast<void *>(src) : dst, *through = nullptr;
+  cudaError_t e = mapped(host, &through);
+  if (e != cudaSuccess)
+  {
+    cudaGetLastError();
+    return ttg::report(TT_EINVAL, "the host end of tt_link_copy is not mapped page-locked memory (cudaHostAlloc)");
+  }
+  unsigned char *d = static_cast<unsigned char *>(direction == 0 ? dst : through);
+  const unsigned char *s = static_cast<const unsigned char *>(direction == 0 ? through : src);
+  const int64_t words = (bytes + 15) / 16;
+  const unsigned grid = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((words + 255) / 256, ttg::device_sms() * 4)));
+  link_copy_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(d, s, bytes);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return ttg::report(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  return TT_OK;
+}

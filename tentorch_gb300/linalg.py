@@ -419,6 +419,28 @@ def clear_tuning() -> None:
     check(lib.tt_autotune_clear())
 
 
+def link_copy(dst: torch.Tensor, src: torch.Tensor) -> torch.Tensor:
+    '''dst.copy_(src) between a page-locked host tensor and a CUDA tensor (either way round) by a
+    kernel that reads or writes the host end over the coherent CPU-GPU link (tt_link_copy), on the
+    current stream, without a copy-engine call.  Both contiguous, of one dtype and size; the host
+    tensor pinned (`pin_memory=True`), else ValueError.'''
+    if dst.dtype != src.dtype or dst.numel() != src.numel() or not dst.is_contiguous() or not src.is_contiguous():
+        raise ValueError('link_copy needs two contiguous tensors of one dtype and size')
+    if dst.device.type == 'cuda' and src.device.type == 'cpu':
+        direction, device = 0, dst.device
+    elif dst.device.type == 'cpu' and src.device.type == 'cuda':
+        direction, device = 1, src.device
+    else:
+        raise ValueError('link_copy copies between a host tensor and a CUDA tensor')
+    stream = torch.cuda.current_stream(device).cuda_stream
+    check(lib.tt_link_copy(dst.data_ptr(), src.data_ptr(), dst.numel() * dst.element_size(), direction, stream))
+    # the kernel wrote dst behind torch's back: mark it written, so that no prepared copy of its
+    # old contents is reused
+    from torch.autograd.graph import increment_version
+    increment_version(dst)
+    return dst
+
+
 def plan_of(spec: str, *tensors: Tensor, outcharge = None) -> Plan:
     '''The compiled plan an einsum of these operands runs (for timing and the roofline).'''
     has = outcharge is not None
