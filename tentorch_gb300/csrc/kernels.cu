@@ -484,6 +484,7 @@ namespace ttg
     __global__ void dot_partial_kernel(const double *const *__restrict__ as, const double *__restrict__ b, int64_t n,
                                        double *__restrict__ partial)
     {
+      dependent_entry();
       const double *a = as[blockIdx.y];
       double re = 0.0, im = 0.0;
       if constexpr (Complex)
@@ -535,6 +536,7 @@ namespace ttg
 
     __global__ void dot_final_kernel(const double *__restrict__ partial, int parts, double *__restrict__ out)
     {
+      dependent_entry();
       // one warp per result, fixed summation order
       const int j = blockIdx.x;
       double re = 0.0, im = 0.0;
@@ -561,12 +563,11 @@ namespace ttg
   {
     const int parts = kDotParts;
     dim3 grid(parts, static_cast<unsigned>(count));
-    if (complex)
-      dot_partial_kernel<true><<<grid, 256, 0, stream>>>(dev_as, b, n_doubles, partial);
-    else
-      dot_partial_kernel<false><<<grid, 256, 0, stream>>>(dev_as, b, n_doubles, partial);
-    dot_final_kernel<<<static_cast<unsigned>(count), 32, 0, stream>>>(partial, parts, out);
-    return cudaGetLastError();
+    cudaError_t e = complex ? launch_dependent(dot_partial_kernel<true>, grid, 256, 0, stream, dev_as, b, n_doubles, partial)
+                            : launch_dependent(dot_partial_kernel<false>, grid, 256, 0, stream, dev_as, b, n_doubles, partial);
+    if (e != cudaSuccess) return e;
+    return launch_dependent(dot_final_kernel, static_cast<unsigned>(count), 32, 0, stream, static_cast<const double *>(partial),
+                            parts, out);
   }
 
 } // namespace ttg

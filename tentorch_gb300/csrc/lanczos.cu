@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "executor.h"
+#include "launch.h"
 
 namespace ttg
 {
@@ -26,6 +27,7 @@ namespace ttg
     __global__ void rows_kernel(const double **table, const double *basis, int64_t n_doubles, int32_t count,
                                 const double *image, const double *start, const double *result)
     {
+      dependent_entry();
       const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
       if (j < count) table[j] = basis + j * n_doubles;
       if (j == count) table[j] = image;
@@ -36,6 +38,7 @@ namespace ttg
     // dst = src / sqrt(norm2[0]) (norm2 the real part of <src, src>); beta_out (optional) = sqrt
     __global__ void scale_kernel(double *dst, const double *src, int64_t n_doubles, const double *norm2, double *beta_out)
     {
+      dependent_entry();
       const double norm = sqrt(fmax(norm2[0], 0.0));
       const double inv = 1.0 / fmax(norm, 1e-300);
       if (beta_out && blockIdx.x == 0 && threadIdx.x == 0) *beta_out = norm;
@@ -49,6 +52,7 @@ namespace ttg
     __global__ void project_kernel(double *y, const double *basis, int64_t n_doubles, int32_t count,
                                    const double *coeffs)
     {
+      dependent_entry();
       const int64_t step = static_cast<int64_t>(gridDim.x) * blockDim.x * (Complex ? 2 : 1);
       for (int64_t i = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) * (Complex ? 2 : 1); i < n_doubles;
            i += step)
@@ -75,11 +79,16 @@ namespace ttg
       }
     }
 
-    __global__ void save_kernel(double *dst, const double *src) { *dst = *src; }
+    __global__ void save_kernel(double *dst, const double *src)
+    {
+      dependent_entry();
+      *dst = *src;
+    }
 
     // out = sum_j c_j basis_j with real c_j, j < *count
     __global__ void combine_kernel(double *out, const double *basis, int64_t n_doubles, const int32_t *count, const double *c)
     {
+      dependent_entry();
       const int32_t used = *count;
       for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n_doubles;
            i += static_cast<int64_t>(gridDim.x) * blockDim.x)
@@ -118,6 +127,7 @@ namespace ttg
     __global__ void ritz_kernel(const double *tri, int32_t n_iter, double tol, double *ritz, double *energy,
                                 int32_t *size_out)
     {
+      dependent_entry();
       extern __shared__ double work[];
       __shared__ double bracket[2];
       __shared__ int32_t shared_size;
@@ -283,10 +293,14 @@ namespace ttg
     cudaStream_t stream = base.stream;
     const int grid = grid_of(n_doubles);
     cudaError_t e;
-    rows_kernel<<<1, 128, 0, stream>>>(table, basis, n_doubles, static_cast<int32_t>(rows), image, start, result);
+    if ((e = launch_dependent(rows_kernel, 1, 128, 0, stream, table, basis, n_doubles, static_cast<int32_t>(rows), image, start,
+                              result)) != cudaSuccess)
+      return e;
     // basis[0] = start / |start|
     if ((e = arena_dots(start_slot, 1, start, n_doubles, complex, partial, coeffs, stream)) != cudaSuccess) return e;
-    scale_kernel<<<grid, 256, 0, stream>>>(basis, start, n_doubles, coeffs, nullptr);
+    if ((e = launch_dependent(scale_kernel, grid, 256, 0, stream, basis, start, n_doubles, static_cast<const double *>(coeffs),
+                              static_cast<double *>(nullptr))) != cudaSuccess)
+      return e;
     std::vector<const void *> inputs(base.inputs, base.inputs + p.n_inputs);
     for (int32_t k = 0; k < n_iter; ++k)
     {
@@ -299,14 +313,20 @@ namespace ttg
       for (int pass = 0; pass < 3; ++pass)
       {
         if ((e = arena_dots(table, k + 1, image, n_doubles, complex, partial, coeffs, stream)) != cudaSuccess) return e;
-        if (pass == 0) save_kernel<<<1, 1, 0, stream>>>(tri + k, coeffs + 2 * k);
+        if (pass == 0 && (e = launch_dependent(save_kernel, 1, 1, 0, stream, tri + k, static_cast<const double *>(coeffs + 2 * k))) != cudaSuccess)
+          return e;
         if (complex)
-          project_kernel<true><<<grid, 256, 0, stream>>>(image, basis, n_doubles, k + 1, coeffs);
+          e = launch_dependent(project_kernel<true>, grid, 256, 0, stream, image, static_cast<const double *>(basis), n_doubles, k + 1,
+                               static_cast<const double *>(coeffs));
         else
-          project_kernel<false><<<grid, 256, 0, stream>>>(image, basis, n_doubles, k + 1, coeffs);
+          e = launch_dependent(project_kernel<false>, grid, 256, 0, stream, image, static_cast<const double *>(basis), n_doubles, k + 1,
+                               static_cast<const double *>(coeffs));
+        if (e != cudaSuccess) return e;
       }
       if ((e = arena_dots(image_slot, 1, image, n_doubles, complex, partial, coeffs, stream)) != cudaSuccess) return e;
-      scale_kernel<<<grid, 256, 0, stream>>>(row + n_doubles, image, n_doubles, coeffs, tri + n_iter + k);
+      if ((e = launch_dependent(scale_kernel, grid, 256, 0, stream, row + n_doubles, static_cast<const double *>(image), n_doubles,
+                                static_cast<const double *>(coeffs), tri + n_iter + k)) != cudaSuccess)
+        return e;
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     // the lowest Ritz pair of the tridiagonal (the steps after the first beta below tol dropped, as
@@ -315,10 +335,16 @@ namespace ttg
     const int smem = static_cast<int>((7 * n_iter + 1) * sizeof(double));
     if (smem > 48 * 1024 && (e = cudaFuncSetAttribute(ritz_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) != cudaSuccess)
       return e;
-    ritz_kernel<<<1, 32, smem, stream>>>(tri, n_iter, tol, ritz, energy_dev, size_dev);
-    combine_kernel<<<grid, 256, 0, stream>>>(result, basis, n_doubles, size_dev, ritz);
+    if ((e = launch_dependent(ritz_kernel, 1, 32, smem, stream, static_cast<const double *>(tri), n_iter, tol, ritz, energy_dev,
+                              size_dev)) != cudaSuccess)
+      return e;
+    if ((e = launch_dependent(combine_kernel, grid, 256, 0, stream, result, static_cast<const double *>(basis), n_doubles,
+                              static_cast<const int32_t *>(size_dev), static_cast<const double *>(ritz))) != cudaSuccess)
+      return e;
     if ((e = arena_dots(result_slot, 1, result, n_doubles, complex, partial, coeffs, stream)) != cudaSuccess) return e;
-    scale_kernel<<<grid, 256, 0, stream>>>(result, result, n_doubles, coeffs, nullptr);
+    if ((e = launch_dependent(scale_kernel, grid, 256, 0, stream, result, static_cast<const double *>(result), n_doubles,
+                              static_cast<const double *>(coeffs), static_cast<double *>(nullptr))) != cudaSuccess)
+      return e;
     return cudaGetLastError();
   }
 
