@@ -159,7 +159,7 @@ int32_t tt_plan_execute_batch(int32_t count, const tt_plan *const *plans, int32_
 int32_t tt_plan_execute_timed(const tt_plan *plan, int32_t dtype, int32_t precision, const void *const *inputs,
                               const void *const *prepared, void *output, void *workspace, void *stream, int32_t cap,
                               float *op_ms, int32_t *op_kind);
-/* ---- autotuning (replaces a fixed choice of kernel forms; SURVEY item "tt_autotune_lookup") --- */
+/* ---- autotuning: the forms of a plan's block products, chosen by timing, cached by histogram ---- */
 
 /* The forms a plan's block products run in, as bits: TT_FORM_SEPARATE runs a product chain (two
  * products with the leg move between them, the two-site matvec) as separate launches instead of
