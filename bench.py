@@ -294,7 +294,7 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
     quotient of the Ritz vector), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one
     cuBLAS call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
     around the sweep, the device synchronised on both sides.  (Every block product of the sweep in
-    split precision, environments included, is the driver's `all_products` option; at this bond it
+    split precision, environments included, is the DMRG object's `all_products` option; at this bond it
     is slower than the matvec alone in split precision and, at 6 slices, outside the 1e-10 bar.)"""
     from tentorch_gb300 import networks as nw
     from tentorch_gb300 import linalg as la
