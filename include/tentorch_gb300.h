@@ -244,6 +244,16 @@ int32_t tt_svd_blocks(int32_t count, int64_t largest, const int64_t *table, cons
  * offset in doubles of each block's working set in the workspace (-1 for an empty block) and the
  * doubles the workspace needs in all. */
 int32_t tt_svd_workspace(int32_t count, const int64_t *shapes, int64_t *offsets, int64_t *total);
+/* Rank a split's singular values on the device (tentorch/linalg/graded/svd.cpp:68-118): `values`
+ * (device, n_values) block after block, each block's `block_k[b]` values in descending order;
+ * block b's domain sector id `block_sector[b]` and each sector's dual `dual[s]` (ids below
+ * n_sectors; device int32 arrays).  The values above `tol` in descending order (ties by position),
+ * at most `max_bond` of them (-1: no cap), then the +-q pairing of the bond: kept[b] (device int32)
+ * receives how many leading values block b keeps.  One CTA; TT_EINVAL when the values do not fit
+ * its shared memory (about 16K values), nothing launched. */
+int32_t tt_svd_rank(const double *values, int32_t n_values, const int32_t *block_k, const int32_t *block_sector,
+                    int32_t n_blocks, const int32_t *dual, int32_t n_sectors, double tol, int64_t max_bond, int32_t *kept,
+                    void *stream);
 /* Write the kept part of the factors of tt_svd_blocks into the two tensors of a split, one CTA per
  * kept block.  `table` is a DEVICE array of 10 int64 per block: u_off, s_off, vh_off (packed
  * factors), first_off, second_off (the blocks of the two output arenas), values_off (the kept

@@ -72,6 +72,7 @@ _declare('tt_autotune_lookup', ctypes.c_uint64, i32, i32, P(i32), P(i32))
 _declare('tt_autotune_store', ctypes.c_uint64, i32, i32, i32)
 _declare('tt_autotune_clear')
 _declare('tt_link_copy', vp, vp, i64, i32, vp)
+_declare('tt_svd_rank', vp, i32, vp, vp, i32, vp, i32, f64, i64, vp, vp)
 _declare('tt_svd_blocks', i32, i64, vp, vp, vp, vp, vp, vp, vp, vp)
 _declare('tt_svd_keep', i32, vp, vp, vp, vp, vp, vp, vp, vp)
 
@@ -105,4 +106,4 @@ EXPORTED = ['tt_last_error', 'tt_version', 'tt_category', 'tt_outcomes', 'tt_dua
             'tt_space_size', 'tt_space_blocks', 'tt_space_legs', 'tt_plan_place', 'tt_plan_conj', 'tt_plan_contract', 'tt_plan_einsum',
             'tt_plan_info', 'tt_plan_describe', 'tt_plan_cache_clear', 'tt_plan_gather', 'tt_plan_prepared_size', 'tt_plan_execute', 'tt_plan_execute_timed', 'tt_plan_prepare', 'tt_step_plan', 'tt_chain', 'tt_svd_workspace', 'tt_lanczos_scratch', 'tt_lanczos', 'tt_svd_blocks', 'tt_svd_keep',
             'tt_dots', 'tt_dots_noalloc', 'tt_plan_execute_batch', 'tt_lanczos_async', 'tt_plan_histogram', 'tt_autotune',
-            'tt_autotune_lookup', 'tt_autotune_store', 'tt_autotune_clear', 'tt_link_copy']
+            'tt_autotune_lookup', 'tt_autotune_store', 'tt_autotune_clear', 'tt_link_copy', 'tt_svd_rank']

@@ -871,6 +871,20 @@ extern "C"
     return TT_OK;
   }
 
+  int32_t tt_svd_rank(const double *values, int32_t n_values, const int32_t *block_k, const int32_t *block_sector,
+                      int32_t n_blocks, const int32_t *dual, int32_t n_sectors, double tol, int64_t max_bond, int32_t *kept,
+                      void *stream)
+  {
+    if (n_values < 0 || n_blocks < 0 || n_sectors < 0) return fail(TT_EINVAL, "negative counts");
+    if (n_blocks == 0) return TT_OK;
+    if (ttg::rank_bytes(n_values, n_blocks, n_sectors) > ttg::kRankMaxBytes)
+      return fail(TT_EINVAL, "too many singular values to rank in one CTA's shared memory (" + std::to_string(n_values) + ")");
+    const cudaError_t e = ttg::svd_rank(values, n_values, block_k, block_sector, n_blocks, dual, n_sectors, tol, max_bond,
+                                        kept, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(TT_ECUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    return TT_OK;
+  }
+
   int32_t tt_dots(int32_t dtype, int32_t count, const void *const *as, const void *b, int64_t n, double *scratch,
                   double *out, void *stream)
   {

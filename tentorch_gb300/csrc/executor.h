@@ -211,6 +211,13 @@ namespace ttg
                          void *workspace, int32_t *info, cudaStream_t stream);
   // doubles of global workspace one block needs (0 when its working set fits in shared memory)
   int64_t svd_workspace_doubles(int64_t rows, int64_t cols);
+  // The ranking of a split's singular values (svd.cu rank_kernel): per block the values it keeps;
+  // shared memory rank_bytes(...) at most kRankMaxBytes.
+  constexpr int64_t kRankMaxBytes = 200 * 1024;
+  int64_t rank_bytes(int32_t n_values, int32_t n_blocks, int32_t n_sectors);
+  cudaError_t svd_rank(const double *values, int32_t n_values, const int32_t *block_k, const int32_t *block_sector,
+                       int32_t n_blocks, const int32_t *dual, int32_t n_sectors, double tol, int64_t max_bond, int32_t *kept,
+                       cudaStream_t stream);
   cudaError_t svd_keep(int32_t count, const void *table, const double *u, const double *s, const double *vh,
                        double *first, double *second, double *values, cudaStream_t stream);
 

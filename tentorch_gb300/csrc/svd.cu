@@ -1108,3 +1108,134 @@ namespace ttg
   }
 
 } // namespace ttg
+
+// ------------------------------------------------------------------------------------------
+// the ranking of a split's singular values on the device
+// ------------------------------------------------------------------------------------------
+
+namespace ttg
+{
+  namespace
+  {
+    // Every singular value of a split (block after block, each block's in descending order) sorted
+    // by (value descending, position ascending) — the order of the host's stable sort — by a bitonic
+    // sort in shared memory; then one thread walks the sorted values: the cut (values above `tol`,
+    // at most `max_bond`), the values each block keeps, and the +-q pairing of the bond (a domain
+    // sector keeps at most as many as its dual, the first ones in the sorted order; a sector whose
+    // dual keeps nothing drops out), as tentorch/linalg/graded/svd.cpp:68-118 ranks them on the host.
+    __global__ void rank_kernel(const double *__restrict__ values, int32_t n_values, const int32_t *__restrict__ block_k,
+                                const int32_t *__restrict__ block_sector, int32_t n_blocks, const int32_t *__restrict__ dual,
+                                int32_t n_sectors, double tol, int64_t max_bond, int32_t *__restrict__ kept_out)
+    {
+      extern __shared__ __align__(16) unsigned char smem_raw[];
+      int n = 1;
+      while (n < n_values) n <<= 1;
+      unsigned long long *key = reinterpret_cast<unsigned long long *>(smem_raw);  // [n]
+      int32_t *pos = reinterpret_cast<int32_t *>(key + n);                          // [n]
+      int32_t *block_of = pos + n;                                                  // [n_values]
+      int32_t *kept = block_of + n_values;                                          // [n_blocks]
+      int32_t *mult = kept + n_blocks;                                              // [n_sectors] x 3
+      int32_t *paired = mult + n_sectors, *used = paired + n_sectors;
+      // keys: the complement of |value|'s bits (ascending keys = descending values); padding last
+      for (int i = threadIdx.x; i < n; i += blockDim.x)
+      {
+        if (i < n_values)
+        {
+          key[i] = ~(static_cast<unsigned long long>(__double_as_longlong(values[i])) & 0x7fffffffffffffffull);
+          pos[i] = i;
+        }
+        else
+        {
+          key[i] = ~0ull;
+          pos[i] = 0x7fffffff;
+        }
+      }
+      if (threadIdx.x == 0)
+      {
+        int32_t at = 0;
+        for (int32_t b = 0; b < n_blocks; ++b)
+        {
+          for (int32_t j = 0; j < block_k[b]; ++j) block_of[at + j] = b;
+          at += block_k[b];
+        }
+      }
+      __syncthreads();
+      for (int size = 2; size <= n; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1)
+        {
+          for (int i = threadIdx.x; i < n; i += blockDim.x)
+          {
+            const int j = i ^ stride;
+            if (j > i)
+            {
+              const bool ascending = (i & size) == 0;
+              const bool greater = key[i] > key[j] || (key[i] == key[j] && pos[i] > pos[j]);
+              if (greater == ascending)
+              {
+                const unsigned long long tk = key[i];
+                key[i] = key[j];
+                key[j] = tk;
+                const int32_t tp = pos[i];
+                pos[i] = pos[j];
+                pos[j] = tp;
+              }
+            }
+          }
+          __syncthreads();
+        }
+      if (threadIdx.x != 0) return;
+      int32_t cut = 0;
+      while (cut < n_values && values[pos[cut]] > tol) ++cut;
+      if (max_bond >= 0 && cut > max_bond) cut = static_cast<int32_t>(max_bond);
+      for (int32_t b = 0; b < n_blocks; ++b) kept[b] = 0;
+      for (int32_t s = 0; s < n_sectors; ++s) mult[s] = used[s] = 0;
+      for (int32_t r = 0; r < cut; ++r) ++kept[block_of[pos[r]]];
+      for (int32_t b = 0; b < n_blocks; ++b) mult[block_sector[b]] += kept[b];
+      bool any = false, differs = false;
+      for (int32_t s = 0; s < n_sectors; ++s)
+      {
+        paired[s] = -1;
+        if (mult[s] == 0) continue;
+        if (mult[dual[s]] > 0)
+        {
+          paired[s] = min(mult[s], mult[dual[s]]);
+          any = true;
+          if (paired[s] != mult[s]) differs = true;
+        }
+        else
+          differs = true;
+      }
+      if (any && differs)
+      {
+        for (int32_t b = 0; b < n_blocks; ++b) kept[b] = 0;
+        for (int32_t r = 0; r < cut; ++r)
+        {
+          const int32_t b = block_of[pos[r]], s = block_sector[b];
+          if (paired[s] < 0 || used[s] >= paired[s]) continue;
+          ++used[s];
+          ++kept[b];
+        }
+      }
+      for (int32_t b = 0; b < n_blocks; ++b) kept_out[b] = kept[b];
+    }
+  } // namespace
+
+  int64_t rank_bytes(int32_t n_values, int32_t n_blocks, int32_t n_sectors)
+  {
+    int64_t n = 1;
+    while (n < n_values) n <<= 1;
+    return n * 12 + static_cast<int64_t>(n_values) * 4 + static_cast<int64_t>(n_blocks) * 4 + static_cast<int64_t>(n_sectors) * 12;
+  }
+
+  cudaError_t svd_rank(const double *values, int32_t n_values, const int32_t *block_k, const int32_t *block_sector,
+                       int32_t n_blocks, const int32_t *dual, int32_t n_sectors, double tol, int64_t max_bond, int32_t *kept,
+                       cudaStream_t stream)
+  {
+    const int64_t bytes = rank_bytes(n_values, n_blocks, n_sectors);
+    cudaError_t e = cudaFuncSetAttribute(rank_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+    if (e != cudaSuccess) return e;
+    rank_kernel<<<1, 1024, bytes, stream>>>(values, n_values, block_k, block_sector, n_blocks, dual, n_sectors, tol, max_bond,
+                                            kept);
+    return cudaGetLastError();
+  }
+} // namespace ttg

@@ -555,23 +555,17 @@ def _factor_blocks(arranged: Tensor):
     stream = torch.cuda.current_stream(device).cuda_stream
     check(lib.tt_svd_blocks(len(present), largest, dev_table.data_ptr(), arranged._data.data_ptr(), u.data_ptr(),
                             sv.data_ptr(), vh.data_ptr(), ws.data_ptr(), info.data_ptr(), stream))
-    # the sweep counts come back with the values: one wait for both
-    info_host = info[:max(len(present), 1)].to('cpu', non_blocking = True)
-    host = sv[:s_at].cpu().tolist()
-    if present and int(info_host.min()) < 0:
-        # a block the Jacobi sweeps did not settle within their cap: this split's blocks go through
-        # cuSOLVER one by one instead (QR iteration, gesvd), as the per-block form runs them
-        global svd_fallbacks
-        svd_fallbacks += 1
-        return _factor_blocks_per_block(arranged, present)
+    # the values stay on the device: the caller ranks them there and reads the sweep counts
+    # (info) with the per-block results in one wait
     factors = [[key, (u_off, rows, k), (s_off, k), (vh_off, k, cols), 0, 0]
                for key, rows, cols, k, u_off, s_off, vh_off in shapes]
-    return factors, host, (u, sv, vh)
+    return factors, None, (u, sv, vh, info[:max(len(present), 1)], s_at, present)
 
 
 def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
-    '''tentorch/linalg/graded/svd.cpp:41-177: the SVD of every block, one host read of all the
-    singular values, a global ranking, truncation, and the +-q pairing of the bond.'''
+    '''tentorch/linalg/graded/svd.cpp:41-177: the SVD of every block, the global ranking of the
+    singular values, truncation and the +-q pairing of the bond (on the device for the engine's
+    batched SVD: one read of each block's kept count), then the two factors.'''
     if absorb not in (0, 1, 2, 3):
         raise ValueError(f'absorb has to be 0, 1, 2 or 3, got {absorb}')
     if max_bond is not None and max_bond < 1:
@@ -579,12 +573,77 @@ def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
     arranged = tensor.place(left) if left is not None else tensor
     cat = arranged.cat
     factors, host, packed = _factor_blocks(arranged)
+    if packed is not None:
+        ranked = _rank_on_device(arranged, factors, packed, max_bond, tol)
+        if ranked is None:
+            # a block the Jacobi sweeps did not settle within their cap: this split's blocks go
+            # through cuSOLVER one by one instead (QR iteration, gesvd), as the per-block form runs them
+            global svd_fallbacks
+            svd_fallbacks += 1
+            factors, host, packed = _factor_blocks_per_block(arranged, packed[5])
+        else:
+            multiplicities = ranked
+            return _split_finish(arranged, factors, packed, multiplicities, absorb)
     candidates, at = [], 0
     for fi, f in enumerate(factors):
-        count = f[2][1] if packed is not None else f[2].numel()
-        for index in range(count):
+        for index in range(f[2].numel()):
             candidates.append((host[at], fi, index))
             at += 1
+    multiplicities = _rank_candidates(factors, candidates, max_bond, tol, cat)
+    return _split_finish(arranged, factors, packed, multiplicities, absorb)
+
+
+def _rank_on_device(arranged: Tensor, factors, packed, max_bond, tol):
+    '''The ranking of the split's singular values on the device (tt_svd_rank): per block the values
+    it keeps, read with the SVD's sweep counts in one wait.  Returns the bond's multiplets per
+    domain sector (the blocks' f[4] set), or None when a block's Jacobi sweeps did not settle.
+    Where the values do not fit the ranking kernel, they are read and ranked on the host.'''
+    u, sv, vh, info, s_at, present = packed
+    cat = arranged.cat
+    ids = {}
+    for f in factors:
+        for sector in (f[0].domain, cat.dual(f[0].domain)):
+            ids.setdefault(sector, len(ids))
+    sectors = sorted(ids, key = ids.get)
+    table = ([f[2][1] for f in factors] + [ids[f[0].domain] for f in factors] +
+             [ids[cat.dual(sector)] for sector in sectors])
+    device = arranged.device
+    dev = torch.tensor(table, dtype = torch.int32).to(device, non_blocking = True)
+    kept = torch.zeros(len(factors), dtype = torch.int32, device = device)
+    nb, ns = len(factors), len(sectors)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    try:
+        check(lib.tt_svd_rank(sv.data_ptr(), s_at, dev.data_ptr(), dev.data_ptr() + 4 * nb, nb, dev.data_ptr() + 8 * nb, ns,
+                              float(tol), -1 if max_bond is None else int(max_bond), kept.data_ptr(), stream))
+    except ValueError:
+        return _rank_on_host(factors, sv[:s_at].cpu().tolist(), info, max_bond, tol, cat)
+    both = torch.cat([info.to(torch.int32), kept]).cpu()
+    if present and int(both[:info.numel()].min()) < 0:
+        return None
+    multiplicities = {}
+    for f, k in zip(factors, both[info.numel():].tolist()):
+        f[4] = k
+        if k:
+            multiplicities[f[0].domain] = multiplicities.get(f[0].domain, 0) + k
+    return multiplicities
+
+
+def _rank_on_host(factors, host, info, max_bond, tol, cat):
+    '''The same ranking on the host, for splits too large for the ranking kernel.'''
+    if factors and int(info.min()) < 0:
+        return None
+    candidates, at = [], 0
+    for fi, f in enumerate(factors):
+        for index in range(f[2][1]):
+            candidates.append((host[at], fi, index))
+            at += 1
+    return _rank_candidates(factors, candidates, max_bond, tol, cat)
+
+
+def _rank_candidates(factors, candidates, max_bond, tol, cat):
+    '''tentorch/linalg/graded/svd.cpp:68-118: the global ranking, truncation and +-q pairing of the
+    bond over (value, block, index) candidates; sets each block's kept count f[4] and returns the
+    bond's multiplets per domain sector.'''
     candidates.sort(key = lambda c: -c[0])
     cut = next((i for i, c in enumerate(candidates) if c[0] <= tol), len(candidates))
     candidates = candidates[:cut]
@@ -613,6 +672,13 @@ def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
             used[f[0].domain] = used.get(f[0].domain, 0) + 1
             f[4] = max(f[4], index + 1)
         multiplicities = paired
+    return multiplicities
+
+
+def _split_finish(arranged: Tensor, factors, packed, multiplicities, absorb):
+    '''The bond of the split from its multiplets per domain sector, and the two factors and the
+    values written (one launch from the packed factors, else block by block).'''
+    cat = arranged.cat
     nxt = {}
     for f in factors:
         f[5] = nxt.get(f[0].domain, 0)
@@ -629,7 +695,7 @@ def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
     second = Tensor(cat, [bond], arranged.domain, cat.trivial(), arranged.dtype, arranged.device)
     if packed is not None:
         # one launch writes every kept block of both factors and the values
-        u, sv, vh = packed
+        u, sv, vh = packed[:3]
         table, count = [], 0
         for key, (u_off, rows, k), (s_off, _), (vh_off, _, cols), kept, offset in factors:
             if kept == 0:
