@@ -134,10 +134,9 @@ namespace ttg
   int64_t chain_partial_slots(const Program &p)
   {
     if (p.chain_first < 0) return 0;
-    ChainCut cut;
-    cut_product(p, p.ops[static_cast<size_t>(p.chain_first)], 0, cut);
-    cut_product(p, p.ops[static_cast<size_t>(p.chain_second)], 1, cut);
-    return cut.slots;
+    // the partial tiles do not depend on the deal: the schedule's sizing pass counts them
+    return schedule_gemm(p, p.ops[static_cast<size_t>(p.chain_first)], kChainTile, kChainTile, false).slots +
+           schedule_gemm(p, p.ops[static_cast<size_t>(p.chain_second)], kChainTile, kChainTile, false).slots;
   }
 
   namespace

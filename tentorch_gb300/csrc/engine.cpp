@@ -10,6 +10,7 @@
 #include <numeric>
 #include <set>
 #include <tuple>
+#include <unordered_map>
 
 namespace ttg
 {
@@ -426,8 +427,52 @@ namespace ttg
   }
 
   // tentorch/symmetry/tree/tree.cpp:375-398
+  namespace
+  {
+    // Hashes and key checks of the per-leg-list caches below, computed in place (no key is
+    // allocated for a lookup): the category, the legs by their interned numbers.
+    void mix(uint64_t &h, uint64_t v) { h ^= v + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2); }
+
+    uint64_t legs_hash(const Category &cat, const std::vector<Leg> &legs)
+    {
+      uint64_t h = 0x9e3779b97f4a7c15ull ^ static_cast<uint64_t>(reinterpret_cast<uintptr_t>(&cat));
+      for (const Leg &l : legs) mix(h, static_cast<uint64_t>(l->id));
+      mix(h, static_cast<uint64_t>(legs.size()));
+      return h;
+    }
+
+    bool same_legs(const std::vector<int32_t> &ids, const std::vector<Leg> &legs)
+    {
+      if (ids.size() != legs.size()) return false;
+      for (size_t i = 0; i < legs.size(); ++i)
+        if (ids[i] != legs[i]->id) return false;
+      return true;
+    }
+
+    std::vector<int32_t> ids_of(const std::vector<Leg> &legs)
+    {
+      std::vector<int32_t> ids;
+      ids.reserve(legs.size());
+      for (const Leg &l : legs) ids.push_back(l->id);
+      return ids;
+    }
+
+    struct ChargesEntry
+    {
+      const Category *cat;
+      std::vector<int32_t> ids;
+      std::vector<Sector> charges;
+    };
+  } // namespace
+
+  // The charges the legs fuse to, in the order a fusion from the first leg meets them; kept per
+  // list of legs (every space and every einsum's output check asks for them).
   std::vector<Sector> reachable_charges(const Category &cat, const std::vector<Leg> &legs)
   {
+    static std::unordered_map<uint64_t, std::vector<ChargesEntry>> cache;
+    std::vector<ChargesEntry> &bucket = cache[legs_hash(cat, legs)];
+    for (const ChargesEntry &e : bucket)
+      if (e.cat == &cat && same_legs(e.ids, legs)) return e.charges;
     std::vector<Sector> charges{cat.trivial()};
     for (Leg leg : legs)
     {
@@ -439,6 +484,7 @@ namespace ttg
             if (seen.insert(o.sector).second) next.push_back(o.sector);
       charges = std::move(next);
     }
+    bucket.push_back(ChargesEntry{&cat, ids_of(legs), charges});
     return charges;
   }
 
@@ -550,25 +596,54 @@ namespace ttg
     return it == position.end() ? -1 : it->second;
   }
 
-  // tentorch/tensors/layout.cpp:18-32, cached per (category, legs, root)
+  namespace
+  {
+    // A cached layout with the key it was built for: the category, the legs (interned, by number)
+    // and the root.
+    struct LayoutEntry
+    {
+      const Category *cat;
+      std::vector<int32_t> ids;
+      Sector root;
+      std::unique_ptr<Layout> layout;
+    };
+
+    uint64_t layout_hash(const Category &cat, const std::vector<Leg> &legs, const Sector &root)
+    {
+      uint64_t h = legs_hash(cat, legs);
+      mix(h, static_cast<uint64_t>(root.size));
+      for (int32_t i = 0; i < root.size; ++i) mix(h, static_cast<uint64_t>(root[i]));
+      return h;
+    }
+  } // namespace
+
+  // tentorch/tensors/layout.cpp:18-32, cached per (category, legs, root).  A lookup hashes the key
+  // in place and compares it against the entries of its hash, with no allocation: compiling a
+  // plan looks layouts up for every block it touches.
   const Layout &layout_of(const Category &cat, const std::vector<Leg> &legs, const Sector &root)
   {
-    static std::map<std::tuple<const Category *, std::vector<int32_t>, Sector>, std::unique_ptr<Layout>> cache;
-    std::vector<int32_t> ids;
-    for (Leg l : legs) ids.push_back(l->id);
-    auto key = std::make_tuple(&cat, std::move(ids), root);
-    auto found = cache.find(key);
-    if (found != cache.end()) return *found->second;
-    auto layout = std::make_unique<Layout>();
+    static std::unordered_map<uint64_t, std::vector<LayoutEntry>> cache;
+    std::vector<LayoutEntry> &bucket = cache[layout_hash(cat, legs, root)];
+    for (const LayoutEntry &e : bucket)
+      if (e.cat == &cat && e.root == root && same_legs(e.ids, legs)) return *e.layout;
+    LayoutEntry entry{&cat, ids_of(legs), root, std::make_unique<Layout>()};
+    Layout *layout = entry.layout.get();
     layout->trees = fusion_trees(cat, legs, root);
     layout->offsets.push_back(0);
+    layout->index.reserve(layout->trees.size() * legs.size());
     for (const Tree &t : layout->trees)
     {
       int64_t rows = 1;
-      for (size_t axis = 0; axis < legs.size(); ++axis) rows *= legs[axis]->multiplicity_of(t.sectors[axis]);
+      for (size_t axis = 0; axis < legs.size(); ++axis)
+      {
+        const int64_t at = legs[axis]->index_of(t.sectors[axis]);
+        layout->index.push_back(static_cast<int32_t>(at));
+        rows *= legs[axis]->mult[static_cast<size_t>(at)];
+      }
       layout->offsets.push_back(layout->offsets.back() + rows);
     }
-    return *cache.emplace(std::move(key), std::move(layout)).first->second;
+    bucket.push_back(std::move(entry));
+    return *layout;
   }
 
   // ------------------------------------------------------------------------------------------

@@ -193,6 +193,7 @@ namespace ttg
   {
     std::vector<Tree> trees;
     std::vector<int64_t> offsets;
+    std::vector<int32_t> index;  // per tree, the sector index of each leg on that leg (tree t at t * legs)
     int64_t rows() const { return offsets.back(); }
     // trees keyed for the lookups a bend makes, built on first use
     mutable std::map<Tree, int32_t> position;

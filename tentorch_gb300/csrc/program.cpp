@@ -349,16 +349,6 @@ namespace ttg
         std::map<std::vector<int32_t>, int32_t> wide_map_;
       };
 
-      // The sector index on `legs` of every leg of every tree of a layout (row t at t * legs).
-      static std::vector<int32_t> tree_indices(const Layout &lay, const std::vector<Leg> &legs)
-      {
-        std::vector<int32_t> out;
-        out.reserve(lay.trees.size() * legs.size());
-        for (const Tree &t : lay.trees)
-          for (size_t l = 0; l < legs.size(); ++l) out.push_back(static_cast<int32_t>(legs[l]->index_of(t.sectors[l])));
-        return out;
-      }
-
       template <typename Fn>
       int64_t walk_pieces(Space in, const std::vector<int32_t> &above, const std::vector<int32_t> &below, Space out,
                           Fn &&fn)
@@ -437,7 +427,7 @@ namespace ttg
                 std::make_tuple(&out_dom, ob.key.domain, cr, &cols_of, &col_at)})
           {
             const Layout &lay = layout_of(cat, *side, root);
-            const std::vector<int32_t> idx = tree_indices(lay, *side);
+            const std::vector<int32_t> &idx = lay.index;
             for (size_t t = 0; t < lay.trees.size(); ++t)
             {
               table->put_first(idx.data() + t * side->size(), static_cast<int32_t>(at->size()));
@@ -454,7 +444,7 @@ namespace ttg
         {
           const Layout &rl = layout_of(cat, in->codomain, blk.key.codomain);
           const Layout &cl = layout_of(cat, in->domain, blk.key.domain);
-          const std::vector<int32_t> r_idx = tree_indices(rl, in->codomain), c_idx = tree_indices(cl, in->domain);
+          const std::vector<int32_t> &r_idx = rl.index, &c_idx = cl.index;
           for (size_t rt = 0; rt < rl.trees.size(); ++rt)
             for (size_t ct = 0; ct < cl.trees.size(); ++ct)
             {
@@ -1277,9 +1267,20 @@ namespace ttg
           break;
         }
     bool closes = output.labels.empty();
-    for (const Sector &a : reachable_charges(cat, above_legs))
-      for (const Sector &c : reachable_charges(cat, below_legs))
-        if (cat.n_symbol(a, cat.dual(c), charge) > 0) closes = true;
+    if (!closes)
+    {
+      const std::vector<Sector> below_charges = reachable_charges(cat, below_legs);
+      for (const Sector &a : reachable_charges(cat, above_legs))
+      {
+        for (const Sector &c : below_charges)
+          if (cat.n_symbol(a, cat.dual(c), charge) > 0)
+          {
+            closes = true;
+            break;
+          }
+        if (closes) break;
+      }
+    }
     if (!closes) throw InvalidArgument("the output legs of '" + spec + "' cannot close to " + charge.str());
     size_t combinations = 1;
     for (const std::vector<Value> &alts : prepared)
