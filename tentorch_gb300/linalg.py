@@ -257,19 +257,29 @@ def place(tensor: Tensor, above, below = None) -> Tensor:
         named = set(a for a in above if 0 <= a < total)
         below = [leg for leg in range(total) if leg not in named]
     below = [int(b) for b in below]
-    a, na = ints32(above)
-    b, nb = ints32(below)
-    plan = _plan(('place', tensor._space.id, tuple(above), tuple(below)),
-                 lambda out: lib.tt_plan_place(tensor._space.id, na, a, nb, b, out), tensor.cat)
+    plan = place_plan(tensor._space, above, below)
     if plan.n_ops == 0:
         return tensor
     return run(plan, [tensor], reuse_prepared = False)
 
 
+def place_plan(space: Space, above, below) -> Plan:
+    '''The compiled plan of `place` on a tensor of this space (legs already resolved).'''
+    above, below = [int(x) for x in above], [int(x) for x in below]
+    a, na = ints32(above)
+    b, nb = ints32(below)
+    return _plan(('place', space.id, tuple(above), tuple(below)),
+                 lambda out: lib.tt_plan_place(space.id, na, a, nb, b, out), space.cat)
+
+
 def conj(tensor: Tensor) -> Tensor:
     '''tentorch/tensors/tensor.cpp:99-107: the bra of a tensor, one compiled pass.'''
-    plan = _plan(('conj', tensor._space.id), lambda out: lib.tt_plan_conj(tensor._space.id, out), tensor.cat)
-    return run(plan, [tensor], reuse_prepared = False)
+    return run(conj_plan(tensor._space), [tensor], reuse_prepared = False)
+
+
+def conj_plan(space: Space) -> Plan:
+    '''The compiled plan of `conj` on a tensor of this space.'''
+    return _plan(('conj', space.id), lambda out: lib.tt_plan_conj(space.id, out), space.cat)
 
 
 def contract(left: Tensor, right: Tensor, left_legs, right_legs, charge = None) -> Tensor:
@@ -278,6 +288,11 @@ def contract(left: Tensor, right: Tensor, left_legs, right_legs, charge = None) 
         raise ValueError('a contraction needs both tensors over one category')
     if left.dtype != right.dtype:
         raise ValueError('a contraction needs both tensors of one scalar type')
+    return run(contract_plan(left._space, right._space, left_legs, right_legs, charge), [left, right])
+
+
+def contract_plan(left: Space, right: Space, left_legs, right_legs, charge = None) -> Plan:
+    '''The compiled plan of `contract` on tensors of these spaces.'''
     left_legs, right_legs = [int(x) for x in left_legs], [int(x) for x in right_legs]
     has = charge is not None
     q = _label(charge) if has else 0
@@ -285,10 +300,8 @@ def contract(left: Tensor, right: Tensor, left_legs, right_legs, charge = None) 
     ra, m = ints32(right_legs)
     if n != m:
         raise ValueError(f'the two legs of a contraction must be given in pairs, got {n} and {m}')
-    plan = _plan(('contract', left._space.id, right._space.id, tuple(left_legs), tuple(right_legs), has, q),
-                 lambda out: lib.tt_plan_contract(left._space.id, right._space.id, n, la, ra, int(has), q, out),
-                 left.cat)
-    return run(plan, [left, right])
+    return _plan(('contract', left.id, right.id, tuple(left_legs), tuple(right_legs), has, q),
+                 lambda out: lib.tt_plan_contract(left.id, right.id, n, la, ra, int(has), q, out), left.cat)
 
 
 def einsum(spec: str, *tensors: Tensor, **options) -> Tensor:
@@ -304,12 +317,7 @@ def einsum(spec: str, *tensors: Tensor, **options) -> Tensor:
     for t in tensors:
         if t.cat is not cat:
             raise ValueError('an einsum needs every operand over one category')
-    has = outcharge is not None
-    q = _label(outcharge) if has else 0
-    ids, n = ints32(t._space.id for t in tensors)
-    plan = _plan(('einsum', spec, tuple(t._space.id for t in tensors), has, q),
-                 lambda out: lib.tt_plan_einsum(spec.encode(), n, ids, int(has), q, out), cat)
-    return run(plan, list(tensors))
+    return run(einsum_plan(spec, [t._space for t in tensors], outcharge), list(tensors))
 
 
 # per (device, stream, dtype, window): the workspace of one window of a batch (a batch's windows run
@@ -443,11 +451,17 @@ def link_copy(dst: torch.Tensor, src: torch.Tensor) -> torch.Tensor:
 
 def plan_of(spec: str, *tensors: Tensor, outcharge = None) -> Plan:
     '''The compiled plan an einsum of these operands runs (for timing and the roofline).'''
+    return einsum_plan(spec, [t._space for t in tensors], outcharge)
+
+
+def einsum_plan(spec: str, spaces, outcharge = None) -> Plan:
+    '''The compiled plan of an einsum over operands of these spaces: compiling ahead of the call
+    (from spaces a caller expects) fills the cache the call reads.'''
     has = outcharge is not None
     q = _label(outcharge) if has else 0
-    ids, n = ints32(t._space.id for t in tensors)
-    return _plan(('einsum', spec, tuple(t._space.id for t in tensors), has, q),
-                 lambda out: lib.tt_plan_einsum(spec.encode(), n, ids, int(has), q, out), tensors[0].cat)
+    ids, n = ints32(s.id for s in spaces)
+    return _plan(('einsum', spec, tuple(s.id for s in spaces), has, q),
+                 lambda out: lib.tt_plan_einsum(spec.encode(), n, ids, int(has), q, out), spaces[0].cat)
 
 
 # ---------------------------------------------------------------------------------------------
@@ -506,18 +520,20 @@ PER_BLOCK_SVD_DRIVER: Optional[str] = 'gesvd'
 svd_fallbacks = 0
 
 
-def _factor_blocks_per_block(arranged: Tensor, present):
+def _factor_blocks_per_block(arranged: Tensor, present, while_waiting = None):
     '''The thin SVD of each present block by at::linalg_svd, one block at a time (svd.cpp:57-62).'''
     factors = []
     driver = PER_BLOCK_SVD_DRIVER if arranged.device.type == 'cuda' else None
     for i, key in present:
         u, sv, vh = torch.linalg.svd(arranged._view(i), full_matrices = False, driver = driver)
         factors.append([key, u, sv, vh, 0, 0])
+    if while_waiting is not None:
+        while_waiting()
     host = torch.cat([f[2] for f in factors]).to('cpu', torch.float64).tolist() if factors else []
     return factors, host, None
 
 
-def _factor_blocks(arranged: Tensor):
+def _factor_blocks(arranged: Tensor, while_waiting = None):
     """The thin SVD of every non-empty block.  float64 blocks on the GPU go through one launch of
     the engine's Jacobi SVD (tt_svd_blocks), complex blocks, blocks beyond its size and the
     per-block comparison form through at::linalg_svd one block at a time, as svd.cpp:57-62 does.
@@ -528,7 +544,7 @@ def _factor_blocks(arranged: Tensor):
     batched = (arranged.dtype == torch.float64 and arranged.device.type == 'cuda' and _precision != PER_BLOCK and
                all(min(space.shapes[i]) <= 1024 for i, _ in present))
     if not batched:
-        return _factor_blocks_per_block(arranged, present)
+        return _factor_blocks_per_block(arranged, present, while_waiting)
     dims, count = ints64(x for i, _ in present for x in space.shapes[i])
     places, total = (i64 * max(len(present), 1))(), i64()
     check(lib.tt_svd_workspace(len(present), dims, places, ctypes.byref(total)))
@@ -562,19 +578,21 @@ def _factor_blocks(arranged: Tensor):
     return factors, None, (u, sv, vh, info[:max(len(present), 1)], s_at, present)
 
 
-def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
+def _split_over(tensor: Tensor, left, max_bond, tol, absorb, while_waiting = None):
     '''tentorch/linalg/graded/svd.cpp:41-177: the SVD of every block, the global ranking of the
     singular values, truncation and the +-q pairing of the bond (on the device for the engine's
-    batched SVD: one read of each block's kept count), then the two factors.'''
+    batched SVD: one read of each block's kept count), then the two factors.  `while_waiting`, when
+    given, runs on the host once the split's device work is queued and before the split reads its
+    results (host work of the caller's that needs no device result: it overlaps the SVD).'''
     if absorb not in (0, 1, 2, 3):
         raise ValueError(f'absorb has to be 0, 1, 2 or 3, got {absorb}')
     if max_bond is not None and max_bond < 1:
         raise ValueError(f'a bond needs at least one multiplet, got {max_bond}')
     arranged = tensor.place(left) if left is not None else tensor
     cat = arranged.cat
-    factors, host, packed = _factor_blocks(arranged)
+    factors, host, packed = _factor_blocks(arranged, while_waiting)
     if packed is not None:
-        ranked = _rank_on_device(arranged, factors, packed, max_bond, tol)
+        ranked = _rank_on_device(arranged, factors, packed, max_bond, tol, while_waiting)
         if ranked is None:
             # a block the Jacobi sweeps did not settle within their cap: this split's blocks go
             # through cuSOLVER one by one instead (QR iteration, gesvd), as the per-block form runs them
@@ -593,7 +611,7 @@ def _split_over(tensor: Tensor, left, max_bond, tol, absorb):
     return _split_finish(arranged, factors, packed, multiplicities, absorb)
 
 
-def _rank_on_device(arranged: Tensor, factors, packed, max_bond, tol):
+def _rank_on_device(arranged: Tensor, factors, packed, max_bond, tol, while_waiting = None):
     '''The ranking of the split's singular values on the device (tt_svd_rank): per block the values
     it keeps, read with the SVD's sweep counts in one wait.  Returns the bond's multiplets per
     domain sector (the blocks' f[4] set), or None when a block's Jacobi sweeps did not settle.
@@ -616,7 +634,11 @@ def _rank_on_device(arranged: Tensor, factors, packed, max_bond, tol):
         check(lib.tt_svd_rank(sv.data_ptr(), s_at, dev.data_ptr(), dev.data_ptr() + 4 * nb, nb, dev.data_ptr() + 8 * nb, ns,
                               float(tol), -1 if max_bond is None else int(max_bond), kept.data_ptr(), stream))
     except ValueError:
+        if while_waiting is not None:
+            while_waiting()
         return _rank_on_host(factors, sv[:s_at].cpu().tolist(), info, max_bond, tol, cat)
+    if while_waiting is not None:
+        while_waiting()
     both = torch.cat([info.to(torch.int32), kept]).cpu()
     if present and int(both[:info.numel()].min()) < 0:
         return None

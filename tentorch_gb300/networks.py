@@ -16,10 +16,11 @@ import numpy as np
 import torch
 
 from tentorch_gb300.lanczos import lanczos, lanczos_einsum
-from tentorch_gb300.linalg import contract, einsum, inner, inner_device, precision, qr, rq, svd
+from tentorch_gb300.linalg import (_split_over, conj_plan, contract, contract_plan, einsum, einsum_plan, inner,
+                                   inner_device, place_plan, precision, qr, rq)
 from tentorch_gb300.symmetry import (AbelianGroup, FusionCategory, FusionTree, Leg, NoSymmetry, fusion_trees,
                                      reachable_charges, u1)
-from tentorch_gb300.tensor import BlockKey, Tensor, block_keys, domain_legs
+from tentorch_gb300.tensor import BlockKey, Space, Tensor, block_keys, domain_legs
 
 # ---------------------------------------------------------------------------------------------
 # entry-by-entry tensors (tentorch/tensors/tree.py)
@@ -375,6 +376,7 @@ class DMRG:
         normalised there: the window's only host wait is the split's read of its singular values.'''
         at = self.center
         first, second = self.state.tensors[at], self.state.tensors[at + 1]
+        bond = second.codomain[0]  # the bond the split replaces
         two = contract(first, second, domain_legs(first), [0])
         site, following = self.operator.tensors[at], self.operator.tensors[at + 1]
         head = einsum('EIa,IPqj->EPaqj', self.left[at], site)
@@ -393,12 +395,49 @@ class DMRG:
             energy = (inner_device(vector, image) / inner_device(vector, vector)).real
             self.matvecs += 1
         factor = 2 if direction == 'right' else 1
-        left, values, right = svd(vector, self.max_bond_dim, self.svd_tol, factor)
+        # svd(vector, max_bond, tol, factor), compiling what follows while the split runs
+        left, values, right = _split_over(vector, None, self.max_bond_dim, self.svd_tol, factor,
+                                          lambda: self._compile_ahead(at, direction, vector._space, bond))
         self.state.tensors[at], self.state.tensors[at + 1] = left, right.place([0, 1])
         self.center = at + 1 if direction == 'right' else at
         centre = self.state.tensors[self.center]._data
         centre.div_(torch.linalg.vector_norm(centre))
         return energy, 1.0 - torch.sum(values * values).real
+
+    def _compile_ahead(self, at: int, direction: str, theta: Space, bond: Leg) -> None:
+        '''Compile, while the split of window `at` runs on the device, the plans of what follows it
+        (the right factor's leg move, the environment update, the next window's contraction, head,
+        tail and matvec) for the shapes they get when the split keeps the bond it replaces: near
+        convergence a DMRG bond keeps its multiplets from sweep to sweep, and the calls then find
+        their plans compiled.  A bond that changed compiles its own plans when the calls run; a
+        predicted shape the engine refuses is left to them.'''
+        cat, ops = theta.cat, self.operator.tensors
+        domain = lambda space: list(range(len(space.codomain), len(space.codomain) + len(space.domain)))
+        try:
+            first = Space.of(cat, theta.codomain, [bond], theta.qtotal)
+            second = Space.of(cat, [bond], theta.domain, cat.trivial())
+            moved = place_plan(second, [0, 1], [2])
+            placed = moved.out_space if moved.n_ops else second
+            if direction == 'right':
+                if at >= self.L - 2 or at + 3 not in self.right:
+                    return
+                env = einsum_plan('EIa,Feq,aPb,IqPj->FJb', [self.left[at]._space, conj_plan(first).out_space, first,
+                                                            ops[at]._space]).out_space
+                two = contract_plan(placed, self.state.tensors[at + 2]._space, domain(placed), [0]).out_space
+                head = einsum_plan('EIa,IPqj->EPaqj', [env, ops[at + 1]._space]).out_space
+                tail = einsum_plan('JRsk,Fkb->JRSFb', [ops[at + 2]._space, self.right[at + 3]._space]).out_space
+            else:
+                if at <= 0 or at - 1 not in self.left or at + 2 not in self.right:
+                    return
+                env = einsum_plan('Gfq,aPb,IqPk,Gkb->FIa', [conj_plan(placed).out_space, placed, ops[at + 1]._space,
+                                                            self.right[at + 2]._space]).out_space
+                before = self.state.tensors[at - 1]._space
+                two = contract_plan(before, first, domain(before), [0]).out_space
+                head = einsum_plan('EIa,IPqj->EPaqj', [self.left[at - 1]._space, ops[at - 1]._space]).out_space
+                tail = einsum_plan('JRsk,Fkb->JRSFb', [ops[at]._space, env]).out_space
+            einsum_plan('EPaqj,JRSFb,AQsb->EPrf', [head, tail, two])
+        except ValueError:
+            pass
 
     def sweep(self) -> tuple[float, float]:
         '''tentorch/algorithms/dmrg.py:131-161'''

@@ -200,3 +200,45 @@ def test_three_slice_sweeps_report_fp64_rayleigh_quotients():
         energy, _ = driver.sweep()
         assert abs(energy - want['energy']) < 1e-5, (energy, want['energy'])
     assert energy > golden['exact'] - 1e-10
+
+
+def test_windows_find_their_matvec_plans_compiled_during_the_previous_split(monkeypatch):
+    '''Near convergence a window's bond keeps its multiplets, so the matvec plan of each window but
+    the first of a half-sweep is compiled while the previous window's split runs (DMRG._compile_ahead),
+    and the sweep's energy matches a sweep from the same state that compiles every plan in its call.'''
+    from tentorch_gb300 import linalg as la
+    driver = _driver(16, 32, n_iter = 5)
+    for _ in range(6):
+        driver.sweep()
+    state = ([t.clone() for t in driver.state.tensors], driver.state.center)
+    matvec = 'EPaqj,JRSFb,AQsb->EPrf'
+    misses = {'ahead': 0, 'call': 0}
+    inside = [False]
+    real_plan, real_ahead = la._plan, nw.DMRG._compile_ahead
+
+    def counting(key, build, cat):
+        if key not in la._plans and key[0] == 'einsum' and key[1] == matvec:
+            misses['ahead' if inside[0] else 'call'] += 1
+        return real_plan(key, build, cat)
+
+    def ahead(self, *args):
+        inside[0] = True
+        try:
+            real_ahead(self, *args)
+        finally:
+            inside[0] = False
+
+    monkeypatch.setattr(la, '_plan', counting)
+    monkeypatch.setattr(nw.DMRG, '_compile_ahead', ahead)
+    la.clear_plans()
+    energy, _ = driver.sweep()
+    # the right half-sweep meets every window's shapes first; a window whose bond changed, and the
+    # first window, compile in the call
+    assert misses['ahead'] >= driver.L // 2 and misses['ahead'] >= misses['call'], misses
+
+    monkeypatch.setattr(nw.DMRG, '_compile_ahead', lambda self, *args: None)
+    driver.state.tensors = [t.clone() for t in state[0]]
+    driver.state.center = state[1]
+    la.clear_plans()
+    plain, _ = driver.sweep()
+    assert abs(energy - plain) < ENERGY_TOL, (energy, plain)
