@@ -214,3 +214,26 @@ def test_gemm_tickets_are_left_zero_in_the_workspace():
     stream = torch.cuda.current_stream().cuda_stream
     pool = la._pools[(torch.cuda.current_device(), stream, torch.float64)]
     assert int(torch.count_nonzero(pool[:8192]).item()) == 0
+
+
+@pytest.mark.parametrize('slices, tol', [(0, TOL), (6, 1000 * 2.0 ** -42)])
+def test_full_size_matvec_is_linear(slices, tol):
+    '''The matvec at the largest bond of the DMRG workloads (chi = 1024, 562,412 entries a vector;
+    beyond what the oracle builds within a test's time) through a size-independent property: the
+    image of 2x + 3y is 2 Hx + 3 Hy, in FP64 to round-off and in six slices within ten times the
+    split's bound on each of the three images (relative to the largest entry).'''
+    import bench
+    head, tail, x = bench.matvec_operands(tg, torch, 'cuda', 1024, 31)
+    y = x.clone()
+    gen = torch.Generator().manual_seed(32)
+    for block in y.to_tuple()[3].values():
+        block.copy_(torch.randn(block.shape, dtype = torch.float64, generator = gen))
+    z = x * 2.0
+    z += y * 3.0
+    with tg.precision(slices):
+        hx, hy, hz = (tg.einsum(orc.MATVEC, head, tail, v) for v in (x, y, z))
+    blocks = lambda t: torch.cat([b.flatten() for b in t.to_tuple()[3].values()])
+    want = blocks(hx) * 2.0 + blocks(hy) * 3.0
+    scale = float(want.abs().max())
+    err = float((blocks(hz) - want).abs().max()) / scale
+    assert scale > 0 and err < tol, err
