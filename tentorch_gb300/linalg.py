@@ -158,6 +158,13 @@ def _plan(key, build, cat) -> Plan:
     return plan
 
 
+def _uploaded(values, dtype, device) -> torch.Tensor:
+    '''A small host table on the device without waiting for the stream's queued work: staged
+    through page-locked memory (torch's host cache keeps the staging block until the copy is done),
+    so the copy is queued like a kernel and the host returns at once.'''
+    return torch.tensor(values, dtype = dtype).pin_memory().to(device, non_blocking = True)
+
+
 def _check_device(tensors) -> None:
     dtype, device = tensors[0].dtype, tensors[0].device
     for t in tensors:
@@ -562,7 +569,8 @@ def _factor_blocks(arranged: Tensor, while_waiting = None):
     table = [x for e in entries for x in e]
     largest = max((min(e[1], e[2]) for e in entries), default = 0)
     device = arranged.device
-    dev_table = torch.tensor(table, dtype = torch.int64).to(device)
+    # no wait for the stream's queued work (the window's Lanczos): the SVD is queued behind it
+    dev_table = _uploaded(table, torch.int64, device)
     u = torch.empty(max(u_at, 1), dtype = torch.float64, device = device)
     sv = torch.empty(max(s_at, 1), dtype = torch.float64, device = device)
     vh = torch.empty(max(vh_at, 1), dtype = torch.float64, device = device)
@@ -626,7 +634,7 @@ def _rank_on_device(arranged: Tensor, factors, packed, max_bond, tol, while_wait
     table = ([f[2][1] for f in factors] + [ids[f[0].domain] for f in factors] +
              [ids[cat.dual(sector)] for sector in sectors])
     device = arranged.device
-    dev = torch.tensor(table, dtype = torch.int32).to(device, non_blocking = True)
+    dev = _uploaded(table, torch.int32, device)
     kept = torch.zeros(len(factors), dtype = torch.int32, device = device)
     nb, ns = len(factors), len(sectors)
     stream = torch.cuda.current_stream(device).cuda_stream
