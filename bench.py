@@ -286,7 +286,7 @@ def launches_of(kind, precision):
 
 def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms = None):
     """The two-site DMRG of the U(1) Heisenberg chain (tentorch/algorithms/dmrg.py) timed per sweep
-    in three forms from one FP64 state: `warm` FP64 sweeps grow the bond to chi, then each form
+    in each form from one FP64 state: `warm` FP64 sweeps grow the bond to chi, then each form
     runs one sweep from a copy of that state, with the plan caches cleared first so that every
     form compiles its plans inside its sweep, and then the next sweep of its run with the plans
     kept (`s_per_sweep_continued`: the steady state of a long run, where the shapes recur).  Forms: split (grouped kernels, the Lanczos matvec in
