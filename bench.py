@@ -290,12 +290,13 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
     runs one sweep from a copy of that state, with the plan caches cleared first so that every
     form compiles its plans inside its sweep, and then the next sweep of its run with the plans
     kept (`s_per_sweep_continued`: the steady state of a long run, where the shapes recur).  Forms: split (grouped kernels, the Lanczos matvec in
-    split precision), bf16x3_fp64_ritz (three slices, the window's energy the FP64 Rayleigh
+    split precision), split_all_products_s7 (every block product of the sweep in seven slices),
+    bf16x3_fp64_ritz (three slices, the window's energy the FP64 Rayleigh
     quotient of the Ritz vector), fp64_grouped (the grouped kernels in FP64) and fp64_per_block (one
     cuBLAS call per block pair and one SVD per block, as the reference runs on a CUDA device).  Wall time
-    around the sweep, the device synchronised on both sides.  (Every block product of the sweep in
-    split precision, environments included, is the DMRG object's `all_products` option; at this bond it
-    is slower than the matvec alone in split precision and, at 6 slices, outside the 1e-10 bar.)"""
+    around the sweep, the device synchronised on both sides.  (At six slices every block product in
+    split precision moves the sweep energy by ~2e-10, outside the bar; seven slices carry 2^-7 of
+    that error.)"""
     from tentorch_gb300 import networks as nw
     from tentorch_gb300 import linalg as la
     from tentorch_gb300.linalg import PER_BLOCK, cached_plans, clear_plans
@@ -315,13 +316,17 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
     out = {}
     if forms is None:
         forms = (('fp64_grouped', 0, 'gesvd', False), ('split', precision, 'gesvd', False),
+                 ('split_all_products_s7', 7, 'gesvd', False, True),
                  ('bf16x3_fp64_ritz', 3, 'gesvd', True), ('fp64_per_block', PER_BLOCK, 'gesvd', False),
                  ('fp64_per_block_default_svd', PER_BLOCK, None, False))
-    for name, form, svd_driver, refine in forms:
+    for name, form, svd_driver, refine, *options in forms:
         driver.state.tensors = [t.clone() for t in snapshot[0]]
         driver.state.center = snapshot[1]
         driver.precision = form
         driver.refine_energy = refine
+        # every block product of the sweep in split precision (environments, head, tail, the
+        # two-site contraction), not only the Lanczos matvec
+        driver.all_products = bool(options and options[0])
         la.PER_BLOCK_SVD_DRIVER = svd_driver
         tg.set_precision(PER_BLOCK if form == PER_BLOCK else 0)
         clear_plans()
@@ -337,7 +342,7 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
         out[name] = {'s_per_sweep': elapsed, 'energy': energy, 'energy_fp64_check': check,
                      'discarded': lost, 'matvecs': driver.matvecs - mv0, 'max_bond': max(driver.state.bond_dims),
                      'svd': 'engine Jacobi (batched)' if form != PER_BLOCK else f'torch.linalg.svd per block, driver {svd_driver}',
-                     'refined_energy': refine}
+                     'refined_energy': refine, 'all_products': driver.all_products}
         if golden is not None:
             out[name]['delta_e_vs_reference'] = abs(energy - golden[warm])
         if svd_driver is None:
@@ -362,6 +367,7 @@ def dmrg_sweeps(tg, torch, device, precision, length, chi, n_iter, warm, forms =
         la.PER_BLOCK_SVD_DRIVER = 'gesvd'
         tg.set_precision(0)
     driver.refine_energy = False
+    driver.all_products = False
     tg.set_precision(0)
     clear_plans()
     ref = out['fp64_grouped']['energy']
