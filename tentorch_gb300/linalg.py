@@ -162,6 +162,8 @@ def _uploaded(values, dtype, device) -> torch.Tensor:
     '''A small host table on the device without waiting for the stream's queued work: staged
     through page-locked memory (torch's host cache keeps the staging block until the copy is done),
     so the copy is queued like a kernel and the host returns at once.'''
+    if not values:
+        return torch.empty(0, dtype = dtype, device = device)
     return torch.tensor(values, dtype = dtype).pin_memory().to(device, non_blocking = True)
 
 
