@@ -741,7 +741,7 @@ def _split_finish(arranged: Tensor, factors, packed, multiplicities, absorb):
             count += 1
         if count:
             device = arranged.device
-            dev_table = torch.tensor(table, dtype = torch.int64).to(device)
+            dev_table = _uploaded(table, torch.int64, device)
             stream = torch.cuda.current_stream(device).cuda_stream
             check(lib.tt_svd_keep(count, dev_table.data_ptr(), u.data_ptr(), sv.data_ptr(), vh.data_ptr(),
                                   first._data.data_ptr(), second._data.data_ptr(), values.data_ptr(), stream))
