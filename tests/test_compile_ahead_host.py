@@ -110,3 +110,25 @@ def test_compile_ahead_fills_the_next_windows_plans():
             assert advance_right(right[at + 2], at + 1) is right[at + 1]
             window_plans(at - 1)
         assert la.cached_plans() == ahead, direction
+
+
+def test_compile_ahead_stops_at_the_turns():
+    '''At the last window of each half-sweep there is no next window to compile for: the right
+    half-sweep's last window and the left half-sweep's window at the chain's start compile nothing
+    beyond the right factor's leg move.'''
+    from types import SimpleNamespace
+    from tentorch_gb300 import networks as nw
+    cat, length = tg.u1, 4
+    operator = nw.heisenberg(cat, length, dtype = torch.float64, device = 'cpu')
+    phys = operator.physical
+    bonds = [tg.Leg(cat, [(0,)], [1]), tg.Leg(cat, [(-1,), (1,)], [1, 1]), tg.Leg(cat, [(-2,), (0,), (2,)], [1, 2, 1]),
+             tg.Leg(cat, [(-1,), (1,)], [1, 1]), tg.Leg(cat, [(0,)], [1])]
+    state = [_stand_in(tg.tensor.Space.of(cat, [bonds[at], phys], [bonds[at + 1]], (0,))) for at in range(length)]
+    driver = SimpleNamespace(L = length, operator = operator, state = SimpleNamespace(tensors = state), left = {}, right = {})
+    T = [t._space for t in state]
+    for at, direction in ((length - 2, 'right'), (0, 'left')):
+        la.clear_plans()
+        theta = la.contract_plan(T[at], T[at + 1], [2], [0]).out_space
+        la.clear_plans()
+        nw.DMRG._compile_ahead(driver, at, direction, theta, T[at + 1].codomain[0])
+        assert la.cached_plans() == 1, direction  # the place of the right factor
