@@ -69,3 +69,25 @@ def test_random_windows_compile_to_the_oracles_output_spaces():
         tail, tail_o = outs['JRsk,Fkb->JRSFb']
         plan = la.einsum_plan(orc.MATVEC, [head, tail, two])
         assert _shapes_of_space(plan.out_space) == _shapes_of_oracle(orc.einsum(orc.MATVEC, head_o, tail_o, two_o)), draw
+
+
+def test_random_su2_recouplings_compile_to_the_oracles_output_spaces():
+    '''SU(2) legs of random spins and multiplets through the recoupling einsum of the named config
+    ('ABcd,DCef->ABef': the second operand's codomain read in the other order, an exchange with F
+    and R symbols), an exchange of the domain's legs ('ABcd->ABdc') and bends of a leg across the
+    sides ('ABcd->ABCd', 'ABcd->Abcd'; a label's case names its side): the compiled output spaces
+    against the oracle's.'''
+    rng = random.Random(11)
+    gen = torch.Generator().manual_seed(4)
+    legs = lambda ls: [tg.Leg(tg.su2, list(l.sectors), list(l.multiplicities)) for l in ls]
+    la.clear_plans()
+    for draw in range(8):
+        spins = sorted(rng.sample(range(0, 5), rng.randint(1, 3)))
+        leg_o = orc.Leg(orc.su2, [(j,) for j in spins], [rng.randint(1, 2) for _ in spins])
+        a_o = orc.Tensor(orc.su2, [leg_o, leg_o], [leg_o, leg_o], orc.su2.trivial(), np.float64).fill_random(gen)
+        a = Space.of(tg.su2, legs(a_o.codomain), legs(a_o.domain), a_o.qtotal)
+        for spec in ('ABcd,DCef->ABef', 'ABcd->ABdc', 'ABcd->ABCd', 'ABcd->Abcd'):
+            operands_o = [a_o, a_o] if ',' in spec else [a_o]
+            plan = la.einsum_plan(spec, [a] * len(operands_o))
+            want = orc.einsum(spec, *operands_o)
+            assert _shapes_of_space(plan.out_space) == _shapes_of_oracle(want), (draw, spec, spins)
