@@ -144,12 +144,13 @@ def to_oracle(orc, t):
 # ---------------------------------------------------------------------------------------------
 
 
-def cpu_matvecs(chi, count):
-    '''Time `count` matvecs of the oracle on the host after one untimed call that builds its
-    plans; returns (matvecs/s, seconds, count).'''
+def cpu_matvecs(chi, count, warmup = 1):
+    '''Time `count` matvecs of the oracle on the host after `warmup` untimed ones (the first builds
+    its plans); returns (matvecs/s, seconds, count).'''
     from oracle import engine as orc
     head, tail, theta = orc.matvec_inputs(chi, seed = SEED)
-    orc.einsum(orc.MATVEC, head, tail, theta)
+    for _ in range(max(1, warmup)):
+        orc.einsum(orc.MATVEC, head, tail, theta)
     start = time.perf_counter()
     for _ in range(count):
         orc.einsum(orc.MATVEC, head, tail, theta)
@@ -172,11 +173,13 @@ def cpu_matvecs_one_thread(chi, count):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    count = max(1, min(args.steps, args.cpu_sample))
-    value, elapsed, n = cpu_matvecs(args.chi, count)
+    # the arm's own steps and warm-up, a step one matvec (~0.15 s on the 16 Grace cores: the default
+    # 1000 steps take ~2.5 minutes)
+    count, warm = max(1, args.steps), max(1, args.warmup)
+    value, elapsed, n = cpu_matvecs(args.chi, count, warm)
     cores = os.cpu_count()
     line = {'metric': METRIC, 'value': value, 'unit': 'matvecs/s', 'n_gpus': args.gpus, 'steps': n,
-            'warmup': 1, 'ms_per_step': 1e3 * elapsed / n, 'higher_is_better': True, 'scaling': 'weak',
+            'warmup': warm, 'ms_per_step': 1e3 * elapsed / n, 'higher_is_better': True, 'scaling': 'weak',
             'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
             'config': config(args, 0),
             'cpu_baseline': {'value': value, 'unit': 'matvecs/s', 'cores': cores, 'kind': 'port',
