@@ -426,7 +426,6 @@ namespace ttg
     return std::tie(sectors, inner, copies, coupled) < std::tie(o.sectors, o.inner, o.copies, o.coupled);
   }
 
-  // tentorch/symmetry/tree/tree.cpp:375-398
   namespace
   {
     // Hashes and key checks of the per-leg-list caches below, computed in place (no key is
@@ -465,8 +464,9 @@ namespace ttg
     };
   } // namespace
 
-  // The charges the legs fuse to, in the order a fusion from the first leg meets them; kept per
-  // list of legs (every space and every einsum's output check asks for them).
+  // tentorch/symmetry/tree/tree.cpp:375-398: the charges the legs fuse to, in the order a fusion
+  // from the first leg meets them; kept per list of legs (every space and every einsum's output
+  // check asks for them).
   std::vector<Sector> reachable_charges(const Category &cat, const std::vector<Leg> &legs)
   {
     static std::unordered_map<uint64_t, std::vector<ChargesEntry>> cache;
